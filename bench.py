@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""GB300 benchmark of the many-lights GI hot path (RSM -> VPLs -> ISM splat -> pull-push -> FG).
+
+One step = one GI frame of the workload (default: 1920x1080, 1024 VPLs, 2^22 points, 4096^2 ISM
+atlas of 128^2 ISMs, 6 pull-push levels, interleave 8, 16x16 same-class tiles with culling):
+mlgi_gi_frame on inputs resident in HBM (`value`), and mlgi_gi_frame_host from pinned host
+buffers with every input copied in and the radiance copied out per step (`e2e`).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2_1920x1080_n1024]
+    python bench.py --impl reference ...   # the CPU implementation of the path, all host cores
+
+Prints one JSON line on rank 0. Multi-GPU (torchrun) runs independent replicas (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "many-lights-gi_gb300")]
+
+METRIC = "1080p GI ms/frame"
+UNIT = "ms/frame"
+PASSES = ["vpl_process", "ism_clear", "ism_splat", "pullpush", "final_gather"]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="mlgi", choices=["mlgi", "reference"])
+    ap.add_argument("--config", default="c2_1920x1080_n1024")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---- algorithmic bytes per pass (one launch each per frame) -------------------------------------
+def algorithmic_bytes(cfg, bucket_stride):
+    px = cfg.width * cfg.height
+    nrm = 4 if cfg.reduced else 8
+    atlas = cfg.atlas_w * cfg.atlas_h
+    vrec = 24 if cfg.reduced else 48
+    return {
+        "vpl_process": cfg.n_vpl * (4 + 4 + 4 + 48 + 16),
+        "ism_clear": atlas * 4,
+        "ism_splat": cfg.n_points * 16 + cfg.n_vpl * 4,
+        "pullpush": atlas * (4 + (2 if cfg.reduced else 4)),
+        "final_gather": px * (4 + nrm + 12) + cfg.pairs * (2 if cfg.reduced else 4) + cfg.n_vpl * vrec,
+    }
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    for fn in sorted(os.listdir(os.path.join(ROOT, "profiles"))) if os.path.isdir(os.path.join(ROOT, "profiles")) else []:
+        try:
+            txt = open(os.path.join(ROOT, "profiles", fn)).read()
+        except Exception:
+            continue
+        m = re.search(r"traffic\[" + re.escape(kernel) + r"\]\s*=\s*([0-9.eE+]+)", txt)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---- CPU implementation of the path (the oracle's FP32 restatement, all host threads) -----------
+def cpu_frame_runner(cfg, scene):
+    import numpy as np
+
+    import mlgi
+    from oracle import oracle as O
+
+    perm = mlgi.shuffle_table(cfg.n_vpl)
+
+    def frame():
+        pos, nrm, col, pn = O.vpl_process(scene.rsm_depth, scene.rsm_normal, scene.rsm_diffuse, cfg.n_vpl,
+                                          scene.mat("inv_biased_light_vp"), cfg.light_intensity, 1, perm)
+        keys = O.ism_splat(scene.points, scene.counts, scene.bucket_stride, pos, pn, cfg.n_vpl, cfg.ism_size,
+                           cfg.grid_x, cfg.grid_y, cfg.z_far)
+        fin = O.pullpush(keys, cfg.ism_size, cfg.levels, cfg.z_far)
+        return O.final_gather(scene.gbuf_depth, scene.gbuf_normal, scene.mat("inv_view_proj"), pos, nrm, col, fin,
+                              cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.z_far, cfg.gi_intensity, cfg.clamp_value,
+                              cfg.interleave, tile=cfg.tile if cfg.cull else 0, cutoff=cfg.influence_cutoff)
+
+    return frame, O.max_threads()
+
+
+def time_cpu(cfg, scene, budget_s, min_frames=2):
+    frame, threads = cpu_frame_runner(cfg, scene)
+    frame()  # warm
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < min_frames or time.perf_counter() < t_end:
+        t0 = time.perf_counter()
+        frame()
+        times.append((time.perf_counter() - t0) * 1e3)
+    return statistics.median(times), threads, len(times)
+
+
+def config_dict(cfg):
+    return {"workload": cfg.name, "resolution": f"{cfg.width}x{cfg.height}", "vpls": cfg.n_vpl,
+            "points": cfg.n_points, "rsm": f"{cfg.rsm}x{cfg.rsm}",
+            "ism": f"{cfg.ism_size}^2 x {cfg.grid_x}x{cfg.grid_y} = {cfg.atlas_w}x{cfg.atlas_h}",
+            "pullpush_levels": cfg.levels, "interleave": cfg.interleave, "tile": cfg.tile, "cull": bool(cfg.cull),
+            "precision": "fp16/bf16 storage, fp32 math" if cfg.reduced else "fp32",
+            "scene": "seeded procedural room (100-unit Cornell box, boxes, spheres, spot light)",
+            "l2": "flushed between steps (256 MiB write)"}
+
+
+def run_reference(args, cfg, rank, world):
+    if rank != 0:
+        return
+    import mlgi
+
+    scene = mlgi.make_scene(cfg)
+    frame, threads = cpu_frame_runner(cfg, scene)
+    for _ in range(min(args.warmup, 1)):
+        frame()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        frame()
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = statistics.mean(times)
+    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(cfg),
+            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full frames of {cfg.name}, FP32 oracle restatement of the "
+                                       f"reference shaders, OpenMP on {threads} threads"},
+            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, cfg, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import mlgi
+    from mlgi.device import DeviceFrame, host_frame_desc, pinned_inputs
+
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    scene = mlgi.make_scene(cfg.replace(seed=cfg.seed + rank))
+    ctx = mlgi.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    df = DeviceFrame(scene, dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    fd = df.frame_desc()
+    out = df.radiance()
+    ctx.set_timing(True)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident frames (value) ----
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            ctx.gi_frame(fd, out, ctx.stream())
+        ctx.check_device_status()
+        barrier()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        passes = np.zeros((args.steps, 5))
+        sampler = ClockSampler(local_rank)
+        sampler.start()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            starts[i].record(stream)
+            ctx.gi_frame(fd, out, ctx.stream())
+            ends[i].record(stream)
+            passes[i] = ctx.last_timings()[:5]
+        barrier()
+        wall = time.perf_counter() - t0
+        clocks = sampler.stop()
+        ctx.check_device_status()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+
+    # ---- end to end through the host-buffer C ABI call (e2e) ----
+    pinned = pinned_inputs(scene)
+    hfd = host_frame_desc(scene, pinned)
+    rgb_host = pinned["rgb"].numpy()
+    for _ in range(max(1, args.warmup // 2)):
+        ctx.gi_frame_host(hfd, rgb_host)
+    barrier()
+    e2e_times = []
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ctx.gi_frame_host(hfd, rgb_host)
+        e2e_times.append((time.perf_counter() - t) * 1e3)
+    e2e_total = sum(e2e_times)
+    sizes = mlgi.FrameHostSizes()
+    mlgi.lib().mlgi_frame_host_sizes_get(mlgi.C.byref(hfd), mlgi.C.byref(sizes))
+    h2d = sizes.rsm_depth + sizes.rsm_normal + sizes.rsm_diffuse + sizes.points + sizes.counts + \
+        sizes.gbuf_depth + sizes.gbuf_normal
+    d2h = sizes.radiance
+
+    if world > 1:
+        t = torch.tensor([total_ms, e2e_total], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms, e2e_total = float(t[0]), float(t[1])
+    if rank != 0:
+        ctx.close()
+        return
+
+    frames = args.steps * world
+    value = total_ms / frames
+    mean_pass = passes.mean(axis=0)
+    ab = algorithmic_bytes(cfg, scene.bucket_stride)
+    dom = int(np.argmax(mean_pass))
+    dom_name = PASSES[dom]
+    peak, peak_kind = measured_peak_gbs()
+    achieved = ab[dom_name] / (mean_pass[dom] * 1e-3) / 1e9
+    traffic = ncu_traffic(dom_name)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if not cfg.reduced else "f32 (fp16/bf16 storage)",
+        "data": "synthetic (seeded procedural room)", "config": config_dict(cfg),
+        "gpixel_vpl_per_s": frames * cfg.width * cfg.height * cfg.n_vpl / (total_ms * 1e-3) / 1e9,
+        "evaluated_pairs_per_s": frames * cfg.pairs / (total_ms * 1e-3),
+        "passes_ms": {n: float(v) for n, v in zip(PASSES, mean_pass)},
+        "gpu_launches": 5 * args.steps,
+        "e2e": {"value": e2e_total / frames, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes": ab[dom_name],
+                     "traffic": traffic},
+        "per_kernel_frac": {n: ab[n] / (mean_pass[i] * 1e-3) / 1e9 / peak for i, n in enumerate(PASSES)
+                            if mean_pass[i] > 0},
+        "clocks": clocks,
+        "wall_s": wall,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        ms, threads, nframes = time_cpu(cfg, scene, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{nframes} full {cfg.name} frames (median), FP32 oracle restatement "
+                                          f"of the reference shaders, OpenMP on {threads} threads"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    import mlgi
+
+    cfg = mlgi.CONFIGS[args.config]
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    try:
+        if args.impl == "reference":
+            run_reference(args, cfg, rank, world)
+        else:
+            run_gpu(args, cfg, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,257 @@
+/*
+ * mlgi.h -- C ABI of the GB300 many-lights GI hot path.
+ *
+ * One entry point per painter stage of the reference (paths inside the reference project):
+ *   mlgi_vpl_process   replaces VPLProcessor::process
+ *                      (source/mfs-painters/multiframepainter/VPLProcessor.h:22, VPLProcessor.cpp:73-101)
+ *                      and the compute pass data/shaders/gi/vpl_processor.comp:41-72
+ *   mlgi_ism_splat     replaces ImperfectShadowmap::render's compute path
+ *                      (ImperfectShadowmap.cpp:194-261: atlas clear :212, dispatch of ism.comp :257)
+ *                      and data/shaders/ism/ism.comp:54-139
+ *   mlgi_pullpush      replaces ImperfectShadowmap::pullpush (ImperfectShadowmap.cpp:121-182)
+ *                      and data/shaders/ism/pull.comp:20-126 + push.comp:44-165
+ *   mlgi_final_gather  replaces GIStage::compute_final_gathering (GIStage.h:66, GIStage.cpp:261-306)
+ *                      and data/shaders/gi/final_gathering.comp:63-135
+ *   mlgi_gi_frame      replaces GIStage::process's GI chain (GIStage.cpp:346-418: VPLP, ISM, FG)
+ *
+ * Conventions
+ *   - The caller owns every buffer passed in; the library never frees them. A context owns its
+ *     scratch space (pull-push pyramid, frame-level VPL buffers and atlas, shuffle tables).
+ *   - Every call returns an mlgi_status; mlgi_last_error() gives the detail of the last failure.
+ *   - Device calls are asynchronous on the given stream (NULL = the context's own stream).
+ *   - A context is thread-compatible (one thread at a time); separate contexts are thread-safe.
+ *   - Pointers marked "device" must be device memory of the context's GPU; "host" pointers are
+ *     ordinary (preferably pinned) host memory.
+ */
+#ifndef MLGI_H
+#define MLGI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t mlgi_status;
+#define MLGI_OK 0
+#define MLGI_EINVAL 1      /* bad argument or unsupported configuration */
+#define MLGI_ENOMEM 2      /* device or host allocation failed, or admission over budget */
+#define MLGI_ETIMEDOUT 3   /* a bounded device-side wait gave up */
+#define MLGI_ECUDA 4       /* a CUDA runtime call failed */
+#define MLGI_ECANCELED 5   /* a queued request was cancelled */
+
+typedef struct mlgi_ctx mlgi_ctx;
+typedef void* mlgi_stream; /* a cudaStream_t; NULL selects the context's stream */
+
+/* storage formats */
+#define MLGI_F32 0
+#define MLGI_F16 1
+#define MLGI_BF16 2
+
+typedef struct {
+    int device;          /* CUDA device ordinal */
+    uint32_t flags;      /* reserved, 0 */
+} mlgi_ctx_desc;
+
+mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc);
+void mlgi_destroy(mlgi_ctx* ctx);
+const char* mlgi_last_error(const mlgi_ctx* ctx);
+const char* mlgi_status_string(mlgi_status s);
+/* Default stream of the context (a cudaStream_t). */
+mlgi_stream mlgi_ctx_stream(mlgi_ctx* ctx);
+
+/* ---- VPL processor ------------------------------------------------------------------------ */
+
+/* RSM of the light as RasterizationStage writes it with renderRSM = true
+ * (RasterizationStage.cpp:139-149): device pointers, width*height texels each. */
+typedef struct {
+    int width, height;
+    const float* depth;      /* window depth in [0,1] */
+    const uint32_t* normal;  /* RGB10_A2 UNORM of n*0.5+0.5 (r in bits 0-9) */
+    const uint32_t* diffuse; /* RGBA8 UNORM flux basis (r in bits 0-7) */
+} mlgi_rsm_view;
+
+typedef struct {
+    int count;                      /* N VPLs; a multiple of 64 (one 64-wide group per 64 VPLs) */
+    float light_intensity;          /* GIStage "LightIntensity" */
+    int shuffle;                    /* GIStage "ShuffleLights" */
+    float inv_biased_light_vp[16];  /* inverse(bias * P_light * V_light), column-major */
+} mlgi_vpl_params;
+
+/* VPL buffers (device). `vpl` and `packed` are the reference's vplBuffer and packedVplBuffer
+ * (VPLProcessor.cpp:29-41). `reduced` (optional, may be NULL) receives the reduced-precision
+ * gather record: float pos[3], half normal[3], bfloat16 flux[3] (24 bytes per VPL). */
+typedef struct {
+    int capacity;
+    float* vpl;     /* capacity x 12 floats: pos, pad, normal, pad, flux, pad (48-byte stride) */
+    float* packed;  /* capacity x 4 floats: pos, uintBitsToFloat(pack3SN(normal)) */
+    void* reduced;  /* capacity x 24 bytes, or NULL */
+} mlgi_vpl_buf;
+
+/* VPLProcessor::process: regular RSM sampling into the VPL buffers. */
+mlgi_status mlgi_vpl_process(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi_vpl_params* params,
+                             mlgi_vpl_buf* out, mlgi_stream stream);
+
+/* Host: the fixed VPL shuffle of VPLProcessor.cpp:58-65 (std::iota, std::mt19937(1979982),
+ * std::shuffle) for n entries. */
+mlgi_status mlgi_shuffle_table(int n, int32_t* out_host);
+
+/* ---- imperfect shadow maps ---------------------------------------------------------------- */
+
+/* Bucketed point buffer: the contract the reference's ism.geom:59-69 produces. Bucket b holds
+ * counts[b] points starting at entry b*bucket_stride. Each entry is 4 floats:
+ * xyz position, uintBitsToFloat(packUnorm4x8(vec4(normal*0.5+0.5, radius/25))). */
+typedef struct {
+    const float* points;     /* device */
+    const uint32_t* counts;  /* device, n_buckets entries */
+    int n_buckets;           /* sampledVplCount */
+    int64_t bucket_stride;   /* imageSize(pointBuffer) / sampledVplCount */
+} mlgi_points;
+
+typedef struct {
+    int vpl_start, vpl_end;   /* GIStage VPLStartIndex / VPLEndIndex */
+    int scale_isms;           /* GIStage ScaleISMs */
+    int points_only_scaled;   /* GIStage PointsOnlyToScaledISMs */
+    int ism_size;             /* texels per ISM edge (reference: 2048 / ismIndices1d) */
+    int grid_x, grid_y;       /* ISM tile grid; the atlas is (grid_x*ism_size) x (grid_y*ism_size) */
+    int levels;               /* pull-push levels; ism_size must be divisible by 2^levels */
+    float z_far;              /* light projection far plane */
+} mlgi_ism_params;
+
+typedef struct {
+    int width, height;   /* grid_x*ism_size, grid_y*ism_size */
+    uint32_t* keys;      /* device: softrender keys (uint(depth*2^24) << 8 | radius byte) */
+    void* depth;         /* device: pull-push result (final ISM depth) */
+    int format;          /* MLGI_F32 or MLGI_F16 for `depth` */
+} mlgi_atlas;
+
+/* ImperfectShadowmap::render (compute path): clear keys to 0xFFFFFFFF, splat every bucketed
+ * point into up to 4 of the 16 VPLs cached for its bucket by atomicMin. Bit-exact with the
+ * reference's FP32 arithmetic. */
+mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                           const mlgi_ism_params* params, mlgi_atlas* atlas, mlgi_stream stream);
+
+/* ImperfectShadowmap::pullpush: fill holes of every ISM with the pull-push pyramid and write
+ * atlas->depth. Bit-exact with the reference's FP32 arithmetic for the FP32 format. */
+mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* params, mlgi_stream stream);
+
+/* ---- final gathering ---------------------------------------------------------------------- */
+
+typedef struct {
+    int width, height;
+    const float* depth;   /* device: FP32 window depth */
+    const void* normal;   /* device: octahedral normal, 2 x FP32 or 2 x FP16 per pixel */
+    int normal_format;    /* MLGI_F32 or MLGI_F16 */
+} mlgi_gbuffer_view;
+
+typedef struct {
+    float inv_view_proj[16]; /* viewInverted * projectionInverted, column-major */
+    float z_far;             /* ISM far plane (the light projection's) */
+    float gi_intensity;      /* GIIntensityFactor */
+    float clamp_value;       /* VPLClampingValue */
+    int vpl_count;           /* N */
+    int vpl_start, vpl_end;  /* final_gathering.comp:40-46 */
+    int scale_isms;
+    int ism_size, grid_x, grid_y; /* atlas layout (see mlgi_ism_params) */
+    int interleave;          /* interleaved-sampling factor I (N must be a multiple of I*I) */
+    int shadowing;           /* GIShadowing */
+    int tile;                /* work tile edge in same-class pixels: 8 or 16 (0 selects 16) */
+    int cull;                /* per-tile VPL culling against the tile's world-space bounds */
+    float influence_cutoff;  /* with cull: flux/d^4 contribution below which a VPL is dropped; 0 = off */
+    int vpl_format;          /* MLGI_F32: 48-byte records; MLGI_F16: 24-byte reduced records */
+} mlgi_fg_params;
+
+typedef struct {
+    int width, height;
+    float* rgb;          /* device: width*height*3 floats */
+} mlgi_radiance;
+
+mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* gbuf, const mlgi_vpl_buf* vpls,
+                              const mlgi_atlas* atlas, const mlgi_fg_params* params, mlgi_radiance* out,
+                              mlgi_stream stream);
+
+/* ---- whole GI chain (GIStage::process) ---------------------------------------------------- */
+
+typedef struct {
+    mlgi_rsm_view rsm;
+    mlgi_vpl_params vpl;
+    mlgi_points points;
+    mlgi_ism_params ism;
+    int atlas_format;        /* MLGI_F32 or MLGI_F16 */
+    mlgi_gbuffer_view gbuffer;
+    mlgi_fg_params fg;
+} mlgi_frame_desc;
+
+/* VPL processing -> ISM splat -> pull-push -> final gathering on device buffers; the VPL
+ * buffers and the atlas are context-owned. */
+mlgi_status mlgi_gi_frame(mlgi_ctx* ctx, const mlgi_frame_desc* frame, mlgi_radiance* out, mlgi_stream stream);
+
+/* Sizes of the host buffers mlgi_gi_frame_host reads, in bytes. */
+typedef struct {
+    size_t rsm_depth, rsm_normal, rsm_diffuse;
+    size_t points, counts;
+    size_t gbuf_depth, gbuf_normal;
+    size_t radiance;
+} mlgi_frame_host_sizes;
+mlgi_status mlgi_frame_host_sizes_get(const mlgi_frame_desc* frame, mlgi_frame_host_sizes* sizes);
+
+/* The same chain from HOST buffers: every pointer in `frame` is a host pointer; the call copies
+ * the inputs to context-owned device buffers, runs the chain and copies the radiance back to
+ * `rgb_host` before returning. */
+mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* frame, float* rgb_host);
+
+/* Per-pass device times (ms) of the last mlgi_gi_frame / mlgi_gi_frame_host call when timing is
+ * enabled, named after the reference's PerfCounter passes:
+ * [0] VPLP, [1] ISM clear, [2] ISM CS (splat), [3] pull-push, [4] FG, [5] H2D, [6] D2H.
+ * Reading them synchronises the context's stream. */
+mlgi_status mlgi_set_timing(mlgi_ctx* ctx, int enabled);
+mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n);
+
+/* Synchronise `stream` and report device-side errors recorded since the last check
+ * (MLGI_ETIMEDOUT when a bounded wait inside a kernel gave up). Clears the error word. */
+mlgi_status mlgi_check_device_status(mlgi_ctx* ctx, mlgi_stream stream);
+
+/* ---- scene fixture (host) ----------------------------------------------------------------- */
+
+/* Seeded Cornell-style room: a 100 x 100 x 100 world-unit box (1 unit = 1 cm) with floor,
+ * ceiling, back, left and right walls, n_boxes axis-aligned boxes and n_spheres spheres, a
+ * ceiling spot light with a 60 degree cone and a pinhole camera. Stands in for the reference's
+ * model loading and rasterisation stages, which are graphics-API code. */
+typedef struct {
+    uint64_t seed;
+    int n_boxes, n_spheres;
+    int width, height;          /* camera G-buffer */
+    int rsm_width, rsm_height;  /* light RSM */
+    int64_t n_points;           /* surface points, area-uniform */
+    int n_buckets;              /* point buckets (sampledVplCount), round-robin assignment */
+    int ism_count;              /* ISMs, for the sqrt(ismCount) point-radius boost (ism.geom:63) */
+    float light_yaw_deg, light_pitch_deg;  /* jitter of the spot light direction */
+    float camera_orbit_deg;     /* camera orbit around the room's vertical axis */
+    float z_near, z_far;
+} mlgi_scene_desc;
+
+typedef struct {
+    float view[16], proj[16], inv_view_proj[16];               /* camera, column-major */
+    float light_view[16], light_proj[16], inv_biased_light_vp[16];
+    float eye[3], light_pos[3], light_dir[3];
+    float z_near, z_far;
+    float total_area, point_radius;                            /* world units */
+    int64_t bucket_stride;
+} mlgi_scene_info;
+
+/* Fill the host buffers that are not NULL:
+ *   gbuf_depth  width*height floats         gbuf_normal width*height*2 floats (octahedral)
+ *   gbuf_albedo width*height RGBA8 words
+ *   rsm_depth   rsm_width*rsm_height floats rsm_normal / rsm_diffuse rsm_width*rsm_height words
+ *   points      n_buckets*bucket_stride*4 floats; counts n_buckets words
+ * bucket_stride = ceil(n_points / n_buckets). Runs on all host threads. */
+mlgi_status mlgi_scene_generate(const mlgi_scene_desc* desc, mlgi_scene_info* info, float* gbuf_depth,
+                                float* gbuf_normal, uint32_t* gbuf_albedo, float* rsm_depth, uint32_t* rsm_normal,
+                                uint32_t* rsm_diffuse, float* points, uint32_t* counts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MLGI_H */

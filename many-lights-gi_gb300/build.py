@@ -1,0 +1,93 @@
+"""Build libmlgi.so (CUDA kernels for sm_103a + C ABI + host scene fixture) in-tree.
+
+The library lands in many-lights-gi_gb300/_build/libmlgi.so. Translation units compile in
+parallel; the VPL/ISM/pull-push unit is built with -fmad=false so its FP32 arithmetic matches
+the reference shaders word for word.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libmlgi.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp",
+               f"-I{INCLUDE}", f"-I{os.path.join(HERE, 'csrc')}"]
+CUDA_UNITS = [
+    ("csrc/ism_kernels.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
+    ("csrc/fg_kernels.cu", []),
+    ("csrc/mlgi_api.cu", []),
+    ("csrc/batch.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
+    ("host/serve.cpp", []),
+    ("host/autotune.cpp", []),
+]
+HOST_UNITS = [("host/scene.cpp", ["-O3", "-fopenmp", "-fPIC", "-std=c++17", f"-I{INCLUDE}"])]
+DEPS = ["csrc/gi_device.cuh", "csrc/kernels.h", "host/serve.h"]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+    return r.stdout
+
+
+def _sources():
+    units = [(u, f) for u, f in CUDA_UNITS if os.path.exists(os.path.join(HERE, u))]
+    return units
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    paths = [os.path.join(HERE, u) for u, _ in _sources() + HOST_UNITS] + [os.path.join(HERE, d) for d in DEPS]
+    paths += [os.path.join(INCLUDE, "mlgi.h"), os.path.abspath(__file__)]
+    return any(os.path.exists(p) and os.path.getmtime(p) > t for p in paths)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile and link libmlgi.so if any source changed; return its path."""
+    if not force and not _stale():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    jobs = []
+    for unit, flags in _sources():
+        src = os.path.join(HERE, unit)
+        obj = os.path.join(BUILD, os.path.basename(unit) + ".o")
+        if unit.endswith(".cu"):
+            cmd = [nvcc()] + ARCH + NVCC_COMMON + flags + ["-c", src, "-o", obj]
+        else:  # host C++ compiled by nvcc's host compiler with the CUDA include path
+            cmd = [nvcc()] + NVCC_COMMON + flags + ["-x", "cu", "-c", src, "-o", obj] + ARCH
+        jobs.append((cmd, obj))
+    for unit, flags in HOST_UNITS:
+        src = os.path.join(HERE, unit)
+        obj = os.path.join(BUILD, os.path.basename(unit) + ".o")
+        jobs.append((["g++"] + flags + ["-c", src, "-o", obj], obj))
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+        outs = list(ex.map(lambda j: _run(j[0]), jobs))
+    if verbose:
+        for o in outs:
+            sys.stdout.write(o)
+    objs = [o for _, o in jobs]
+    tmp = LIB + ".tmp"
+    _run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fopenmp", "-lgomp", "-lpthread"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

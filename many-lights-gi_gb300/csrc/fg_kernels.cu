@@ -1,0 +1,377 @@
+// Final gathering: interleaved-sampling VPL accumulation with ISM visibility
+// (data/shaders/gi/final_gathering.comp:63-135, dispatched by GIStage::compute_final_gathering,
+// GIStage.cpp:261-306).
+//
+// Work mapping. Pixel (x, y) belongs to interleave class c = (x % I) + (y % I) * I and gathers
+// the class's VPL slice [c*N/I^2, (c+1)*N/I^2). A block is a T x T tile of one class in the
+// de-interleaved sub-image (pixels (i*I + cx, j*I + cy)), so every thread of a block walks the
+// same VPL list and reads each VPL from shared memory as a broadcast. The slice is staged with
+// a 1-D bulk TMA copy (cp.async.bulk) completed on an mbarrier whose wait is bounded; per-VPL
+// derived data (lookAtRH rows, ISM tile origin) is computed once per block. With culling on,
+// the block reduces its pixels' world-space bounding box and drops VPLs whose front half-space
+// misses the box (lossless: those pairs have a zero angle factor) and, when an influence cutoff
+// is given, VPLs farther from the box than (maxflux / cutoff)^(1/4) (lossy, error stated).
+// Accumulation order is ascending VPL index for every pixel, so results are deterministic.
+#include <cuda_runtime.h>
+
+#include "gi_device.cuh"
+#include "kernels.h"
+
+namespace mlgi {
+
+constexpr int kMaxVplChunk = 128;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// Bounded wait on an mbarrier phase: gives up after ~2^31 SM cycles (about a second) and
+// returns false, so a lost transfer can never hang the GPU.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > (1ll << 31)) return false;
+    }
+}
+
+template <bool kReduced>
+__device__ __forceinline__ void decode_vpl(const unsigned char* rec, v3& p, v3& n, v3& f) {
+    if (!kReduced) {
+        const float4* r = reinterpret_cast<const float4*>(rec);
+        const float4 a = r[0], b = r[1], c = r[2];
+        p = mk(a.x, a.y, a.z);
+        n = mk(b.x, b.y, b.z);
+        f = mk(c.x, c.y, c.z);
+    } else {
+        const uint2* r = reinterpret_cast<const uint2*>(rec);
+        const uint2 a = r[0], b = r[1], c = r[2];
+        p = mk(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(b.x));
+        n = mk(__half2float(__ushort_as_half((unsigned short)(b.y & 0xFFFFu))),
+               __half2float(__ushort_as_half((unsigned short)(b.y >> 16))),
+               __half2float(__ushort_as_half((unsigned short)(c.x & 0xFFFFu))));
+        f = mk(__bfloat162float(__ushort_as_bfloat16((unsigned short)(c.x >> 16))),
+               __bfloat162float(__ushort_as_bfloat16((unsigned short)(c.y & 0xFFFFu))),
+               __bfloat162float(__ushort_as_bfloat16((unsigned short)(c.y >> 16))));
+    }
+}
+
+// ---- compensated ("double-float") arithmetic for the world-position reconstruction ----------
+// inv_vp * ndc followed by the w divide cancels badly near the far plane (w is a small difference
+// of two ~0.5 terms), which makes a plain FP32 evaluation drift ~1e-4 world units from the exact
+// value -- enough to flip the clamped 1/d^4 term of near-coplanar VPLs. Each quantity is kept as an
+// unevaluated sum hi + lo using the error-free transformations TwoSum (Knuth) and TwoProduct via
+// FMA (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 2005); the
+// result is rounded once to FP32. Intrinsics keep the compiler from contracting or reordering.
+struct df {
+    float hi, lo;
+};
+__device__ __forceinline__ df two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+    const df s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+    const float p = __fmul_rn(a.hi, b);
+    const float e = __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p));
+    return fast_two_sum(p, e);
+}
+// a / b rounded to FP32 from double-float operands: one Newton correction of the FP32 quotient.
+__device__ __forceinline__ float df_div(df a, df b) {
+    const float q = __fdiv_rn(a.hi, b.hi);
+    // r = a - q*b: the FMA remainder a.hi - q*b.hi is exact; add the low-order parts
+    const float r = __fadd_rn(__fmaf_rn(-q, b.hi, a.hi), __fmaf_rn(-q, b.lo, a.lo));
+    return __fadd_rn(q, __fdiv_rn(r, b.hi));
+}
+// 2*k/n - 1 as double-float (k, n small integers): the pixel-corner NDC coordinate.
+__device__ __forceinline__ df ndc_coord(int k, int n) {
+    const float fk = float(k), fn = float(n);
+    const float q = __fdiv_rn(fk, fn);
+    const float ql = __fdiv_rn(__fmaf_rn(-q, fn, fk), fn);
+    const df t = two_sum(__fmul_rn(q, 2.0f), -1.0f);
+    return fast_two_sum(t.hi, __fadd_rn(t.lo, __fmul_rn(ql, 2.0f)));
+}
+// world = (inv_vp * (ndc, 1)).xyz / w, each row summed in double-float.
+__device__ __forceinline__ v3 reconstruct_world(const float* m, int x, int y, int w, int h, float d) {
+    const df nx = ndc_coord(x, w), ny = ndc_coord(y, h);
+    const df nz = two_sum(__fmul_rn(d, 2.0f), -1.0f);
+    df r[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        df acc = df_mul_f(nx, m[k]);
+        acc = df_add(acc, df_mul_f(ny, m[4 + k]));
+        acc = df_add(acc, df_mul_f(nz, m[8 + k]));
+        acc = df_add(acc, df{m[12 + k], 0.0f});
+        r[k] = acc;
+    }
+    return mk(df_div(r[0], r[3]), df_div(r[1], r[3]), df_div(r[2], r[3]));
+}
+
+__device__ __forceinline__ v3 oct_decode(float ex, float ey) {
+    v3 n = mk(ex, ey, 1.0f - fabsf(ex) - fabsf(ey));
+    if (n.z < 0.f) {
+        const float sx = ex >= 0.f ? 1.f : -1.f, sy = ey >= 0.f ? 1.f : -1.f;
+        n.x = (1.0f - fabsf(ey)) * sx;
+        n.y = (1.0f - fabsf(ex)) * sy;
+    }
+    return normalize(n);
+}
+
+template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16>
+__global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
+    constexpr int NT = T * T;
+    constexpr int kRec = kReduced ? 24 : 48;
+    __shared__ __align__(128) unsigned char s_raw[kMaxVplChunk * 48];
+    __shared__ float4 s_a[kMaxVplChunk], s_b[kMaxVplChunk], s_c[kMaxVplChunk], s_d[kMaxVplChunk];
+    __shared__ int s_list[kMaxVplChunk];
+    __shared__ unsigned char s_flag[kMaxVplChunk];
+    __shared__ float s_box[6][NT / 32];
+    __shared__ int s_n;
+    __shared__ __align__(8) uint64_t s_bar;
+
+    const int tid = threadIdx.x;
+    const int I = a.interleave;
+    const int c = blockIdx.y;
+    const int cx = c % I, cy = c / I;
+    const int sw = (a.width + I - 1) / I;
+    const int ntx = (sw + T - 1) / T;
+    const int tix = blockIdx.x % ntx, tiy = blockIdx.x / ntx;
+    const int x = (tix * T + tid % T) * I + cx;
+    const int y = (tiy * T + tid / T) * I + cy;
+    const bool valid = x < a.width && y < a.height;
+
+    // ---- pixel setup: world position from depth (final_gathering.comp:70-76, evaluated with
+    // compensated arithmetic) and the octahedral normal ----
+    v3 fw = mk(0.f, 0.f, 0.f), fn = mk(0.f, 0.f, 1.f);
+    if (valid) {
+        const size_t pix = (size_t)y * a.width + x;
+        const float d = __ldg(a.depth + pix);
+        fw = reconstruct_world(a.inv_vp, x, y, a.width, a.height, d);
+        float ex, ey;
+        if (kNormalF16) {
+            const __half2 h = reinterpret_cast<const __half2*>(a.normal)[pix];
+            ex = __low2float(h);
+            ey = __high2float(h);
+        } else {
+            const float2 e = reinterpret_cast<const float2*>(a.normal)[pix];
+            ex = e.x;
+            ey = e.y;
+        }
+        fn = oct_decode(ex, ey);
+    }
+
+    // ---- per-tile bounds for culling ----
+    v3 bmin = mk(0.f, 0.f, 0.f), bmax = mk(0.f, 0.f, 0.f);
+    if (a.cull) {
+        const float inf = __int_as_float(0x7f800000);
+        float b[6] = {valid ? fw.x : inf,  valid ? fw.y : inf,  valid ? fw.z : inf,
+                      valid ? -fw.x : inf, valid ? -fw.y : inf, valid ? -fw.z : inf};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) b[k] = fminf(b[k], __shfl_xor_sync(0xffffffffu, b[k], o));
+        }
+        if ((tid & 31) == 0)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s_box[k][tid >> 5] = b[k];
+        __syncthreads();
+        float r[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            r[k] = s_box[k][0];
+            for (int w = 1; w < NT / 32; ++w) r[k] = fminf(r[k], s_box[k][w]);
+        }
+        bmin = mk(r[0], r[1], r[2]);
+        bmax = mk(-r[3], -r[4], -r[5]);
+    }
+
+    if (tid == 0) mbar_init(&s_bar, 1);
+    __syncthreads();
+
+    const int vbase = c * a.per_class;
+    const bool use_tma = ((size_t)vbase * kRec) % 16 == 0;
+    const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
+    const float hs = float(a.ism_size) * 0.5f;
+    const float inv_zfar = 1.0f / a.z_far;
+    uint32_t parity = 0;
+    float accx = 0.f, accy = 0.f, accz = 0.f;
+
+    for (int base = 0; base < a.per_class; base += kMaxVplChunk) {
+        const int cnt = min(kMaxVplChunk, a.per_class - base);
+        const size_t bytes = (size_t)cnt * kRec;
+        if (use_tma && bytes % 16 == 0) {
+            if (tid == 0) {
+                mbar_expect_tx(&s_bar, (uint32_t)bytes);
+                tma_bulk_g2s(s_raw, src + (size_t)(vbase + base) * kRec, (uint32_t)bytes, &s_bar);
+            }
+            const bool ok = __syncthreads_and(mbar_wait(&s_bar, parity));
+            if (!ok) {  // block-uniform: flag the error, give the copy one more bounded wait, leave
+                if (tid == 0) {
+                    atomicOr(a.status, kStatusTmaTimeout);
+                    mbar_wait(&s_bar, parity);
+                }
+                return;
+            }
+            parity ^= 1u;
+        } else {
+            for (size_t k = tid * 4; k < bytes; k += NT * 4)
+                *reinterpret_cast<uint32_t*>(s_raw + k) =
+                    __ldg(reinterpret_cast<const uint32_t*>(src + (size_t)(vbase + base) * kRec + k));
+            __syncthreads();
+        }
+        // derive per-VPL data and the cull flag
+        for (int k = tid; k < cnt; k += NT) {
+            v3 p, n, f;
+            decode_vpl<kReduced>(s_raw + (size_t)k * kRec, p, n, f);
+            v3 s, u;
+            look_at_rows(n, s, u);
+            const int vid = vbase + base + k;
+            const float ismIndex = float(vid) - float(a.ism_index_offset);
+            const int ty = int(ismIndex / float(a.gx));
+            const int tx = int(ismIndex - float(ty) * float(a.gx));
+            s_a[k] = make_float4(p.x, p.y, p.z, f.x);
+            s_b[k] = make_float4(n.x, n.y, n.z, f.y);
+            s_c[k] = make_float4(s.x, s.y, s.z, f.z);
+            s_d[k] = make_float4(u.x, u.y, u.z, __int_as_float((tx * a.ism_size) | ((ty * a.ism_size) << 16)));
+            bool keep = true;
+            if (a.cull) {
+                // front half-space of the VPL against the box corner farthest along its normal
+                const v3 sup = mk(n.x > 0.f ? bmax.x : bmin.x, n.y > 0.f ? bmax.y : bmin.y, n.z > 0.f ? bmax.z : bmin.z);
+                if (dot(n, sup - p) < -1e-3f) keep = false;
+                if (keep && a.influence_cutoff > 0.f) {
+                    const float fl = fmaxf(f.x, fmaxf(f.y, f.z));
+                    const float r = sqrtf(sqrtf(fl / a.influence_cutoff));
+                    const v3 q = mk(fminf(fmaxf(p.x, bmin.x), bmax.x), fminf(fmaxf(p.y, bmin.y), bmax.y),
+                                    fminf(fmaxf(p.z, bmin.z), bmax.z));
+                    const v3 dq = q - p;
+                    if (dot(dq, dq) > r * r) keep = false;
+                }
+            }
+            s_flag[k] = keep ? 1 : 0;
+        }
+        __syncthreads();
+        // order-preserving compaction of the kept indices by warp 0
+        if (tid < 32) {
+            int run = 0;
+            for (int w = 0; w < cnt; w += 32) {
+                const int k = w + tid;
+                const bool keep = k < cnt && s_flag[k];
+                const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+                if (keep) s_list[run + __popc(ballot & ((1u << tid) - 1u))] = k;
+                run += __popc(ballot);
+            }
+            if (tid == 0) s_n = run;
+        }
+        __syncthreads();
+
+        // ---- gather over the kept list (final_gathering.comp:97-130) ----
+        const int nk = s_n;
+        if (valid) {
+            for (int q = 0; q < nk; ++q) {
+                const int k = s_list[q];
+                const float4 A = s_a[k], B = s_b[k];
+                const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                const float inv = rsqrtf(d2);
+                const float ndx = dx * inv, ndy = dy * inv, ndz = dz * inv;
+                const float a1 = B.x * ndx + B.y * ndy + B.z * ndz;
+                const float a2 = -(fn.x * ndx + fn.y * ndy + fn.z * ndz);
+                const float angle = fmaxf(0.f, a1) * fmaxf(0.f, a2);
+                if (angle <= 0.f) continue;
+                const float att = (inv * inv) * (inv * inv);
+                float G = fminf(angle * att, a.clamp_value);
+                if (a.shadowing) {
+                    const float4 C = s_c[k], D = s_d[k];
+                    // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false)
+                    const float rz = __frcp_rn(1.0f + a1);
+                    const float px = (C.x * ndx + C.y * ndy + C.z * ndz) * rz;
+                    const float py = (D.x * ndx + D.y * ndy + D.z * ndz) * rz;
+                    const int org = __float_as_int(D.w);
+                    int ix = __float2int_rd(fmaf(px, hs, hs) + float(org & 0xFFFF));
+                    int iy = __float2int_rd(fmaf(py, hs, hs) + float((unsigned)org >> 16));
+                    if (ix >= a.atlas_w) ix -= a.atlas_w;  // GL_REPEAT
+                    if (ix < 0) ix += a.atlas_w;
+                    if (iy >= a.atlas_h) iy -= a.atlas_h;
+                    if (iy < 0) iy += a.atlas_h;
+                    const size_t t = (size_t)iy * a.atlas_w + ix;
+                    const float occ = kAtlasF16 ? __half2float(__ldg(reinterpret_cast<const __half*>(a.atlas) + t))
+                                                : __ldg(reinterpret_cast<const float*>(a.atlas) + t);
+                    const float vz = (d2 * inv) * inv_zfar;
+                    const float sv0 = 1.0f - (vz - occ);
+                    const float tt = __saturatef((sv0 - 0.98f) * 50.0f);
+                    G *= tt * tt * (3.0f - 2.0f * tt);
+                }
+                accx = fmaf(A.w, G, accx);
+                accy = fmaf(B.w, G, accy);
+                accz = fmaf(s_c[k].w, G, accz);
+            }
+        }
+        __syncthreads();
+    }
+    if (valid) {
+        const size_t pix = (size_t)y * a.width + x;
+        // vec3(acc * giIntensityFactor / vplCount) * interleavedPixels
+        a.out[3 * pix + 0] = accx * a.gi_intensity / a.vpl_count_f * a.i2;
+        a.out[3 * pix + 1] = accy * a.gi_intensity / a.vpl_count_f * a.i2;
+        a.out[3 * pix + 2] = accz * a.gi_intensity / a.vpl_count_f * a.i2;
+    }
+}
+
+template <int T>
+static cudaError_t launch_fg_t(const FgArgs& a, cudaStream_t s) {
+    const int I = a.interleave;
+    const int sw = (a.width + I - 1) / I, sh = (a.height + I - 1) / I;
+    const dim3 grid(((sw + T - 1) / T) * ((sh + T - 1) / T), I * I);
+    const int sel = (a.reduced ? 4 : 0) | (a.atlas_f16 ? 2 : 0) | (a.normal_f16 ? 1 : 0);
+    switch (sel) {
+        case 0: fg_kernel<T, false, false, false><<<grid, T * T, 0, s>>>(a); break;
+        case 1: fg_kernel<T, false, false, true><<<grid, T * T, 0, s>>>(a); break;
+        case 2: fg_kernel<T, false, true, false><<<grid, T * T, 0, s>>>(a); break;
+        case 3: fg_kernel<T, false, true, true><<<grid, T * T, 0, s>>>(a); break;
+        case 4: fg_kernel<T, true, false, false><<<grid, T * T, 0, s>>>(a); break;
+        case 5: fg_kernel<T, true, false, true><<<grid, T * T, 0, s>>>(a); break;
+        case 6: fg_kernel<T, true, true, false><<<grid, T * T, 0, s>>>(a); break;
+        default: fg_kernel<T, true, true, true><<<grid, T * T, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s) {
+    if (a.width <= 0 || a.height <= 0) return cudaSuccess;
+    if (a.tile == 8) return launch_fg_t<8>(a, s);
+    return launch_fg_t<16>(a, s);
+}
+
+}  // namespace mlgi

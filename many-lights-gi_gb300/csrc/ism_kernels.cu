@@ -1,0 +1,427 @@
+// VPL processing, ISM point splat and the fused pull-push pyramid.
+//
+// This translation unit is compiled with -fmad=false and IEEE division/square root so that its
+// FP32 results are word-for-word those of the reference shaders' arithmetic in GLSL order:
+//   vpl_process_kernel  <- data/shaders/gi/vpl_processor.comp:41-72
+//   ism_splat_kernel    <- data/shaders/ism/ism.comp:54-139
+//   pullpush_kernel     <- data/shaders/ism/pull.comp:20-126 and push.comp:44-165, as driven by
+//                          ImperfectShadowmap::pullpush (ImperfectShadowmap.cpp:121-182)
+#include <cuda_runtime.h>
+
+#include "gi_device.cuh"
+#include "kernels.h"
+
+namespace mlgi {
+
+// ---------------------------------------------------------------------------------------------
+// VPL processor: one thread per VPL. Regular RSM sample -> unproject -> flux -> 10:10:10 normal
+// round trip -> optional shuffled slot.
+__global__ void __launch_bounds__(64) vpl_process_kernel(VplArgs a) {
+    const uint32_t idx = blockIdx.x * 64u + threadIdx.x;
+    if (idx >= (uint32_t)a.n) return;
+    const uint32_t tcx = (idx % a.ax) * (uint32_t)a.rsm_w / a.ax;
+    const uint32_t tcy = (idx / a.ax) * (uint32_t)a.rsm_h / a.ay;
+    const float tfx = float(tcx) / float(a.rsm_w);
+    const float tfy = float(tcy) / float(a.rsm_h);
+    v3 diffuse = mk(0.f, 0.f, 0.f);
+    uint32_t nb = 0;
+    float d = 0.f;
+    if (tcx < (uint32_t)a.rsm_w && tcy < (uint32_t)a.rsm_h) {  // texelFetch out of range reads zero
+        const size_t t = (size_t)tcy * a.rsm_w + tcx;
+        const uint32_t dw = __ldg(a.diffuse + t);
+        diffuse = mk(float(dw & 0xFFu) / 255.0f, float((dw >> 8) & 0xFFu) / 255.0f, float((dw >> 16) & 0xFFu) / 255.0f);
+        nb = __ldg(a.normal + t);
+        d = __ldg(a.depth + t);
+    }
+    const v3 normal = mk(float(nb & 0x3FFu) / 1023.0f * 2.0f - 1.0f, float((nb >> 10) & 0x3FFu) / 1023.0f * 2.0f - 1.0f,
+                         float((nb >> 20) & 0x3FFu) / 1023.0f * 2.0f - 1.0f);
+    // mat4 * vec4(tfx, tfy, d, 1): ((c0*x + c1*y) + c2*z) + c3*w
+    const float* m = a.inv_bpv;
+    float w4[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) w4[r] = ((m[r] * tfx + m[4 + r] * tfy) + m[8 + r] * d) + m[12 + r] * 1.0f;
+    const v3 pos = mk(w4[0] / w4[3], w4[1] / w4[3], w4[2] / w4[3]);
+    const v3 color = diffuse * a.intensity;
+    const uint32_t ri = a.perm ? (uint32_t)__ldg(a.perm + idx) : idx;
+    const uint32_t pn = pack3SN(normal);
+    const v3 un = unpack3SN(pn);
+    a.vpl[3 * ri + 0] = make_float4(pos.x, pos.y, pos.z, 0.f);
+    a.vpl[3 * ri + 1] = make_float4(un.x, un.y, un.z, 0.f);
+    a.vpl[3 * ri + 2] = make_float4(color.x, color.y, color.z, 0.f);
+    a.packed[ri] = make_float4(pos.x, pos.y, pos.z, __uint_as_float(pn));
+    if (a.reduced) {
+        // float pos[3], half normal[3], bfloat16 flux[3]
+        uint32_t* r = reinterpret_cast<uint32_t*>(a.reduced + 24 * (size_t)ri);
+        const uint32_t hx = __half_as_ushort(__float2half_rn(un.x));
+        const uint32_t hy = __half_as_ushort(__float2half_rn(un.y));
+        const uint32_t hz = __half_as_ushort(__float2half_rn(un.z));
+        const uint32_t br = __bfloat16_as_ushort(__float2bfloat16_rn(color.x));
+        const uint32_t bg = __bfloat16_as_ushort(__float2bfloat16_rn(color.y));
+        const uint32_t bb = __bfloat16_as_ushort(__float2bfloat16_rn(color.z));
+        reinterpret_cast<uint2*>(r)[0] = make_uint2(__float_as_uint(pos.x), __float_as_uint(pos.y));
+        reinterpret_cast<uint2*>(r)[1] = make_uint2(__float_as_uint(pos.z), hx | (hy << 16));
+        reinterpret_cast<uint2*>(r)[2] = make_uint2(hz | (br << 16), bg | (bb << 16));
+    }
+}
+
+cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s) {
+    if (a.n <= 0) return cudaSuccess;
+    vpl_process_kernel<<<(a.n + 63) / 64, 64, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Atlas clear to 0xFFFFFFFF (ImperfectShadowmap.cpp:212), 16-byte stores.
+__global__ void ism_clear_kernel(uint4* p, size_t n4) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (; i < n4; i += stride) p[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+}
+
+cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if ((n & 3) || (reinterpret_cast<uintptr_t>(keys) & 15)) return cudaMemsetAsync(keys, 0xFF, n * 4, s);
+    const size_t n4 = n / 4;
+    int blocks = (int)std::min<size_t>((n4 + 255) / 256, 152 * 16);
+    ism_clear_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<uint4*>(keys), n4);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// ISM splat: one block per bucket. The 16 VPLs the bucket tests (ids wg..wg+15 mod N) are cached
+// in shared memory together with their unpacked normals and lookAtRH rows, which are computed
+// once per block with the same operations the shader repeats per point (so the values are
+// identical). Each point keeps the first <= 4 VPLs that pass the two-sided hemisphere cull and
+// atomicMin's its key into their paraboloid ISMs.
+constexpr int kSplatThreads = 256;
+
+__global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
+    __shared__ v3 s_pos[16], s_n[16], s_s[16], s_u[16];
+    __shared__ float s_ism[16];
+    const int wg = blockIdx.x;
+    const int vplCount = a.vpl_end - a.vpl_start;
+    if (a.points_only_scaled && wg > vplCount) return;
+    if (threadIdx.x < 16) {
+        int index = (wg + (int)threadIdx.x) % a.n_vpl;
+        if (a.points_only_scaled) {
+            index %= vplCount;
+            index += a.vpl_start;
+        }
+        const float4 pk = a.packed[index];
+        const v3 n = unpack3SN(__float_as_uint(pk.w));
+        v3 s, u;
+        look_at_rows(n, s, u);
+        s_pos[threadIdx.x] = mk(pk.x, pk.y, pk.z);
+        s_n[threadIdx.x] = n;
+        s_s[threadIdx.x] = s;
+        s_u[threadIdx.x] = u;
+        s_ism[threadIdx.x] = a.scale_isms ? float(index) - float(a.vpl_start) : float(index);
+    }
+    __syncthreads();
+
+    const uint32_t cnt = __ldg(a.counts + wg);
+    const float4* bucket = a.points + (int64_t)wg * a.bucket_stride;
+    const float fw = float(a.atlas_w), fh = float(a.atlas_h), fgx = float(a.gx), fgy = float(a.gy);
+    for (uint32_t j = threadIdx.x; j < cnt; j += kSplatThreads) {
+        const float4 pt = __ldg(bucket + j);
+        const v3 position = mk(pt.x, pt.y, pt.z);
+        const uint32_t nr = __float_as_uint(pt.w);
+        const v3 pn = mk(float(nr & 0xFFu) / 255.0f * 2.0f - 1.0f, float((nr >> 8) & 0xFFu) / 255.0f * 2.0f - 1.0f,
+                         float((nr >> 16) & 0xFFu) / 255.0f * 2.0f - 1.0f);
+        const float pointRadius = float(nr >> 24) / 255.0f * 25.0f;
+        const uint32_t rbyte = f2u(pointRadius * 10.0f / 2.0f);  // / sqrt(maxVplCollectCount)
+        int found = 0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            if (found >= 4) break;
+            const v3 rel = position - s_pos[i];
+            const bool cull = dot(s_n[i], rel) < 0.0f || dot(pn, -rel) < 0.0f;
+            if (cull) continue;
+            ++found;
+            // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
+            const float dist = length(rel);
+            const v3 n = s_n[i];
+            float vx = dot(s_s[i], rel);
+            float vy = dot(s_u[i], rel);
+            float vz = ((-n.x) * rel.x + (-n.y) * rel.y) + (-n.z) * rel.z;
+            const float signOfV = gsign(vz);
+            vx = vx / dist;
+            vy = vy / dist;
+            vz = vz / dist;
+            vz = 1.0f - vz;
+            vx = vx / vz;
+            vy = vy / vz;
+            vz = dist / a.z_far;
+            vz = vz * -signOfV;
+            vx = (vx + 1.0f) / 2.0f;
+            vy = (vy + 1.0f) / 2.0f;
+            const float ismIndex = s_ism[i];
+            const float ty = float(f2i(ismIndex / fgx));
+            const int tx = f2i(ismIndex - ty * fgx);
+            vx = vx + float(tx);
+            vy = vy + float(f2i(ty));
+            vx = vx / fgx;
+            vy = vy / fgy;
+            vx = vx * fw;
+            vy = vy * fh;
+            vz = vz * 16777216.0f;
+            const uint32_t key = (f2u(vz) << 8) | rbyte;
+            const int px = f2i(vx), py = f2i(vy);
+            if (px < 0 || py < 0 || px >= a.atlas_w || py >= a.atlas_h) continue;  // image op out of range: no-op
+            atomicMin(a.keys + (size_t)py * a.atlas_w + px, key);
+        }
+    }
+}
+
+cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s) {
+    if (a.n_groups <= 0) return cudaSuccess;
+    ism_splat_kernel<<<a.n_groups, kSplatThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fused pull-push: one block per ISM. Pull levels and push levels never mix texels of different
+// ISMs (2x2 pulls stay inside an ISM because its edge is divisible by 2^levels, and push gives
+// weight 0 to every coarse texel across an ISM border), so a whole ISM's pyramid lives in shared
+// memory: keys (level 0) plus RGBA texels of levels 1..L. Push level l overwrites pull level l
+// in place (a push texel reads only its own pull texel at that level). Coordinates entering the
+// displacement arithmetic are global atlas coordinates, as in the level-by-level shaders.
+constexpr int kPullPushThreads = 512;
+
+__device__ __forceinline__ float pow2neg(int level) { return __int_as_float((127 - level) << 23); }
+
+__global__ void __launch_bounds__(kPullPushThreads) pullpush_kernel(PullPushArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int s = a.ism_size, L = a.levels;
+    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);
+    float4* lvl_base = reinterpret_cast<float4*>(smem + (((size_t)s * s * 4 + 15) & ~(size_t)15));
+    const int ism = blockIdx.x;
+    const int bx = (ism % a.grid_x) * s, by = (ism / a.grid_x) * s;
+    const int nt = blockDim.x, tid = threadIdx.x;
+
+    // level 0 keys
+    if ((s & 3) == 0) {
+        const int s4 = s >> 2;
+        for (int i = tid; i < s * s4; i += nt) {
+            const int r = i / s4, c = i % s4;
+            const uint4 k = __ldg(reinterpret_cast<const uint4*>(a.keys + (size_t)(by + r) * a.atlas_w + bx) + c);
+            reinterpret_cast<uint4*>(keys)[i] = k;
+        }
+    } else {
+        for (int i = tid; i < s * s; i += nt) {
+            const int r = i / s, c = i % s;
+            keys[i] = __ldg(a.keys + (size_t)(by + r) * a.atlas_w + bx + c);
+        }
+    }
+    __syncthreads();
+
+    // level l data starts at lvl_off(l) texels from lvl_base
+    auto lvl = [&](int l) {
+        size_t off = 0;
+        for (int k = 1; k < l; ++k) off += (size_t)(s >> k) * (s >> k);
+        return lvl_base + off;
+    };
+
+    // ---- pull, levels 1..L (pull.comp) ----
+    const int poff[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};
+    for (int l = 1; l <= L; ++l) {
+        const int sl = s >> l, si = s >> (l - 1);
+        const int ox0 = bx >> l, oy0 = by >> l;
+        const float4* in = l == 1 ? nullptr : lvl(l - 1);
+        float4* out = lvl(l);
+        const float scale = pow2neg(l);
+        for (int i = tid; i < sl * sl; i += nt) {
+            const int lx = i % sl, ly = i / sl;
+            const int gox = ox0 + lx, goy = oy0 + ly;
+            float depthSamples[4], maxDepths[4], radiuses[4], dvx[4], dvy[4];
+            bool valid[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int lix = 2 * lx + poff[k][0], liy = 2 * ly + poff[k][1];
+                const int gix = 2 * gox + poff[k][0], giy = 2 * goy + poff[k][1];
+                float depthSample, radius, maxDepth, dx, dy;
+                if (l == 1) {
+                    const uint32_t key = keys[liy * si + lix];
+                    depthSample = float(key >> 8) / 16777216.0f;
+                    radius = float(key & 0xFFu) / 10.0f;
+                    dx = 0.f;
+                    dy = 0.f;
+                    maxDepth = depthSample + (radius * 2.0f) / a.z_far * 0.6f;
+                    const float distToCamera = depthSample * a.z_far;
+                    radius = radius / distToCamera / 3.14f * float(s);
+                    radius = radius * 1.3f;
+                    radius = gmin(radius, 15.0f);
+                } else {
+                    const float4 t = in[liy * si + lix];
+                    depthSample = t.x;
+                    maxDepth = t.y;
+                    radius = t.z;
+                    const float2 d = unpack_half2(__float_as_uint(t.w));
+                    dx = d.x;
+                    dy = d.y;
+                }
+                const float ndx = (float(gix) + 0.5f + dx) / 2.0f - (float(gox) + 0.5f);
+                const float ndy = (float(giy) + 0.5f + dy) / 2.0f - (float(goy) + 0.5f);
+                const float dist = sqrtf(ndx * ndx + ndy * ndy);
+                const bool pass = dist <= radius * scale;
+                depthSamples[k] = depthSample;
+                maxDepths[k] = maxDepth;
+                radiuses[k] = radius;
+                dvx[k] = ndx;
+                dvy[k] = ndy;
+                valid[k] = depthSample != 1.0f && pass;
+            }
+            float minimum = __int_as_float(0x7f800000);
+            float maxDepth = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!valid[k]) continue;
+                minimum = gmin(depthSamples[k], minimum);
+                if (minimum == depthSamples[k]) maxDepth = maxDepths[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (depthSamples[k] > maxDepth) valid[k] = false;
+            float depthAcc = 0.f, radiusAcc = 0.f, maxValid = 0.f, dax = 0.f, day = 0.f;
+            uint32_t numValid = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!valid[k]) continue;
+                depthAcc = depthAcc + depthSamples[k];
+                dax = dax + dvx[k];
+                day = day + dvy[k];
+                radiusAcc = radiusAcc + radiuses[k];
+                maxValid = gmax(maxValid, maxDepths[k]);
+                numValid++;
+            }
+            float4 r;
+            if (numValid > 0) {
+                const float nv = float(numValid);
+                r = make_float4(depthAcc / nv, maxValid, radiusAcc / nv, __uint_as_float(pack_half2(dax / nv, day / nv)));
+            } else {
+                r = make_float4(1.0f, 0.f, 0.f, 0.f);
+            }
+            out[i] = r;
+        }
+        __syncthreads();
+    }
+
+    // ---- push, levels L-1..0 (push.comp) ----
+    const int qoff[4][2] = {{0, 0}, {0, 1}, {1, 1}, {1, 0}};
+    const int weightsX[4] = {9, 3, 1, 3};
+    for (int l = L - 1; l >= 0; --l) {
+        const int sl = s >> l, sc = s >> (l + 1);
+        const int o0x = bx >> l, o0y = by >> l;          // this ISM's origin at level l
+        const int c0x = bx >> (l + 1), c0y = by >> (l + 1);  // and at level l+1
+        const float4* coarse = lvl(l + 1);
+        float4* same = l == 0 ? nullptr : lvl(l);
+        const float scale = pow2neg(l);
+        for (int i = tid; i < sl * sl; i += nt) {
+            const int lpx = i % sl, lpy = i / sl;
+            const int px = o0x + lpx, py = o0y + lpy;  // global output pixel
+            const int gidx = (px + 1) >> 1, gidy = (py + 1) >> 1;
+            const int cllx = gidx - 1, clly = gidy - 1;
+            const int ofx = px - (2 * gidx - 1), ofy = py - (2 * gidy - 1);
+            const int op = ofx == 0 ? (ofy == 0 ? 0 : 1) : (ofy == 1 ? 2 : 3);
+            float depths[4], maxDepths[4], radiuses[4], dcx[4], dcy[4];
+            int w[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int cx = cllx + qoff[k][0] - c0x, cy = clly + qoff[k][1] - c0y;
+                w[k] = weightsX[(k - op + 4) & 3];
+                if (cx >= 0 && cy >= 0 && cx < sc && cy < sc) {
+                    const float4 t = coarse[cy * sc + cx];
+                    depths[k] = t.x;
+                    maxDepths[k] = t.y;
+                    radiuses[k] = t.z;
+                    const float2 d = unpack_half2(__float_as_uint(t.w));
+                    dcx[k] = d.x;
+                    dcy[k] = d.y;
+                } else {  // across the ISM border: weight 0 (push.comp:77-86)
+                    depths[k] = 0.f;
+                    maxDepths[k] = 0.f;
+                    radiuses[k] = 0.f;
+                    dcx[k] = 0.f;
+                    dcy[k] = 0.f;
+                    w[k] = 0;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (depths[k] == 1.0f) w[k] = 0;
+            float dvx[4], dvy[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float ctx = (float(cllx + qoff[k][0]) + 0.5f) * 2.0f;
+                const float cty = (float(clly + qoff[k][1]) + 0.5f) * 2.0f;
+                const float ttx = float(px) + 0.5f, tty = float(py) + 0.5f;
+                dvx[k] = ctx - ttx + dcx[k] * 2.0f;
+                dvy[k] = cty - tty + dcy[k] * 2.0f;
+                const float dist = sqrtf(dvx[k] * dvx[k] + dvy[k] * dvy[k]);
+                if (dist > radiuses[k] * scale) w[k] = 0;
+            }
+            float minimum = 9001.0f, maxDepth = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (w[k] == 0) continue;
+                minimum = gmin(depths[k], minimum);
+                if (minimum == depths[k]) maxDepth = maxDepths[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (depths[k] > maxDepth) w[k] = 0;
+            float depthAcc = 0.f, maxDepthAcc = 0.f, radiusAcc = 0.f, dax = 0.f, day = 0.f;
+            int weightAcc = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float wf = float(w[k]);
+                depthAcc = depthAcc + depths[k] * wf;
+                maxDepthAcc = maxDepthAcc + maxDepths[k] * wf;
+                radiusAcc = radiusAcc + radiuses[k] * wf;
+                dax = dax + dvx[k] * wf;
+                day = day + dvy[k] * wf;
+                weightAcc += w[k];
+            }
+            const float wa = float(weightAcc);
+            float4 r = make_float4(depthAcc / wa, maxDepthAcc / wa, radiusAcc / wa,
+                                   __uint_as_float(pack_half2(dax / wa, day / wa)));
+            float4 orig;
+            if (l == 0) {
+                orig = make_float4(float(keys[lpy * s + lpx] >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
+            } else {
+                orig = same[i];
+            }
+            const bool invalid = orig.x == 1.0f;
+            bool occluded = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) occluded = occluded || (w[k] > 0 && orig.x > maxDepths[k]);
+            if (weightAcc <= 0 || (!invalid && !occluded)) r = orig;
+            if (l == 0) {
+                const size_t o = (size_t)py * a.atlas_w + px;
+                if (a.out_f16)
+                    reinterpret_cast<__half*>(a.out)[o] = __float2half_rn(r.x);
+                else
+                    reinterpret_cast<float*>(a.out)[o] = r.x;
+            } else {
+                same[i] = r;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+size_t pullpush_smem_bytes(int ism_size, int levels) {
+    size_t b = (((size_t)ism_size * ism_size * 4) + 15) & ~(size_t)15;
+    for (int l = 1; l <= levels; ++l) b += (size_t)(ism_size >> l) * (ism_size >> l) * 16;
+    return b;
+}
+
+cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s) {
+    const size_t smem = pullpush_smem_bytes(a.ism_size, a.levels);
+    cudaError_t e = cudaFuncSetAttribute(pullpush_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    pullpush_kernel<<<a.grid_x * a.grid_y, kPullPushThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace mlgi

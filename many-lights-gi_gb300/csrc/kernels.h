@@ -1,0 +1,86 @@
+// Launch interface between the C ABI (mlgi_api.cu) and the kernel translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mlgi {
+
+struct VplArgs {
+    int n;                 // VPL count (work items)
+    uint32_t ax, ay;       // lightsOnAxis
+    int rsm_w, rsm_h;
+    const float* depth;
+    const uint32_t* normal;
+    const uint32_t* diffuse;
+    float inv_bpv[16];
+    float intensity;
+    const int32_t* perm;   // nullptr: no shuffle
+    float4* vpl;           // 3 float4 per VPL
+    float4* packed;
+    uint8_t* reduced;      // 24 bytes per VPL, or nullptr
+};
+
+struct SplatArgs {
+    const float4* points;
+    const uint32_t* counts;
+    int64_t bucket_stride;
+    int n_groups;
+    const float4* packed;  // packedVplBuffer
+    int n_vpl;
+    int vpl_start, vpl_end;
+    int scale_isms, points_only_scaled;
+    int gx, gy, atlas_w, atlas_h;
+    float z_far;
+    uint32_t* keys;
+};
+
+struct PullPushArgs {
+    const uint32_t* keys;
+    void* out;            // final depth (FP32 or FP16)
+    int out_f16;
+    int atlas_w, atlas_h;
+    int ism_size, levels;
+    int grid_x, grid_y;
+    float z_far;
+};
+
+struct FgArgs {
+    int width, height;
+    const float* depth;
+    const void* normal;
+    int normal_f16;
+    float inv_vp[16];
+    const float4* vpl;        // 48-byte records (3 float4), or nullptr when reduced is used
+    const uint8_t* reduced;   // 24-byte records, or nullptr
+    const void* atlas;
+    int atlas_f16;
+    int atlas_w, atlas_h;
+    int gx, gy, ism_size;
+    int n_vpl, per_class;
+    int interleave;
+    int shadowing;
+    int ism_index_offset;
+    float z_far, gi_scale;    // gi_scale = giIntensity / vplCount * I^2 applied as in the shader
+    float gi_intensity;
+    float vpl_count_f;       // float(vplEndIndex - vplStartIndex)
+    float i2;
+    float clamp_value;
+    int tile;                 // tile edge (threads = tile*tile)
+    int cull;                 // per-tile culling on/off
+    float influence_cutoff;   // 0: off
+    float* out;               // width*height*3
+    uint32_t* status;         // device error word (bit 0: VPL staging wait timed out)
+};
+
+// Error bits written to the device status word.
+constexpr uint32_t kStatusTmaTimeout = 1u;
+
+cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s);
+cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s);
+cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s);
+cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s);
+size_t pullpush_smem_bytes(int ism_size, int levels);
+cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s);
+
+}  // namespace mlgi

@@ -1,0 +1,503 @@
+// C ABI of the GI hot path: argument checking, context-owned buffers, per-pass timing and the
+// frame-level chain (GIStage::process's GI part, GIStage.cpp:346-418).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <random>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "mlgi.h"
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+enum Pass { kVplp = 0, kIsmClear, kIsmCs, kPullPush, kFg, kH2D, kD2H, kNumPasses };
+// Event slots: ev[k]..ev[k+1] bracket device pass k (k <= kFg); two extra slots bracket the
+// host-frame copies.
+constexpr int kEvH2DStart = kNumPasses + 1, kEvD2HEnd = kNumPasses + 2, kNumEvents = kNumPasses + 3;
+
+}  // namespace
+
+struct mlgi_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::map<int, int32_t*> shuffle_dev;  // per VPL count
+    uint32_t* status = nullptr;           // device error word
+    // frame-level buffers
+    DevBuf vpl, packed, reduced, keys, depth;
+    // host-frame input copies
+    DevBuf h_rsm_depth, h_rsm_normal, h_rsm_diffuse, h_points, h_counts, h_gdepth, h_gnormal, h_rgb;
+    bool timing = false;
+    bool timed_host_frame = false;  // the last timed call was mlgi_gi_frame_host
+    bool timed_frame = false;
+    cudaEvent_t ev[kNumEvents] = {};
+    float last_ms[kNumPasses] = {};
+};
+
+namespace {
+
+mlgi_status fail(mlgi_ctx* ctx, mlgi_status s, const char* fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return s;
+}
+
+mlgi_status cuda_fail(mlgi_ctx* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, MLGI_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define MLGI_CUDA(ctx, call)                                 \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+mlgi_status ensure(mlgi_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes) return MLGI_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, MLGI_ENOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    return MLGI_OK;
+}
+
+cudaStream_t pick(mlgi_ctx* ctx, mlgi_stream s) { return s ? static_cast<cudaStream_t>(s) : ctx->stream; }
+
+void shuffle_host(int n, int32_t* out) {
+    // VPLProcessor.cpp:58-65: iota, then std::shuffle with std::mt19937 seeded 1979982.
+    std::vector<int> v(n);
+    std::iota(v.begin(), v.end(), 0);
+    std::mt19937 g(1979982);
+    std::shuffle(v.begin(), v.end(), g);
+    std::memcpy(out, v.data(), sizeof(int32_t) * n);
+}
+
+mlgi_status get_shuffle(mlgi_ctx* ctx, int n, const int32_t** out) {
+    auto it = ctx->shuffle_dev.find(n);
+    if (it != ctx->shuffle_dev.end()) {
+        *out = it->second;
+        return MLGI_OK;
+    }
+    std::vector<int32_t> h(n);
+    shuffle_host(n, h.data());
+    int32_t* d = nullptr;
+    if (cudaMalloc(&d, sizeof(int32_t) * n) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, MLGI_ENOMEM, "shuffle table allocation failed");
+    }
+    MLGI_CUDA(ctx, cudaMemcpy(d, h.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    ctx->shuffle_dev[n] = d;
+    *out = d;
+    return MLGI_OK;
+}
+
+void mark(mlgi_ctx* ctx, int pass, cudaStream_t s) {
+    if (ctx->timing) cudaEventRecord(ctx->ev[pass], s);
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+mlgi_status check_ism(mlgi_ctx* ctx, const mlgi_ism_params* p) {
+    if (!p) return fail(ctx, MLGI_EINVAL, "ism params are NULL");
+    if (p->ism_size <= 0 || p->grid_x <= 0 || p->grid_y <= 0 || p->levels < 1 || p->levels > 10)
+        return fail(ctx, MLGI_EINVAL, "bad ISM geometry (size %d, grid %dx%d, levels %d)", p->ism_size, p->grid_x,
+                    p->grid_y, p->levels);
+    if (p->ism_size % (1 << p->levels) != 0)
+        return fail(ctx, MLGI_EINVAL, "ISM size %d is not divisible by 2^%d", p->ism_size, p->levels);
+    if ((int64_t)p->grid_x * p->ism_size > 65535 || (int64_t)p->grid_y * p->ism_size > 65535)
+        return fail(ctx, MLGI_EINVAL, "atlas larger than 65535 texels on a side");
+    if (!(p->z_far > 0.f)) return fail(ctx, MLGI_EINVAL, "z_far must be positive");
+    if (p->vpl_end <= p->vpl_start || p->vpl_start < 0)
+        return fail(ctx, MLGI_EINVAL, "empty VPL range [%d, %d)", p->vpl_start, p->vpl_end);
+    return MLGI_OK;
+}
+
+mlgi_status check_atlas(mlgi_ctx* ctx, const mlgi_atlas* a, const mlgi_ism_params* p) {
+    if (!a) return fail(ctx, MLGI_EINVAL, "atlas is NULL");
+    if (a->width != p->grid_x * p->ism_size || a->height != p->grid_y * p->ism_size)
+        return fail(ctx, MLGI_EINVAL, "atlas %dx%d does not match grid %dx%d of %d-texel ISMs", a->width, a->height,
+                    p->grid_x, p->grid_y, p->ism_size);
+    if (a->format != MLGI_F32 && a->format != MLGI_F16) return fail(ctx, MLGI_EINVAL, "atlas format must be F32 or F16");
+    return MLGI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mlgi_status_string(mlgi_status s) {
+    switch (s) {
+        case MLGI_OK: return "ok";
+        case MLGI_EINVAL: return "invalid argument";
+        case MLGI_ENOMEM: return "out of memory";
+        case MLGI_ETIMEDOUT: return "device wait timed out";
+        case MLGI_ECUDA: return "CUDA error";
+        case MLGI_ECANCELED: return "cancelled";
+        default: return "unknown status";
+    }
+}
+
+mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
+    if (!out) return MLGI_EINVAL;
+    *out = nullptr;
+    mlgi_ctx* ctx = new mlgi_ctx();
+    ctx->device = desc ? desc->device : 0;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->status, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->status, 0, sizeof(uint32_t));
+    for (int i = 0; e == cudaSuccess && i < kNumEvents; ++i) e = cudaEventCreate(&ctx->ev[i]);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        mlgi_destroy(ctx);
+        return MLGI_ECUDA;
+    }
+    *out = ctx;
+    return MLGI_OK;
+}
+
+void mlgi_destroy(mlgi_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->shuffle_dev) cudaFree(kv.second);
+    for (DevBuf* b : {&ctx->vpl, &ctx->packed, &ctx->reduced, &ctx->keys, &ctx->depth, &ctx->h_rsm_depth,
+                      &ctx->h_rsm_normal, &ctx->h_rsm_diffuse, &ctx->h_points, &ctx->h_counts, &ctx->h_gdepth,
+                      &ctx->h_gnormal, &ctx->h_rgb})
+        if (b->p) cudaFree(b->p);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->status) cudaFree(ctx->status);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* mlgi_last_error(const mlgi_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+mlgi_stream mlgi_ctx_stream(mlgi_ctx* ctx) { return ctx ? static_cast<mlgi_stream>(ctx->stream) : nullptr; }
+
+mlgi_status mlgi_shuffle_table(int n, int32_t* out_host) {
+    if (n <= 0 || !out_host) return MLGI_EINVAL;
+    shuffle_host(n, out_host);
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_vpl_process(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi_vpl_params* p, mlgi_vpl_buf* out,
+                             mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!rsm || !p || !out) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    if (p->count <= 0 || p->count % 64 != 0)
+        return fail(ctx, MLGI_EINVAL, "VPL count %d is not a positive multiple of 64", p->count);
+    if (p->count > out->capacity) return fail(ctx, MLGI_EINVAL, "VPL count %d exceeds capacity %d", p->count, out->capacity);
+    if (rsm->width <= 0 || rsm->height <= 0 || !rsm->depth || !rsm->normal || !rsm->diffuse)
+        return fail(ctx, MLGI_EINVAL, "bad RSM view");
+    if (!out->vpl || !out->packed || !aligned16(out->vpl) || !aligned16(out->packed))
+        return fail(ctx, MLGI_EINVAL, "VPL buffers must be non-NULL and 16-byte aligned");
+    mlgi::VplArgs a{};
+    a.n = p->count;
+    a.ax = (uint32_t)std::ceil(std::sqrt((float)p->count));  // rsmSamples1d = uint(ceil(sqrt(N)))
+    a.ay = (uint32_t)p->count / a.ax;
+    a.rsm_w = rsm->width;
+    a.rsm_h = rsm->height;
+    a.depth = rsm->depth;
+    a.normal = rsm->normal;
+    a.diffuse = rsm->diffuse;
+    std::memcpy(a.inv_bpv, p->inv_biased_light_vp, sizeof(a.inv_bpv));
+    a.intensity = p->light_intensity;
+    a.perm = nullptr;
+    if (p->shuffle) {
+        mlgi_status st = get_shuffle(ctx, p->count, &a.perm);
+        if (st != MLGI_OK) return st;
+    }
+    a.vpl = reinterpret_cast<float4*>(out->vpl);
+    a.packed = reinterpret_cast<float4*>(out->packed);
+    a.reduced = static_cast<uint8_t*>(out->reduced);
+    MLGI_CUDA(ctx, mlgi::launch_vpl_process(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                           const mlgi_ism_params* p, mlgi_atlas* atlas, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi_status st = check_ism(ctx, p);
+    if (st != MLGI_OK) return st;
+    if ((st = check_atlas(ctx, atlas, p)) != MLGI_OK) return st;
+    if (!pts || !vpls || !atlas->keys) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    if (n_vpl <= 0 || n_vpl > vpls->capacity || p->vpl_end > n_vpl)
+        return fail(ctx, MLGI_EINVAL, "bad VPL count %d (capacity %d, range end %d)", n_vpl, vpls->capacity, p->vpl_end);
+    const int vplCount = p->vpl_end - p->vpl_start;
+    const int ismCount = p->scale_isms ? vplCount : n_vpl;
+    if (ismCount > p->grid_x * p->grid_y)
+        return fail(ctx, MLGI_EINVAL, "%d ISMs do not fit a %dx%d grid", ismCount, p->grid_x, p->grid_y);
+    const int sampled = p->points_only_scaled ? vplCount : n_vpl;
+    if (pts->n_buckets != sampled)
+        return fail(ctx, MLGI_EINVAL, "point buffer has %d buckets, the splat samples %d", pts->n_buckets, sampled);
+    if (pts->n_buckets > 0 && (!pts->points || !pts->counts || pts->bucket_stride < 0 || !aligned16(pts->points)))
+        return fail(ctx, MLGI_EINVAL, "bad point buffer");
+    cudaStream_t s = pick(ctx, stream);
+    MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas->keys, (size_t)atlas->width * atlas->height, s));
+    mark(ctx, kIsmClear + 1, s);
+    mlgi::SplatArgs a{};
+    a.points = reinterpret_cast<const float4*>(pts->points);
+    a.counts = pts->counts;
+    a.bucket_stride = pts->bucket_stride;
+    a.n_groups = pts->n_buckets;
+    a.packed = reinterpret_cast<const float4*>(vpls->packed);
+    a.n_vpl = n_vpl;
+    a.vpl_start = p->vpl_start;
+    a.vpl_end = p->vpl_end;
+    a.scale_isms = p->scale_isms;
+    a.points_only_scaled = p->points_only_scaled;
+    a.gx = p->grid_x;
+    a.gy = p->grid_y;
+    a.atlas_w = atlas->width;
+    a.atlas_h = atlas->height;
+    a.z_far = p->z_far;
+    a.keys = atlas->keys;
+    MLGI_CUDA(ctx, mlgi::launch_ism_splat(a, s));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* p, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi_status st = check_ism(ctx, p);
+    if (st != MLGI_OK) return st;
+    if ((st = check_atlas(ctx, atlas, p)) != MLGI_OK) return st;
+    if (!atlas->keys || !atlas->depth) return fail(ctx, MLGI_EINVAL, "atlas buffers are NULL");
+    if (mlgi::pullpush_smem_bytes(p->ism_size, p->levels) > 227 * 1024)
+        return fail(ctx, MLGI_EINVAL, "a %d-texel ISM pyramid exceeds shared memory", p->ism_size);
+    if ((p->ism_size & 3) == 0 && !aligned16(atlas->keys))
+        return fail(ctx, MLGI_EINVAL, "atlas keys must be 16-byte aligned");
+    mlgi::PullPushArgs a{};
+    a.keys = atlas->keys;
+    a.out = atlas->depth;
+    a.out_f16 = atlas->format == MLGI_F16;
+    a.atlas_w = atlas->width;
+    a.atlas_h = atlas->height;
+    a.ism_size = p->ism_size;
+    a.levels = p->levels;
+    a.grid_x = p->grid_x;
+    a.grid_y = p->grid_y;
+    a.z_far = p->z_far;
+    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls,
+                              const mlgi_atlas* atlas, const mlgi_fg_params* p, mlgi_radiance* out,
+                              mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!g || !vpls || !atlas || !p || !out) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    if (g->width <= 0 || g->height <= 0 || !g->depth || !g->normal) return fail(ctx, MLGI_EINVAL, "bad G-buffer view");
+    if (out->width != g->width || out->height != g->height || !out->rgb)
+        return fail(ctx, MLGI_EINVAL, "radiance buffer does not match the G-buffer");
+    const int I = p->interleave;
+    if (I < 1 || I > 16 || p->vpl_count <= 0 || p->vpl_count % (I * I) != 0)
+        return fail(ctx, MLGI_EINVAL, "VPL count %d is not a multiple of I^2 = %d", p->vpl_count, I * I);
+    if (p->vpl_count > vpls->capacity) return fail(ctx, MLGI_EINVAL, "VPL count exceeds capacity");
+    if (p->tile != 0 && p->tile != 8 && p->tile != 16) return fail(ctx, MLGI_EINVAL, "tile must be 0, 8 or 16");
+    if (p->vpl_end <= p->vpl_start) return fail(ctx, MLGI_EINVAL, "empty VPL range");
+    if (p->vpl_format != MLGI_F32 && p->vpl_format != MLGI_F16) return fail(ctx, MLGI_EINVAL, "bad VPL format");
+    if (p->vpl_format == MLGI_F16 && !vpls->reduced) return fail(ctx, MLGI_EINVAL, "reduced VPL records missing");
+    if (p->vpl_format == MLGI_F32 && (!vpls->vpl || !aligned16(vpls->vpl)))
+        return fail(ctx, MLGI_EINVAL, "VPL records must be 16-byte aligned");
+    if (p->shadowing && (!atlas->depth || atlas->width <= 0 || atlas->height <= 0 || atlas->width > 65535 ||
+                         atlas->height > 65535 || (atlas->format != MLGI_F32 && atlas->format != MLGI_F16)))
+        return fail(ctx, MLGI_EINVAL, "bad shadow atlas");
+    if (p->shadowing && (p->ism_size <= 0 || p->grid_x <= 0 || p->grid_y <= 0 ||
+                         p->grid_x * p->ism_size != atlas->width || p->grid_y * p->ism_size != atlas->height))
+        return fail(ctx, MLGI_EINVAL, "FG atlas layout does not match the atlas");
+    if (p->shadowing && (p->scale_isms ? p->vpl_end - p->vpl_start : p->vpl_count) > p->grid_x * p->grid_y)
+        return fail(ctx, MLGI_EINVAL, "more ISMs than grid slots");
+    mlgi::FgArgs a{};
+    a.width = g->width;
+    a.height = g->height;
+    a.depth = g->depth;
+    a.normal = g->normal;
+    a.normal_f16 = g->normal_format == MLGI_F16;
+    std::memcpy(a.inv_vp, p->inv_view_proj, sizeof(a.inv_vp));
+    a.vpl = p->vpl_format == MLGI_F32 ? reinterpret_cast<const float4*>(vpls->vpl) : nullptr;
+    a.reduced = p->vpl_format == MLGI_F16 ? static_cast<const uint8_t*>(vpls->reduced) : nullptr;
+    a.atlas = atlas->depth;
+    a.atlas_f16 = atlas->format == MLGI_F16;
+    a.atlas_w = atlas->width;
+    a.atlas_h = atlas->height;
+    a.n_vpl = p->vpl_count;
+    a.per_class = p->vpl_count / (I * I);
+    a.interleave = I;
+    a.shadowing = p->shadowing;
+    a.ism_index_offset = p->scale_isms ? p->vpl_start : 0;
+    a.z_far = p->z_far;
+    a.gi_intensity = p->gi_intensity;
+    a.vpl_count_f = (float)(p->vpl_end - p->vpl_start);
+    a.i2 = (float)(I * I);
+    a.clamp_value = p->clamp_value;
+    a.tile = p->tile == 0 ? 16 : p->tile;
+    a.cull = p->cull;
+    a.influence_cutoff = p->influence_cutoff;
+    a.out = out->rgb;
+    a.status = ctx->status;
+    a.gx = p->grid_x > 0 ? p->grid_x : 1;
+    a.gy = p->grid_y > 0 ? p->grid_y : 1;
+    a.ism_size = p->ism_size > 0 ? p->ism_size : 1;
+    cudaStream_t s = pick(ctx, stream);
+    MLGI_CUDA(ctx, mlgi::launch_final_gather(a, s));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_check_device_status(mlgi_ctx* ctx, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    cudaStream_t s = pick(ctx, stream);
+    uint32_t word = 0;
+    MLGI_CUDA(ctx, cudaMemcpyAsync(&word, ctx->status, sizeof(word), cudaMemcpyDeviceToHost, s));
+    MLGI_CUDA(ctx, cudaStreamSynchronize(s));
+    if (word) {
+        MLGI_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(uint32_t), s));
+        MLGI_CUDA(ctx, cudaStreamSynchronize(s));
+        if (word & mlgi::kStatusTmaTimeout) return fail(ctx, MLGI_ETIMEDOUT, "a VPL staging wait timed out");
+        return fail(ctx, MLGI_ECUDA, "device status word 0x%x", word);
+    }
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_set_timing(mlgi_ctx* ctx, int enabled) {
+    if (!ctx) return MLGI_EINVAL;
+    ctx->timing = enabled != 0;
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n) {
+    if (!ctx || !ms) return MLGI_EINVAL;
+    for (int k = 0; k < kNumPasses; ++k) ctx->last_ms[k] = 0.f;
+    if (ctx->timed_frame) {
+        MLGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[kFg + 1]));
+        for (int k = kVplp; k <= kFg; ++k) cudaEventElapsedTime(&ctx->last_ms[k], ctx->ev[k], ctx->ev[k + 1]);
+        if (ctx->timed_host_frame) {
+            MLGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[kEvD2HEnd]));
+            cudaEventElapsedTime(&ctx->last_ms[kH2D], ctx->ev[kEvH2DStart], ctx->ev[kVplp]);
+            cudaEventElapsedTime(&ctx->last_ms[kD2H], ctx->ev[kFg + 1], ctx->ev[kEvD2HEnd]);
+        }
+    }
+    for (int i = 0; i < n && i < kNumPasses; ++i) ms[i] = ctx->last_ms[i];
+    return MLGI_OK;
+}
+
+namespace {
+
+// Runs the chain on device buffers; ctx-owned VPL buffers and atlas. Events ev[k] .. ev[k+1]
+// bracket pass k when timing is on (ev[0] is recorded by the caller).
+mlgi_status run_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, mlgi_radiance* out, cudaStream_t s) {
+    const int n = f->vpl.count;
+    mlgi_status st = ensure(ctx, ctx->vpl, (size_t)n * 48);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->packed, (size_t)n * 16);
+    const bool reduced = f->fg.vpl_format == MLGI_F16;
+    if (st == MLGI_OK && reduced) st = ensure(ctx, ctx->reduced, (size_t)n * 24);
+    const int aw = f->ism.grid_x * f->ism.ism_size, ah = f->ism.grid_y * f->ism.ism_size;
+    if (st == MLGI_OK) st = ensure(ctx, ctx->keys, (size_t)aw * ah * 4);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->depth, (size_t)aw * ah * (f->atlas_format == MLGI_F16 ? 2 : 4));
+    if (st != MLGI_OK) return st;
+    mlgi_vpl_buf vb{n, static_cast<float*>(ctx->vpl.p), static_cast<float*>(ctx->packed.p),
+                    reduced ? ctx->reduced.p : nullptr};
+    mlgi_atlas atlas{aw, ah, static_cast<uint32_t*>(ctx->keys.p), ctx->depth.p, f->atlas_format};
+    if ((st = mlgi_vpl_process(ctx, &f->rsm, &f->vpl, &vb, s)) != MLGI_OK) return st;
+    mark(ctx, kVplp + 1, s);
+    if ((st = mlgi_ism_splat(ctx, &f->points, &vb, n, &f->ism, &atlas, s)) != MLGI_OK) return st;
+    mark(ctx, kIsmCs + 1, s);
+    if ((st = mlgi_pullpush(ctx, &atlas, &f->ism, s)) != MLGI_OK) return st;
+    mark(ctx, kPullPush + 1, s);
+    if ((st = mlgi_final_gather(ctx, &f->gbuffer, &vb, &atlas, &f->fg, out, s)) != MLGI_OK) return st;
+    mark(ctx, kFg + 1, s);
+    return MLGI_OK;
+}
+
+}  // namespace
+
+mlgi_status mlgi_gi_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, mlgi_radiance* out, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!f || !out) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    cudaStream_t s = pick(ctx, stream);
+    mark(ctx, kVplp, s);
+    mlgi_status st = run_frame(ctx, f, out, s);
+    ctx->timed_frame = st == MLGI_OK && ctx->timing;
+    ctx->timed_host_frame = false;
+    return st;
+}
+
+mlgi_status mlgi_frame_host_sizes_get(const mlgi_frame_desc* f, mlgi_frame_host_sizes* z) {
+    if (!f || !z) return MLGI_EINVAL;
+    const size_t rt = (size_t)f->rsm.width * f->rsm.height;
+    z->rsm_depth = rt * 4;
+    z->rsm_normal = rt * 4;
+    z->rsm_diffuse = rt * 4;
+    z->points = (size_t)f->points.n_buckets * (size_t)f->points.bucket_stride * 16;
+    z->counts = (size_t)f->points.n_buckets * 4;
+    const size_t gp = (size_t)f->gbuffer.width * f->gbuffer.height;
+    z->gbuf_depth = gp * 4;
+    z->gbuf_normal = gp * (f->gbuffer.normal_format == MLGI_F16 ? 4 : 8);
+    z->radiance = gp * 12;
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!f || !rgb_host) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    mlgi_frame_host_sizes z;
+    mlgi_frame_host_sizes_get(f, &z);
+    mlgi_status st = MLGI_OK;
+    DevBuf* bufs[] = {&ctx->h_rsm_depth, &ctx->h_rsm_normal, &ctx->h_rsm_diffuse, &ctx->h_points,
+                      &ctx->h_counts,    &ctx->h_gdepth,     &ctx->h_gnormal,      &ctx->h_rgb};
+    const size_t sizes[] = {z.rsm_depth, z.rsm_normal, z.rsm_diffuse, z.points, z.counts, z.gbuf_depth, z.gbuf_normal, z.radiance};
+    const void* srcs[] = {f->rsm.depth, f->rsm.normal, f->rsm.diffuse, f->points.points, f->points.counts,
+                          f->gbuffer.depth, f->gbuffer.normal, nullptr};
+    for (int i = 0; i < 8 && st == MLGI_OK; ++i) st = ensure(ctx, *bufs[i], std::max<size_t>(sizes[i], 16));
+    if (st != MLGI_OK) return st;
+    cudaStream_t s = ctx->stream;
+    mark(ctx, kEvH2DStart, s);
+    for (int i = 0; i < 7; ++i) {
+        if (!sizes[i]) continue;
+        if (!srcs[i]) return fail(ctx, MLGI_EINVAL, "host input %d is NULL", i);
+        MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, s));
+    }
+    mlgi_frame_desc d = *f;
+    d.rsm.depth = static_cast<const float*>(ctx->h_rsm_depth.p);
+    d.rsm.normal = static_cast<const uint32_t*>(ctx->h_rsm_normal.p);
+    d.rsm.diffuse = static_cast<const uint32_t*>(ctx->h_rsm_diffuse.p);
+    d.points.points = static_cast<const float*>(ctx->h_points.p);
+    d.points.counts = static_cast<const uint32_t*>(ctx->h_counts.p);
+    d.gbuffer.depth = static_cast<const float*>(ctx->h_gdepth.p);
+    d.gbuffer.normal = ctx->h_gnormal.p;
+    mlgi_radiance out{f->gbuffer.width, f->gbuffer.height, static_cast<float*>(ctx->h_rgb.p)};
+    mark(ctx, kVplp, s);
+    if ((st = run_frame(ctx, &d, &out, s)) != MLGI_OK) return st;
+    MLGI_CUDA(ctx, cudaMemcpyAsync(rgb_host, out.rgb, z.radiance, cudaMemcpyDeviceToHost, s));
+    mark(ctx, kEvD2HEnd, s);
+    MLGI_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->timed_frame = ctx->timed_host_frame = ctx->timing;
+    return mlgi_check_device_status(ctx, s);
+}
+
+}  // extern "C"

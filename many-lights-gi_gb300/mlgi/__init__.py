@@ -1,0 +1,353 @@
+"""ctypes binding of libmlgi.so (include/mlgi.h) plus the workload configurations.
+
+This module is a thin caller of the C ABI: every device computation goes through the CUDA
+kernels in libmlgi.so. Loading fails loudly when the library has not been built; there is no
+fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(PKG, "_build", "libmlgi.so")
+
+OK, EINVAL, ENOMEM, ETIMEDOUT, ECUDA, ECANCELED = 0, 1, 2, 3, 4, 5
+F32, F16, BF16 = 0, 1, 2
+
+_p = C.c_void_p
+_f16 = C.c_float * 16
+
+
+class RsmView(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("depth", _p), ("normal", _p), ("diffuse", _p)]
+
+
+class VplParams(C.Structure):
+    _fields_ = [("count", C.c_int), ("light_intensity", C.c_float), ("shuffle", C.c_int),
+                ("inv_biased_light_vp", _f16)]
+
+
+class VplBuf(C.Structure):
+    _fields_ = [("capacity", C.c_int), ("vpl", _p), ("packed", _p), ("reduced", _p)]
+
+
+class Points(C.Structure):
+    _fields_ = [("points", _p), ("counts", _p), ("n_buckets", C.c_int), ("bucket_stride", C.c_int64)]
+
+
+class IsmParams(C.Structure):
+    _fields_ = [("vpl_start", C.c_int), ("vpl_end", C.c_int), ("scale_isms", C.c_int),
+                ("points_only_scaled", C.c_int), ("ism_size", C.c_int), ("grid_x", C.c_int),
+                ("grid_y", C.c_int), ("levels", C.c_int), ("z_far", C.c_float)]
+
+
+class Atlas(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("keys", _p), ("depth", _p), ("format", C.c_int)]
+
+
+class GBufferView(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("depth", _p), ("normal", _p), ("normal_format", C.c_int)]
+
+
+class FgParams(C.Structure):
+    _fields_ = [("inv_view_proj", _f16), ("z_far", C.c_float), ("gi_intensity", C.c_float),
+                ("clamp_value", C.c_float), ("vpl_count", C.c_int), ("vpl_start", C.c_int), ("vpl_end", C.c_int),
+                ("scale_isms", C.c_int), ("ism_size", C.c_int), ("grid_x", C.c_int), ("grid_y", C.c_int),
+                ("interleave", C.c_int), ("shadowing", C.c_int), ("tile", C.c_int), ("cull", C.c_int),
+                ("influence_cutoff", C.c_float), ("vpl_format", C.c_int)]
+
+
+class Radiance(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("rgb", _p)]
+
+
+class FrameDesc(C.Structure):
+    _fields_ = [("rsm", RsmView), ("vpl", VplParams), ("points", Points), ("ism", IsmParams),
+                ("atlas_format", C.c_int), ("gbuffer", GBufferView), ("fg", FgParams)]
+
+
+class FrameHostSizes(C.Structure):
+    _fields_ = [(n, C.c_size_t) for n in ("rsm_depth", "rsm_normal", "rsm_diffuse", "points", "counts",
+                                           "gbuf_depth", "gbuf_normal", "radiance")]
+
+
+class CtxDesc(C.Structure):
+    _fields_ = [("device", C.c_int), ("flags", C.c_uint32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_boxes", C.c_int), ("n_spheres", C.c_int), ("width", C.c_int),
+                ("height", C.c_int), ("rsm_width", C.c_int), ("rsm_height", C.c_int), ("n_points", C.c_int64),
+                ("n_buckets", C.c_int), ("ism_count", C.c_int), ("light_yaw_deg", C.c_float),
+                ("light_pitch_deg", C.c_float), ("camera_orbit_deg", C.c_float), ("z_near", C.c_float),
+                ("z_far", C.c_float)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("view", _f16), ("proj", _f16), ("inv_view_proj", _f16), ("light_view", _f16),
+                ("light_proj", _f16), ("inv_biased_light_vp", _f16), ("eye", C.c_float * 3),
+                ("light_pos", C.c_float * 3), ("light_dir", C.c_float * 3), ("z_near", C.c_float),
+                ("z_far", C.c_float), ("total_area", C.c_float), ("point_radius", C.c_float),
+                ("bucket_stride", C.c_int64)]
+
+
+# Every entry point of include/mlgi.h with its ctypes signature.
+_SIGS = {
+    "mlgi_create": (C.c_int32, [C.POINTER(C.c_void_p), C.POINTER(CtxDesc)]),
+    "mlgi_destroy": (None, [_p]),
+    "mlgi_last_error": (C.c_char_p, [_p]),
+    "mlgi_status_string": (C.c_char_p, [C.c_int32]),
+    "mlgi_ctx_stream": (_p, [_p]),
+    "mlgi_vpl_process": (C.c_int32, [_p, C.POINTER(RsmView), C.POINTER(VplParams), C.POINTER(VplBuf), _p]),
+    "mlgi_shuffle_table": (C.c_int32, [C.c_int, _p]),
+    "mlgi_ism_splat": (C.c_int32, [_p, C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams),
+                                   C.POINTER(Atlas), _p]),
+    "mlgi_pullpush": (C.c_int32, [_p, C.POINTER(Atlas), C.POINTER(IsmParams), _p]),
+    "mlgi_final_gather": (C.c_int32, [_p, C.POINTER(GBufferView), C.POINTER(VplBuf), C.POINTER(Atlas),
+                                      C.POINTER(FgParams), C.POINTER(Radiance), _p]),
+    "mlgi_gi_frame": (C.c_int32, [_p, C.POINTER(FrameDesc), C.POINTER(Radiance), _p]),
+    "mlgi_frame_host_sizes_get": (C.c_int32, [C.POINTER(FrameDesc), C.POINTER(FrameHostSizes)]),
+    "mlgi_gi_frame_host": (C.c_int32, [_p, C.POINTER(FrameDesc), _p]),
+    "mlgi_set_timing": (C.c_int32, [_p, C.c_int]),
+    "mlgi_last_timings": (C.c_int32, [_p, _p, C.c_int]),
+    "mlgi_check_device_status": (C.c_int32, [_p, _p]),
+    "mlgi_scene_generate": (C.c_int32, [C.POINTER(SceneDesc), C.POINTER(SceneInfo), _p, _p, _p, _p, _p, _p, _p, _p]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libmlgi.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libmlgi.so is not built ({LIB_PATH}); run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+class MlgiError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"mlgi status {status}: {msg}")
+        self.status = status
+
+
+def ptr(x) -> int:
+    """Device or host address of a torch tensor / numpy array (None -> NULL)."""
+    if x is None:
+        return 0
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    return x.data_ptr()
+
+
+def mat16(m) -> "C.Array":
+    a = np.asarray(m, dtype=np.float32).reshape(16)
+    return _f16(*a.tolist())
+
+
+class Context:
+    """Owns an mlgi_ctx; each method calls one C-ABI entry point and raises on failure."""
+
+    def __init__(self, device: int = 0):
+        self.h = C.c_void_p()
+        d = CtxDesc(device, 0)
+        st = lib().mlgi_create(C.byref(self.h), C.byref(d))
+        if st != OK:
+            raise MlgiError(st, "mlgi_create failed")
+
+    def close(self):
+        if self.h:
+            lib().mlgi_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, st: int):
+        if st != OK:
+            raise MlgiError(st, lib().mlgi_last_error(self.h).decode())
+        return st
+
+    def stream(self) -> int:
+        return lib().mlgi_ctx_stream(self.h) or 0
+
+    def vpl_process(self, rsm: RsmView, params: VplParams, out: VplBuf, stream: int = 0):
+        return self._chk(lib().mlgi_vpl_process(self.h, C.byref(rsm), C.byref(params), C.byref(out), stream))
+
+    def ism_splat(self, pts: Points, vpls: VplBuf, n_vpl: int, params: IsmParams, atlas: Atlas, stream: int = 0):
+        return self._chk(lib().mlgi_ism_splat(self.h, C.byref(pts), C.byref(vpls), n_vpl, C.byref(params),
+                                              C.byref(atlas), stream))
+
+    def pullpush(self, atlas: Atlas, params: IsmParams, stream: int = 0):
+        return self._chk(lib().mlgi_pullpush(self.h, C.byref(atlas), C.byref(params), stream))
+
+    def final_gather(self, g: GBufferView, vpls: VplBuf, atlas: Atlas, params: FgParams, out: Radiance,
+                     stream: int = 0):
+        return self._chk(lib().mlgi_final_gather(self.h, C.byref(g), C.byref(vpls), C.byref(atlas),
+                                                 C.byref(params), C.byref(out), stream))
+
+    def gi_frame(self, f: FrameDesc, out: Radiance, stream: int = 0):
+        return self._chk(lib().mlgi_gi_frame(self.h, C.byref(f), C.byref(out), stream))
+
+    def gi_frame_host(self, f: FrameDesc, rgb_host: np.ndarray):
+        return self._chk(lib().mlgi_gi_frame_host(self.h, C.byref(f), ptr(rgb_host)))
+
+    def set_timing(self, on: bool):
+        return self._chk(lib().mlgi_set_timing(self.h, int(on)))
+
+    def last_timings(self) -> np.ndarray:
+        ms = np.zeros(7, np.float32)
+        self._chk(lib().mlgi_last_timings(self.h, ms.ctypes.data, 7))
+        return ms
+
+    def check_device_status(self, stream: int = 0):
+        return self._chk(lib().mlgi_check_device_status(self.h, stream))
+
+
+def shuffle_table(n: int) -> np.ndarray:
+    out = np.zeros(n, np.int32)
+    st = lib().mlgi_shuffle_table(n, out.ctypes.data)
+    if st != OK:
+        raise MlgiError(st, "mlgi_shuffle_table")
+    return out
+
+
+# ---- workload configurations ------------------------------------------------------------------
+
+@dataclasses.dataclass(frozen=True)
+class Config:
+    """One GI workload: scene, buffer sizes and the GI parameters of GIStage (GIStage.cpp:213-232)."""
+    name: str
+    width: int
+    height: int
+    rsm: int
+    n_vpl: int
+    n_points: int
+    ism_size: int
+    grid_x: int
+    grid_y: int
+    levels: int
+    interleave: int
+    n_boxes: int
+    n_spheres: int
+    tile: int = 16
+    cull: int = 0
+    influence_cutoff: float = 0.0
+    reduced: bool = False          # FP16 atlas, BF16/FP16 VPL records, FP16 G-buffer normals
+    seed: int = 1
+    light_intensity: float = 5.0   # GIStage.cpp:215
+    gi_intensity: float = 3000.0   # GIStage.cpp:217
+    clamp_value: float = 0.001     # GIStage.cpp:218
+    shuffle: bool = True           # GIStage.cpp:232
+    z_near: float = 1.0
+    z_far: float = 400.0
+    light_yaw_deg: float = 0.0
+    light_pitch_deg: float = 0.0
+    camera_orbit_deg: float = 0.0
+
+    @property
+    def atlas_w(self) -> int:
+        return self.grid_x * self.ism_size
+
+    @property
+    def atlas_h(self) -> int:
+        return self.grid_y * self.ism_size
+
+    @property
+    def pairs(self) -> int:
+        """Evaluated pixel-VPL pairs per frame: W*H*N/I^2."""
+        return self.width * self.height * self.n_vpl // (self.interleave ** 2)
+
+    def replace(self, **kw) -> "Config":
+        return dataclasses.replace(self, **kw)
+
+
+# Plain method, small, FP32, one frame (640x360, 256 VPLs, 2^18 points, 64^2 ISMs, 4 levels, I=4).
+C1 = Config("c1_640x360_n256", 640, 360, 256, 256, 1 << 18, 64, 16, 16, 4, 4, 4, 2, tile=16, cull=0)
+# Plain method, full size (1080p, 1024 VPLs, 2^22 points, 128^2 ISMs in a 4096^2 atlas, 6 levels, I=8,
+# 16x16 tiles with per-tile culling).
+C2 = Config("c2_1920x1080_n1024", 1920, 1080, 512, 1024, 1 << 22, 128, 32, 32, 6, 8, 16, 8, tile=16, cull=1)
+# Reduced-precision form of C1 (FP16 atlas, FP16 normals, BF16 flux).
+C3 = C1.replace(name="c3_640x360_n256_fp16", reduced=True)
+# Reduced precision with 2048 VPLs at 96^2 ISMs on a 64x32 grid (6144x3072 atlas), 2^23 points.
+C3B = C1.replace(name="c3b_640x360_n2048_ism96_fp16", n_vpl=2048, n_points=1 << 23, ism_size=96, grid_x=64,
+                 grid_y=32, levels=5, reduced=True)
+# A tiny case for unit-sized parity checks.
+C0 = Config("c0_160x96_n64", 160, 96, 64, 64, 1 << 14, 32, 8, 8, 3, 4, 3, 1, tile=8, cull=0)
+
+CONFIGS = {c.name: c for c in (C0, C1, C2, C3, C3B)}
+
+
+@dataclasses.dataclass
+class Scene:
+    """Host arrays of one seeded room (numpy), as mlgi_scene_generate writes them."""
+    cfg: Config
+    info: SceneInfo
+    gbuf_depth: np.ndarray
+    gbuf_normal: np.ndarray   # float32 (H, W, 2) octahedral
+    gbuf_albedo: np.ndarray
+    rsm_depth: np.ndarray
+    rsm_normal: np.ndarray
+    rsm_diffuse: np.ndarray
+    points: np.ndarray        # float32 (n_buckets*stride, 4)
+    counts: np.ndarray
+    bucket_stride: int
+
+    def mat(self, name: str) -> np.ndarray:
+        return np.array(getattr(self.info, name), dtype=np.float32)
+
+
+def make_scene(cfg: Config, points: bool = True) -> Scene:
+    """Generate a seeded room on the host through mlgi_scene_generate."""
+    d = SceneDesc(cfg.seed, cfg.n_boxes, cfg.n_spheres, cfg.width, cfg.height, cfg.rsm, cfg.rsm, cfg.n_points,
+                  cfg.n_vpl, cfg.n_vpl, cfg.light_yaw_deg, cfg.light_pitch_deg, cfg.camera_orbit_deg,
+                  cfg.z_near, cfg.z_far)
+    info = SceneInfo()
+    stride = (cfg.n_points + cfg.n_vpl - 1) // cfg.n_vpl
+    W, H, R = cfg.width, cfg.height, cfg.rsm
+    gd = np.empty((H, W), np.float32)
+    gn = np.empty((H, W, 2), np.float32)
+    ga = np.empty((H, W), np.uint32)
+    rd = np.empty((R, R), np.float32)
+    rn = np.empty((R, R), np.uint32)
+    rf = np.empty((R, R), np.uint32)
+    pts = np.empty((cfg.n_vpl * stride, 4), np.float32) if points else None
+    cnt = np.empty(cfg.n_vpl, np.uint32)
+    st = lib().mlgi_scene_generate(C.byref(d), C.byref(info), ptr(gd), ptr(gn), ptr(ga), ptr(rd), ptr(rn), ptr(rf),
+                                   ptr(pts), ptr(cnt))
+    if st != OK:
+        raise MlgiError(st, "mlgi_scene_generate")
+    return Scene(cfg, info, gd, gn, ga, rd, rn, rf, pts, cnt, int(info.bucket_stride))
+
+
+def ism_params(cfg: Config) -> IsmParams:
+    return IsmParams(0, cfg.n_vpl, 0, 0, cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.levels, cfg.z_far)
+
+
+def vpl_params(cfg: Config, scene: Scene) -> VplParams:
+    return VplParams(cfg.n_vpl, cfg.light_intensity, int(cfg.shuffle), mat16(scene.mat("inv_biased_light_vp")))
+
+
+def fg_params(cfg: Config, scene: Scene) -> FgParams:
+    return FgParams(mat16(scene.mat("inv_view_proj")), cfg.z_far, cfg.gi_intensity, cfg.clamp_value, cfg.n_vpl, 0,
+                    cfg.n_vpl, 0, cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.interleave, 1, cfg.tile, cfg.cull,
+                    cfg.influence_cutoff, F16 if cfg.reduced else F32)

@@ -1,0 +1,117 @@
+"""Device-resident buffers of one GI frame, allocated with torch and handed to the C ABI.
+
+torch is used only for device memory, pinned host memory and streams; every computation is a
+libmlgi.so kernel.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import (F16, F32, Atlas, Config, FgParams, FrameDesc, GBufferView, Points, Radiance, RsmView, Scene,
+               VplBuf, fg_params, ism_params, ptr, vpl_params)
+
+
+def _t(a: np.ndarray, device):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+
+
+class DeviceFrame:
+    """Inputs, intermediate buffers and output of one frame on the GPU."""
+
+    def __init__(self, scene: Scene, device: str = "cuda"):
+        import torch
+
+        cfg: Config = scene.cfg
+        self.cfg, self.scene, self.device = cfg, scene, device
+        self.rsm_depth = _t(scene.rsm_depth, device)
+        self.rsm_normal = _t(scene.rsm_normal.view(np.int32), device)
+        self.rsm_diffuse = _t(scene.rsm_diffuse.view(np.int32), device)
+        self.points = _t(scene.points, device)
+        self.counts = _t(scene.counts.view(np.int32), device)
+        self.gbuf_depth = _t(scene.gbuf_depth, device)
+        gn = scene.gbuf_normal.astype(np.float16) if cfg.reduced else scene.gbuf_normal
+        self.gbuf_normal = _t(gn, device)
+        n = cfg.n_vpl
+        self.vpl = torch.zeros(n * 12, dtype=torch.float32, device=device)
+        self.packed = torch.zeros(n * 4, dtype=torch.float32, device=device)
+        self.reduced = torch.zeros(n * 24, dtype=torch.uint8, device=device)
+        self.keys = torch.zeros(cfg.atlas_h * cfg.atlas_w, dtype=torch.int32, device=device)
+        self.atlas = torch.zeros(cfg.atlas_h * cfg.atlas_w, dtype=torch.float16 if cfg.reduced else torch.float32,
+                                 device=device)
+        self.rgb = torch.zeros(cfg.height * cfg.width * 3, dtype=torch.float32, device=device)
+
+    # -- C structs ---------------------------------------------------------------------------
+    def rsm_view(self) -> RsmView:
+        c = self.cfg
+        return RsmView(c.rsm, c.rsm, ptr(self.rsm_depth), ptr(self.rsm_normal), ptr(self.rsm_diffuse))
+
+    def vpl_buf(self) -> VplBuf:
+        return VplBuf(self.cfg.n_vpl, ptr(self.vpl), ptr(self.packed), ptr(self.reduced))
+
+    def points_view(self) -> Points:
+        return Points(ptr(self.points), ptr(self.counts), self.cfg.n_vpl, self.scene.bucket_stride)
+
+    def atlas_view(self) -> Atlas:
+        c = self.cfg
+        return Atlas(c.atlas_w, c.atlas_h, ptr(self.keys), ptr(self.atlas), F16 if c.reduced else F32)
+
+    def gbuffer_view(self) -> GBufferView:
+        c = self.cfg
+        return GBufferView(c.width, c.height, ptr(self.gbuf_depth), ptr(self.gbuf_normal), F16 if c.reduced else F32)
+
+    def radiance(self) -> Radiance:
+        return Radiance(self.cfg.width, self.cfg.height, ptr(self.rgb))
+
+    def fg(self) -> FgParams:
+        return fg_params(self.cfg, self.scene)
+
+    def frame_desc(self) -> FrameDesc:
+        c = self.cfg
+        return FrameDesc(self.rsm_view(), vpl_params(c, self.scene), self.points_view(), ism_params(c),
+                         F16 if c.reduced else F32, self.gbuffer_view(), self.fg())
+
+    # -- host copies -----------------------------------------------------------------------
+    def vpl_records(self):
+        """(pos[N,3], normal[N,3], flux[N,3], packed_normal_bits[N]) as numpy."""
+        v = self.vpl.view(-1, 12).cpu().numpy()
+        p = self.packed.view(-1, 4).cpu().numpy()
+        return v[:, 0:3].copy(), v[:, 4:7].copy(), v[:, 8:11].copy(), p[:, 3].view(np.uint32).copy()
+
+    def keys_np(self) -> np.ndarray:
+        return self.keys.cpu().numpy().view(np.uint32).reshape(self.cfg.atlas_h, self.cfg.atlas_w)
+
+    def atlas_np(self) -> np.ndarray:
+        return self.atlas.float().cpu().numpy().reshape(self.cfg.atlas_h, self.cfg.atlas_w)
+
+    def rgb_np(self) -> np.ndarray:
+        return self.rgb.cpu().numpy().reshape(self.cfg.height, self.cfg.width, 3)
+
+
+def host_frame_desc(scene: Scene, pinned: dict) -> FrameDesc:
+    """FrameDesc whose pointers are the HOST arrays in `pinned` (for mlgi_gi_frame_host)."""
+    c = scene.cfg
+    fd = FrameDesc(RsmView(c.rsm, c.rsm, ptr(pinned["rsm_depth"]), ptr(pinned["rsm_normal"]),
+                           ptr(pinned["rsm_diffuse"])),
+                   vpl_params(c, scene),
+                   Points(ptr(pinned["points"]), ptr(pinned["counts"]), c.n_vpl, scene.bucket_stride),
+                   ism_params(c), F16 if c.reduced else F32,
+                   GBufferView(c.width, c.height, ptr(pinned["gbuf_depth"]), ptr(pinned["gbuf_normal"]),
+                               F16 if c.reduced else F32),
+                   fg_params(c, scene))
+    return fd
+
+
+def pinned_inputs(scene: Scene) -> dict:
+    """Copies of the frame's host inputs in page-locked memory (torch pin_memory)."""
+    import torch
+
+    c = scene.cfg
+    gn = scene.gbuf_normal.astype(np.float16) if c.reduced else scene.gbuf_normal
+    arrs = {"rsm_depth": scene.rsm_depth, "rsm_normal": scene.rsm_normal.view(np.int32),
+            "rsm_diffuse": scene.rsm_diffuse.view(np.int32), "points": scene.points,
+            "counts": scene.counts.view(np.int32), "gbuf_depth": scene.gbuf_depth, "gbuf_normal": gn}
+    out = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in arrs.items()}
+    out["rgb"] = torch.zeros(c.height * c.width * 3, dtype=torch.float32).pin_memory()
+    return out

@@ -1,0 +1,80 @@
+"""CPU-side checks of the C ABI: the library loads, exports every declared symbol, and the host
+entry points (scene fixture, shuffle table, host sizes, status strings) behave."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+import mlgi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "mlgi.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mlgi_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = mlgi.lib()
+    names = header_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(mlgi.declared_symbols()) == sorted(n for n in names if n in mlgi.declared_symbols())
+
+
+def test_status_strings():
+    L = mlgi.lib()
+    assert L.mlgi_status_string(mlgi.OK) == b"ok"
+    assert L.mlgi_status_string(mlgi.ETIMEDOUT) == b"device wait timed out"
+
+
+def test_null_context_is_rejected():
+    L = mlgi.lib()
+    assert L.mlgi_vpl_process(None, None, None, None, None) == mlgi.EINVAL
+    assert L.mlgi_gi_frame(None, None, None, None) == mlgi.EINVAL
+
+
+def test_shuffle_table_matches_std_shuffle_prefix():
+    # VPLProcessor.cpp:58-65 with libstdc++: pinned prefix of the 1024-entry permutation.
+    p = mlgi.shuffle_table(1024)
+    assert sorted(p.tolist()) == list(range(1024))
+    golden = np.load(os.path.join(ROOT, "tests", "golden", "shuffle_1024.npy"))
+    assert (p == golden).all()
+
+
+def test_scene_is_deterministic_and_well_formed():
+    cfg = mlgi.C0
+    a = mlgi.make_scene(cfg)
+    b = mlgi.make_scene(cfg)
+    for k in ("gbuf_depth", "gbuf_normal", "rsm_depth", "rsm_normal", "rsm_diffuse", "points", "counts"):
+        assert (getattr(a, k) == getattr(b, k)).all(), k
+    assert a.counts.sum() == cfg.n_points
+    assert (a.gbuf_depth > 0).all() and (a.gbuf_depth <= 1).all()
+    assert np.abs(a.gbuf_normal).max() <= 1.0
+    # points inside the room, radius byte as packed from the area per point
+    p = a.points[: a.counts[0]]
+    assert (p[:, :3] >= -1e-3).all() and (p[:, :3] <= 100 + 1e-3).all()
+    rbyte = p[:, 3].view(np.uint32) >> 24
+    r = np.sqrt(a.info.total_area / (cfg.n_points * np.pi)) * np.sqrt(cfg.n_vpl)
+    assert (rbyte == round(r / 25 * 255)).all()
+    c = mlgi.make_scene(cfg.replace(seed=2))
+    assert not (c.gbuf_depth == a.gbuf_depth).all()
+
+
+def test_frame_host_sizes():
+    cfg = mlgi.C1
+    sc = mlgi.make_scene(cfg, points=False)
+    fd = mlgi.FrameDesc()
+    fd.rsm.width = fd.rsm.height = cfg.rsm
+    fd.points.n_buckets = cfg.n_vpl
+    fd.points.bucket_stride = sc.bucket_stride
+    fd.gbuffer.width, fd.gbuffer.height = cfg.width, cfg.height
+    z = mlgi.FrameHostSizes()
+    assert mlgi.lib().mlgi_frame_host_sizes_get(C.byref(fd), C.byref(z)) == mlgi.OK
+    assert z.points == cfg.n_vpl * sc.bucket_stride * 16
+    assert z.radiance == cfg.width * cfg.height * 12
+    assert z.gbuf_normal == cfg.width * cfg.height * 8

@@ -1,0 +1,291 @@
+"""GPU parity: each CUDA pass, called through the C ABI, against the CPU oracle.
+
+Bar (stated per test): VPL records, ISM keys and the FP32 pull-push atlas are bit-exact with the
+oracle's FP32 restatement of the reference shaders; gathered radiance is within a relative L2 of
+1e-3 of the FP64 oracle on identical inputs (max-abs reported in the failure message).
+"""
+import numpy as np
+import pytest
+
+import mlgi
+from mlgi.device import DeviceFrame, host_frame_desc, pinned_inputs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FG_REL_L2 = 1e-3  # FP32 gather vs FP64 oracle, relative L2 over the image
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = mlgi.Context(0)
+    yield c
+    c.close()
+
+
+_scenes = {}
+
+
+def scene(cfg):
+    if cfg.name not in _scenes:
+        _scenes[cfg.name] = mlgi.make_scene(cfg)
+    return _scenes[cfg.name]
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-30))
+
+
+def oracle_vpls(cfg, sc, dtype=np.float32):
+    perm = mlgi.shuffle_table(cfg.n_vpl) if cfg.shuffle else None
+    return O.vpl_process(sc.rsm_depth, sc.rsm_normal, sc.rsm_diffuse, cfg.n_vpl, sc.mat("inv_biased_light_vp"),
+                         cfg.light_intensity, int(cfg.shuffle), perm, dtype=dtype)
+
+
+def run_vpl(ctx, df):
+    import torch
+
+    ctx.vpl_process(df.rsm_view(), mlgi.vpl_params(df.cfg, df.scene), df.vpl_buf())
+    torch.cuda.synchronize()
+
+
+CFGS_SMALL = [mlgi.C0, mlgi.C1]
+
+
+@pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2, mlgi.C1.replace(shuffle=False, name="c1_noshuffle")],
+                         ids=lambda c: c.name)
+def test_vpl_process_bit_exact(ctx, cfg):
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    pos, nrm, col, pn = df.vpl_records()
+    opos, onrm, ocol, opn = oracle_vpls(cfg, sc)
+    assert (pn == opn).all()
+    assert (pos.view(np.uint32) == opos.view(np.uint32)).all()
+    assert (nrm.view(np.uint32) == onrm.view(np.uint32)).all()
+    assert (col.view(np.uint32) == ocol.view(np.uint32)).all()
+
+
+@pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2], ids=lambda c: c.name)
+def test_ism_splat_bit_exact(ctx, cfg):
+    import torch
+
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    ctx.ism_splat(df.points_view(), df.vpl_buf(), cfg.n_vpl, mlgi.ism_params(cfg), df.atlas_view())
+    torch.cuda.synchronize()
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    keys = df.keys_np()
+    assert (okeys != 0xFFFFFFFF).mean() > 0.05  # the case does splat something
+    mism = int((keys != okeys).sum())
+    assert mism == 0, f"{mism} of {keys.size} atlas words differ"
+
+
+def test_ism_splat_vpl_subrange_and_scaled_isms(ctx):
+    """VPLStartIndex/EndIndex with ScaleISMs and PointsOnlyToScaledISMs (ism.comp:31-40,56-66)."""
+    import torch
+
+    cfg = mlgi.C0
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    start, end = 16, 48
+    ip = mlgi.ism_params(cfg)
+    ip.vpl_start, ip.vpl_end, ip.scale_isms, ip.points_only_scaled = start, end, 1, 1
+    pts = df.points_view()
+    pts.n_buckets = end - start
+    ctx.ism_splat(pts, df.vpl_buf(), cfg.n_vpl, ip, df.atlas_view())
+    torch.cuda.synchronize()
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far, vpl_start=start, vpl_end=end, scale_isms=1, points_only=1)
+    assert (df.keys_np() == okeys).all()
+
+
+def test_ism_splat_empty_buckets(ctx):
+    import torch
+
+    cfg = mlgi.C0
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    df.counts.zero_()
+    ctx.ism_splat(df.points_view(), df.vpl_buf(), cfg.n_vpl, mlgi.ism_params(cfg), df.atlas_view())
+    torch.cuda.synchronize()
+    assert (df.keys_np() == 0xFFFFFFFF).all()
+
+
+@pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2, mlgi.C3B.replace(reduced=False, name="c3b_fp32")],
+                         ids=lambda c: c.name)
+def test_pullpush_bit_exact(ctx, cfg):
+    """Fused per-ISM pyramid vs the level-by-level restatement of pull.comp/push.comp."""
+    import torch
+
+    sc = scene(cfg)
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    ofin = O.pullpush(okeys, cfg.ism_size, cfg.levels, cfg.z_far)
+    df = DeviceFrame(sc)
+    df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
+    ctx.pullpush(df.atlas_view(), mlgi.ism_params(cfg))
+    torch.cuda.synchronize()
+    fin = df.atlas_np()
+    assert (ofin < 0.99).mean() > (okeys >> 8 < 0.99 * 2 ** 24).mean()  # the pyramid fills holes
+    mism = int((fin.view(np.uint32) != ofin.view(np.uint32)).sum())
+    assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
+
+
+def test_pullpush_fp16_atlas_is_rounded_fp32(ctx):
+    import torch
+
+    cfg = mlgi.C3
+    sc = scene(cfg)
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    ofin = O.pullpush(okeys, cfg.ism_size, cfg.levels, cfg.z_far)
+    df = DeviceFrame(sc)
+    df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
+    ctx.pullpush(df.atlas_view(), mlgi.ism_params(cfg))
+    torch.cuda.synchronize()
+    assert (df.atlas.cpu().numpy().reshape(ofin.shape) == ofin.astype(np.float16)).all()
+
+
+def _fg_inputs(ctx, cfg):
+    """Run the GPU chain up to the atlas; return the frame and oracle-side copies of its inputs."""
+    import torch
+
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    ctx.ism_splat(df.points_view(), df.vpl_buf(), cfg.n_vpl, mlgi.ism_params(cfg), df.atlas_view())
+    ctx.pullpush(df.atlas_view(), mlgi.ism_params(cfg))
+    torch.cuda.synchronize()
+    return sc, df
+
+
+def _oracle_fg(cfg, sc, df, dtype, tile=0, cutoff=0.0, reduced_inputs=False):
+    pos, nrm, col, _ = df.vpl_records()
+    gn = sc.gbuf_normal
+    if reduced_inputs:  # the reduced path's stored values, widened back
+        rec = df.reduced.cpu().numpy().view(np.uint8).reshape(-1, 24)
+        pos = rec[:, 0:12].copy().view(np.float32).reshape(-1, 3)
+        nrm = rec[:, 12:18].copy().view(np.float16).astype(np.float32).reshape(-1, 3)
+        fl = rec[:, 18:24].copy().view(np.uint16).astype(np.uint32) << 16
+        col = fl.view(np.float32).reshape(-1, 3)
+        gn = sc.gbuf_normal.astype(np.float16).astype(np.float32)
+    atlas = df.atlas_np()
+    return O.final_gather(sc.gbuf_depth, gn, sc.mat("inv_view_proj").astype(dtype), pos.astype(dtype),
+                          nrm.astype(dtype), col.astype(dtype), atlas, cfg.ism_size, cfg.grid_x, cfg.grid_y,
+                          cfg.z_far, cfg.gi_intensity, cfg.clamp_value, cfg.interleave, tile=tile, cutoff=cutoff,
+                          dtype=dtype)
+
+
+@pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C1.replace(interleave=8, tile=8, name="c1_i8_t8"),
+                                              mlgi.C1.replace(interleave=1, name="c1_i1")], ids=lambda c: c.name)
+def test_final_gather_matches_fp64_oracle(ctx, cfg):
+    import torch
+
+    sc, df = _fg_inputs(ctx, cfg)
+    ctx.final_gather(df.gbuffer_view(), df.vpl_buf(), df.atlas_view(), df.fg(), df.radiance())
+    ctx.check_device_status()
+    torch.cuda.synchronize()
+    rgb = df.rgb_np()
+    ref = _oracle_fg(cfg, sc, df, np.float64)
+    e = rel_l2(rgb, ref)
+    assert e < FG_REL_L2, f"rel L2 {e:.3e}, max abs {np.abs(rgb - ref).max():.3e}"
+    assert np.abs(ref).max() > 0
+
+
+def test_final_gather_culling_c2(ctx):
+    """C2: 16x16 same-class tiles with culling. The lossless half-space cull must match the FP64
+    oracle that applies the same rule, and the no-cull FP64 oracle within the same bar."""
+    import torch
+
+    cfg = mlgi.C2
+    sc, df = _fg_inputs(ctx, cfg)
+    ctx.final_gather(df.gbuffer_view(), df.vpl_buf(), df.atlas_view(), df.fg(), df.radiance())
+    torch.cuda.synchronize()
+    rgb = df.rgb_np()
+    ref_nocull = _oracle_fg(cfg, sc, df, np.float64)
+    e = rel_l2(rgb, ref_nocull)
+    assert e < FG_REL_L2, f"C2 culled vs unculled FP64: rel L2 {e:.3e}"
+
+
+def test_reduced_precision_error_c3(ctx):
+    """C3: FP16 atlas, FP16 normals, BF16 flux. FG on the stored reduced values matches the FP64
+    oracle on the same widened values; the end-to-end error against the FP32 chain is stated."""
+    import torch
+
+    cfg = mlgi.C3
+    sc, df = _fg_inputs(ctx, cfg)
+    ctx.final_gather(df.gbuffer_view(), df.vpl_buf(), df.atlas_view(), df.fg(), df.radiance())
+    torch.cuda.synchronize()
+    rgb = df.rgb_np()
+    same_inputs = _oracle_fg(cfg, sc, df, np.float64, reduced_inputs=True)
+    assert rel_l2(rgb, same_inputs) < FG_REL_L2
+    full = mlgi.C1
+    sc32, df32 = _fg_inputs(ctx, full)
+    ref32 = _oracle_fg(full, sc32, df32, np.float64)
+    e = rel_l2(rgb, ref32)
+    assert e < 2e-2, f"reduced-precision chain vs FP64 oracle: rel L2 {e:.3e}"
+
+
+def test_frame_chain_and_host_frame_agree(ctx):
+    import torch
+
+    cfg = mlgi.C1
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    ctx.gi_frame(df.frame_desc(), df.radiance())
+    torch.cuda.synchronize()
+    dev = df.rgb_np().copy()
+    pinned = pinned_inputs(sc)
+    ctx.gi_frame_host(host_frame_desc(sc, pinned), pinned["rgb"].numpy())
+    host = pinned["rgb"].numpy().reshape(dev.shape)
+    assert (dev == host).all()
+    # and the chain equals the stage-by-stage oracle within the FG bar
+    opos, onrm, ocol, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    ofin = O.pullpush(okeys, cfg.ism_size, cfg.levels, cfg.z_far)
+    ref = O.final_gather(sc.gbuf_depth, sc.gbuf_normal, sc.mat("inv_view_proj").astype(np.float64),
+                         opos.astype(np.float64), onrm.astype(np.float64), ocol.astype(np.float64), ofin,
+                         cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.z_far, cfg.gi_intensity, cfg.clamp_value,
+                         cfg.interleave, dtype=np.float64)
+    assert rel_l2(dev, ref) < FG_REL_L2
+
+
+def test_frame_is_deterministic(ctx):
+    import torch
+
+    cfg = mlgi.C1
+    df = DeviceFrame(scene(cfg))
+    outs = []
+    for _ in range(3):
+        ctx.gi_frame(df.frame_desc(), df.radiance())
+        torch.cuda.synchronize()
+        outs.append(df.rgb_np().copy())
+    assert all((o == outs[0]).all() for o in outs[1:])
+
+
+def test_invalid_arguments_are_rejected(ctx):
+    cfg = mlgi.C0
+    df = DeviceFrame(scene(cfg))
+    vp = mlgi.vpl_params(cfg, df.scene)
+    vp.count = 100  # not a multiple of 64
+    with pytest.raises(mlgi.MlgiError) as e:
+        ctx.vpl_process(df.rsm_view(), vp, df.vpl_buf())
+    assert e.value.status == mlgi.EINVAL
+    ip = mlgi.ism_params(cfg)
+    ip.ism_size = 30  # not divisible by 2^levels and mismatching the atlas
+    with pytest.raises(mlgi.MlgiError):
+        ctx.pullpush(df.atlas_view(), ip)
+    fp = df.fg()
+    fp.interleave = 3  # 64 VPLs are not a multiple of 9
+    with pytest.raises(mlgi.MlgiError):
+        ctx.final_gather(df.gbuffer_view(), df.vpl_buf(), df.atlas_view(), fp, df.radiance())
