@@ -25,6 +25,7 @@ CUDA_UNITS = [
     ("csrc/ism_kernels.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     ("csrc/fg_kernels.cu", []),
     ("csrc/mlgi_api.cu", []),
+    ("csrc/ism_static.cu", []),
     ("csrc/batch.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     ("host/serve.cpp", []),
     ("host/autotune.cpp", []),

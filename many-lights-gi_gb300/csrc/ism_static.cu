@@ -1,0 +1,120 @@
+// Allocation-free ISM rendering: splat + pull-push with the softrender key atlas held in a
+// fixed, statically allocated device array instead of caller- or context-owned memory.
+//
+// Who needs it: code that must not call cudaMalloc -- e.g. a renderer running inside a host
+// process whose device memory is fully reserved up front by another allocator, a plugin that is
+// only handed pre-allocated buffers, or a callback that runs while the CUDA allocator is locked.
+// Such callers still pass their own input (points, VPLs) and output (final depth atlas) buffers;
+// only the intermediate key atlas lives here.
+//
+// Limits and behaviour:
+//   * The key atlas holds at most kStaticKeyTexels = 1,048,576 texels (a 1024 x 1024 atlas,
+//     4 MiB). Larger atlases are rejected with MLGI_EINVAL. Every GPU that loads this library
+//     keeps those 4 MiB reserved until the process exits.
+//   * The first call on a device resolves the array's device address (cudaGetSymbolAddress)
+//     with that device current; make that first call before any stream capture.
+//   * All calls share the one array. Each call clears it to the empty key (0xFFFFFFFF) before
+//     splatting, so nothing of a previous call leaks into the result, but calls whose work
+//     overlaps on the GPU (different streams, or different host threads) race on it.
+//   * No cudaMalloc, cudaFree or allocating library call is made.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "kernels.h"
+#include "mlgi.h"
+
+namespace {
+
+constexpr size_t kStaticKeyTexels = size_t(1) << 20;
+
+__device__ __align__(256) uint32_t g_static_keys[kStaticKeyTexels];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+uint32_t* g_static_keys_dev[kMaxDevices] = {};
+
+// Device address of g_static_keys on the current device (resolved once per device).
+mlgi_status static_keys_address(uint32_t** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return MLGI_ECUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) return MLGI_EINVAL;
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_static_keys_dev[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_keys);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return MLGI_ECUDA;
+        }
+        g_static_keys_dev[dev] = static_cast<uint32_t*>(p);
+    }
+    *out = g_static_keys_dev[dev];
+    return MLGI_OK;
+}
+
+}  // namespace
+
+extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                                              const mlgi_ism_params* p, void* depth_out, int depth_format,
+                                              mlgi_stream stream) {
+    if (!pts || !vpls || !p || !depth_out) return MLGI_EINVAL;
+    if (depth_format != MLGI_F32 && depth_format != MLGI_F16) return MLGI_EINVAL;
+    if (p->ism_size <= 0 || p->grid_x <= 0 || p->grid_y <= 0 || p->levels < 1 || p->levels > 10 ||
+        p->ism_size % (1 << p->levels) != 0 || !(p->z_far > 0.f))
+        return MLGI_EINVAL;
+    const size_t aw = (size_t)p->grid_x * p->ism_size, ah = (size_t)p->grid_y * p->ism_size;
+    if (aw * ah > kStaticKeyTexels) return MLGI_EINVAL;  // beyond the static key atlas
+    if (p->vpl_start < 0 || p->vpl_end <= p->vpl_start || n_vpl <= 0 || n_vpl > vpls->capacity ||
+        p->vpl_end > n_vpl)
+        return MLGI_EINVAL;
+    const int vplCount = p->vpl_end - p->vpl_start;
+    if ((p->scale_isms ? vplCount : n_vpl) > p->grid_x * p->grid_y) return MLGI_EINVAL;
+    if (pts->n_buckets != (p->points_only_scaled ? vplCount : n_vpl)) return MLGI_EINVAL;
+    if (pts->n_buckets > 0 && (!pts->points || !pts->counts || pts->bucket_stride < 0)) return MLGI_EINVAL;
+    if (!vpls->packed || (reinterpret_cast<uintptr_t>(vpls->packed) & 15) ||
+        (reinterpret_cast<uintptr_t>(pts->points) & 15))
+        return MLGI_EINVAL;
+    if (mlgi::pullpush_smem_bytes(p->ism_size, p->levels) > 227 * 1024) return MLGI_EINVAL;
+
+    uint32_t* keys = nullptr;
+    const mlgi_status st = static_keys_address(&keys);
+    if (st != MLGI_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    if (mlgi::launch_ism_clear(keys, aw * ah, s) != cudaSuccess) return MLGI_ECUDA;
+    mlgi::SplatArgs a{};
+    a.points = reinterpret_cast<const float4*>(pts->points);
+    a.counts = pts->counts;
+    a.bucket_stride = pts->bucket_stride;
+    a.n_groups = pts->n_buckets;
+    a.packed = reinterpret_cast<const float4*>(vpls->packed);
+    a.n_vpl = n_vpl;
+    a.vpl_start = p->vpl_start;
+    a.vpl_end = p->vpl_end;
+    a.scale_isms = p->scale_isms;
+    a.points_only_scaled = p->points_only_scaled;
+    a.gx = p->grid_x;
+    a.gy = p->grid_y;
+    a.atlas_w = (int)aw;
+    a.atlas_h = (int)ah;
+    a.z_far = p->z_far;
+    a.keys = keys;
+    if (mlgi::launch_ism_splat(a, s) != cudaSuccess) return MLGI_ECUDA;
+    mlgi::PullPushArgs q{};
+    q.keys = keys;
+    q.out = depth_out;
+    q.out_f16 = depth_format == MLGI_F16;
+    q.atlas_w = (int)aw;
+    q.atlas_h = (int)ah;
+    q.ism_size = p->ism_size;
+    q.levels = p->levels;
+    q.grid_x = p->grid_x;
+    q.grid_y = p->grid_y;
+    q.z_far = p->z_far;
+    if (mlgi::launch_pullpush(q, s) != cudaSuccess) return MLGI_ECUDA;
+    return MLGI_OK;
+}

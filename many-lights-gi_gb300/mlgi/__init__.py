@@ -108,6 +108,8 @@ _SIGS = {
     "mlgi_ism_splat": (C.c_int32, [_p, C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams),
                                    C.POINTER(Atlas), _p]),
     "mlgi_pullpush": (C.c_int32, [_p, C.POINTER(Atlas), C.POINTER(IsmParams), _p]),
+    "mlgi_ism_render_static": (C.c_int32, [C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams), _p,
+                                           C.c_int, _p]),
     "mlgi_final_gather": (C.c_int32, [_p, C.POINTER(GBufferView), C.POINTER(VplBuf), C.POINTER(Atlas),
                                       C.POINTER(FgParams), C.POINTER(Radiance), _p]),
     "mlgi_gi_frame": (C.c_int32, [_p, C.POINTER(FrameDesc), C.POINTER(Radiance), _p]),
