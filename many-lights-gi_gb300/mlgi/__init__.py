@@ -293,10 +293,14 @@ C3 = C1.replace(name="c3_640x360_n256_fp16", reduced=True)
 # Reduced precision with 2048 VPLs at 96^2 ISMs on a 64x32 grid (6144x3072 atlas), 2^23 points.
 C3B = C1.replace(name="c3b_640x360_n2048_ism96_fp16", n_vpl=2048, n_points=1 << 23, ism_size=96, grid_x=64,
                  grid_y=32, levels=5, reduced=True)
+# The reference's own defaults where its shaders hard-code them: 1024 VPLs, 64^2 ISMs in a 2048^2
+# atlas (ImperfectShadowmap.cpp:34), 6 pull-push levels, interleave 4 (final_gathering.comp:53);
+# only axis-aligned geometry, so G-buffer normals are exact in every encoding.
+CREF = Config("cref_640x360_n1024_ism64", 640, 360, 512, 1024, 1 << 20, 64, 32, 32, 6, 4, 8, 0, tile=16, cull=0)
 # A tiny case for unit-sized parity checks.
 C0 = Config("c0_160x96_n64", 160, 96, 64, 64, 1 << 14, 32, 8, 8, 3, 4, 3, 1, tile=8, cull=0)
 
-CONFIGS = {c.name: c for c in (C0, C1, C2, C3, C3B)}
+CONFIGS = {c.name: c for c in (C0, C1, C2, C3, C3B, CREF)}
 
 
 @dataclasses.dataclass

@@ -14,6 +14,9 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <stdexcept>
+#include <type_traits>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -45,10 +48,14 @@ struct Swz {
         if constexpr (N == 3) p[C] = v.z;
     }
     Swz& operator=(const VT& v) { set(v); return *this; }
-    template <class U> Swz& operator+=(const U& o) { set(get() + o); return *this; }
-    template <class U> Swz& operator-=(const U& o) { set(get() - o); return *this; }
-    template <class U> Swz& operator*=(const U& o) { set(get() * o); return *this; }
-    template <class U> Swz& operator/=(const U& o) { set(get() / o); return *this; }
+    template <class U> Swz& operator+=(const U& o) { set(VT(get() + unswz(o))); return *this; }
+    template <class U> Swz& operator-=(const U& o) { set(VT(get() - unswz(o))); return *this; }
+    template <class U> Swz& operator*=(const U& o) { set(VT(get() * unswz(o))); return *this; }
+    template <class U> Swz& operator/=(const U& o) { set(VT(get() / unswz(o))); return *this; }
+    template <class U> static decltype(auto) unswz(const U& o) {
+        if constexpr (requires { o.get(); }) return o.get();
+        else return (o);
+    }
 };
 
 template <class T> struct V2 {
@@ -59,6 +66,7 @@ template <class T> struct V2 {
     V2(A a, B b) : x(T(a)), y(T(b)) {}
     explicit V2(T s) : x(s), y(s) {}
     template <class U> explicit V2(const V2<U>& o) : x(T(o.x)), y(T(o.y)) {}
+    template <class S, class = decltype(std::declval<S>().get().y)> explicit V2(const S& s) : V2(s.get()) {}
     T& operator[](int i) { return (&x)[i]; }
     T operator[](int i) const { return (&x)[i]; }
     Swz<T, 2, 0, 1> xy() { return {&x}; }
@@ -176,6 +184,25 @@ auto operator*(const Swz<T, N, A, B, C>& s, const U& u) { return s.get() * u; }
 template <class T, int N, int A, int B, int C, class U>
 auto operator/(const Swz<T, N, A, B, C>& s, const U& u) { return s.get() / u; }
 
+template <class X> struct is_swz : std::false_type {};
+template <class T, int N, int A, int B, int C> struct is_swz<Swz<T, N, A, B, C>> : std::true_type {};
+template <class X> decltype(auto) val(const X& x) {
+    if constexpr (is_swz<X>::value) return x.get();
+    else return (x);
+}
+template <class X, class Y, class = std::enable_if_t<is_swz<Y>::value && !is_swz<X>::value>>
+auto operator*(const X& a, const Y& b) { return a * b.get(); }
+template <class X, class Y, class = std::enable_if_t<is_swz<Y>::value && !is_swz<X>::value>>
+auto operator+(const X& a, const Y& b) { return a + b.get(); }
+template <class X, class Y, class = std::enable_if_t<is_swz<Y>::value && !is_swz<X>::value>>
+auto operator-(const X& a, const Y& b) { return a - b.get(); }
+template <class X, class Y, class = std::enable_if_t<is_swz<Y>::value && !is_swz<X>::value>>
+auto operator/(const X& a, const Y& b) { return a / b.get(); }
+template <class T, int N, int A, int B, int C, class S>
+auto operator>>(const Swz<T, N, A, B, C>& s, S k) { return s.get() >> k; }
+template <class T, int N, int A, int B, int C, class S>
+auto operator&(const Swz<T, N, A, B, C>& s, S k) { return s.get() & k; }
+
 template <class T> V2<T>& operator+=(V2<T>& a, const V2<T>& b) { a = a + b; return a; }
 template <class T> V3<T>& operator+=(V3<T>& a, const V3<T>& b) { a = a + b; return a; }
 template <class T> V4<T>& operator+=(V4<T>& a, const V4<T>& b) { a = a + b; return a; }
@@ -189,10 +216,6 @@ template <class T, class S> V2<T> operator>>(const V2<T>& a, S s) { return V2<T>
 template <class T, class S> V2<T> operator&(const V2<T>& a, S s) { return V2<T>(a.x & s, a.y & s); }
 template <class T> bool operator!=(const V2<T>& a, const V2<T>& b) { return a.x != b.x || a.y != b.y; }
 template <class T> bool operator==(const V2<T>& a, const V2<T>& b) { return a.x == b.x && a.y == b.y; }
-template <class T> V2<T> operator/(const V2<T>& a, int s) {
-    if constexpr (std::is_floating_point_v<T>) return V2<T>(a.x / T(s), a.y / T(s));
-    else return V2<T>(a.x / T(s), a.y / T(s));
-}
 
 // ---- scalar built-ins --------------------------------------------------------------------------
 inline float sqrt(float x) { return std::sqrt(x); }
@@ -206,6 +229,7 @@ inline float mod(float x, float y) { return x - y * std::floor(x / y); }
 inline float min(float x, float y) { return y < x ? y : x; }
 inline float max(float x, float y) { return x < y ? y : x; }
 inline float max(float x, int y) { return max(x, float(y)); }
+inline float min(float x, int y) { return min(x, float(y)); }
 inline int min(int x, int y) { return y < x ? y : x; }
 inline float clamp(float x, float a, float b) { return min(max(x, a), b); }
 inline float step(float e, float x) { return x < e ? 0.0f : 1.0f; }
@@ -284,9 +308,14 @@ struct ImageBuffer {
     float* f = nullptr;
     int n = 0;
 };
+struct UImage2D {
+    uint* u = nullptr;
+    int w = 0, h = 0;
+    int comps = 1;
+};
 using image2D = Image2D;
-using uimage2D = Image2D;
-using uimage1D = Image2D;
+using uimage2D = UImage2D;
+using uimage1D = UImage2D;
 using uimage3D = Image3D;
 using imageBuffer = ImageBuffer;
 struct Sampler2D {
@@ -295,8 +324,12 @@ struct Sampler2D {
     int w = 0, h = 0;
     bool repeat = true;
 };
+struct USampler2D {
+    const uint* u = nullptr;  // one uint per texel
+    int w = 0, h = 0;
+};
 using sampler2D = Sampler2D;
-using usampler2D = Sampler2D;
+using usampler2D = USampler2D;
 struct sampler3D {};
 
 struct IntScalar {  // imageSize of a buffer image: an int that also answers .x
@@ -306,17 +339,17 @@ struct IntScalar {  // imageSize of a buffer image: an int that also answers .x
 
 inline vec4 imageLoad(const Image2D& im, ivec2 p) {
     if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return vec4();
-    const float* t = im.f + 4 * ((size_t)p.y * im.w + p.x);
+    const float* t = im.f + (size_t)im.comps * ((size_t)p.y * im.w + p.x);
+    if (im.comps == 1) return vec4(t[0], 0.f, 0.f, 1.f);
     return vec4(t[0], t[1], t[2], t[3]);
 }
-inline uvec4 imageLoad_u(const Image2D& im, ivec2 p) {
+inline uvec4 imageLoad(const UImage2D& im, ivec2 p) {
     if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return uvec4();
-    const uint* t = im.u + 4 * ((size_t)p.y * im.w + p.x);
-    return uvec4(t[0], t[1], t[2], t[3]);
+    return uvec4(im.u[(size_t)p.y * im.w + p.x], 0u, 0u, 1u);
 }
 inline uvec4 imageLoad(const Image3D& im, ivec3 p) {
     if (p.x < 0 || p.y < 0 || p.z < 0 || p.x >= im.w || p.y >= im.h || p.z >= im.d) return uvec4();
-    return uvec4(im.u[((size_t)p.z * im.h + p.y) * im.w + p.x], 0u, 0u, 0u);
+    return uvec4(im.u[((size_t)p.z * im.h + p.y) * im.w + p.x], 0u, 0u, 1u);
 }
 inline vec4 imageLoad(const ImageBuffer& im, int i) {
     if (i < 0 || i >= im.n) return vec4();
@@ -325,43 +358,39 @@ inline vec4 imageLoad(const ImageBuffer& im, int i) {
 }
 inline void imageStore(Image2D& im, ivec2 p, vec4 v) {
     if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return;
-    float* t = im.f + 4 * ((size_t)p.y * im.w + p.x);
-    t[0] = v.x; t[1] = v.y; t[2] = v.z; t[3] = v.w;
+    float* t = im.f + (size_t)im.comps * ((size_t)p.y * im.w + p.x);
+    t[0] = v.x;
+    if (im.comps == 4) { t[1] = v.y; t[2] = v.z; t[3] = v.w; }
 }
-inline void imageStore(Image2D& im, ivec2 p, uvec4 v) {
+inline void imageStore(UImage2D& im, ivec2 p, uvec4 v) {
     if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return;
-    uint* t = im.u + 4 * ((size_t)p.y * im.w + p.x);
-    t[0] = v.x; t[1] = v.y; t[2] = v.z; t[3] = v.w;
+    im.u[(size_t)p.y * im.w + p.x] = v.x;
 }
-inline void imageStore(Image2D& im, int i, uvec4 v) { imageStore(im, ivec2(i, 0), v); }
 inline void imageStore(ImageBuffer& im, int i, vec4 v) {
     if (i < 0 || i >= im.n) return;
     float* t = im.f + 4 * (size_t)i;
     t[0] = v.x; t[1] = v.y; t[2] = v.z; t[3] = v.w;
 }
-inline uint imageAtomicMin(Image2D& im, ivec2 p, uint v) {
+inline uint imageAtomicMin(UImage2D& im, ivec2 p, uint v) {
     if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return 0;
-    uint* t = im.u + 4 * ((size_t)p.y * im.w + p.x);
+    uint* t = im.u + ((size_t)p.y * im.w + p.x);
     uint cur = __atomic_load_n(t, __ATOMIC_RELAXED);
     while (v < cur && !__atomic_compare_exchange_n(t, &cur, v, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
     }
     return cur;
 }
 inline ivec2 imageSize(const Image2D& im) { return ivec2(im.w, im.h); }
+inline ivec2 imageSize(const UImage2D& im) { return ivec2(im.w, im.h); }
 inline IntScalar imageSize(const ImageBuffer& im) { return IntScalar{im.n}; }
 
-struct TexelF {  // texelFetch result of a float sampler
-    vec4 v;
-};
 inline vec4 texelFetch(const Sampler2D& s, ivec2 p, int) {
     if (p.x < 0 || p.y < 0 || p.x >= s.w || p.y >= s.h) return vec4();
     const float* t = s.f + 4 * ((size_t)p.y * s.w + p.x);
     return vec4(t[0], t[1], t[2], t[3]);
 }
-inline uvec4 texelFetch_u(const Sampler2D& s, ivec2 p, int) {
+inline uvec4 texelFetch(const USampler2D& s, ivec2 p, int) {
     if (p.x < 0 || p.y < 0 || p.x >= s.w || p.y >= s.h) return uvec4();
-    const uint* t = s.u + 4 * ((size_t)p.y * s.w + p.x);
-    return uvec4(t[0], t[1], t[2], t[3]);
+    return uvec4(s.u[(size_t)p.y * s.w + p.x], 0u, 0u, 1u);
 }
 inline ivec2 textureSize(const Sampler2D& s, int) { return ivec2(s.w, s.h); }
 // Nearest filtering with GL_REPEAT wrap (the default wrap of the reference's ISM result texture).
@@ -373,17 +402,56 @@ inline vec4 textureLod(const Sampler2D& s, vec2 uv, float) {
 }
 inline vec4 texture(const Sampler2D& s, vec2 uv, float = 0) { return textureLod(s, uv, 0); }
 inline vec4 texture(const sampler3D&, vec3) { return vec4(); }
+inline vec2 floor(vec2 v) { return vec2(std::floor(v.x), std::floor(v.y)); }
 
-// ---- per-invocation built-ins and the work-group scheduler hook ------------------------------
-struct Bindings;  // defined by the harness
-
-struct RefShaderBase {
-    uvec3 gl_WorkGroupID, gl_LocalInvocationID, gl_NumWorkGroups, gl_WorkGroupSize;
-    Bindings* B;
-    explicit RefShaderBase(Bindings* b) : B(b) {}
+// ---- bindings, per-invocation built-ins and the work-group scheduler hook ---------------------
+struct Bindings {
+    std::map<std::string, std::vector<unsigned char>> values;  // uniforms (raw bytes of the C++ type)
+    std::map<std::string, void*> buffers;                      // interface-block members
+    uvec3 local_size, num_groups;
+    template <class T> void set(const std::string& n, const T& v) {
+        auto& b = values[n];
+        b.resize(sizeof(T));
+        std::memcpy(b.data(), &v, sizeof(T));
+    }
+    template <class T> bool get(const std::string& n, T& v) const {
+        auto it = values.find(n);
+        if (it == values.end() || it->second.size() != sizeof(T)) return false;
+        std::memcpy(&v, it->second.data(), sizeof(T));
+        return true;
+    }
 };
 
-void barrier();  // yields the current invocation's fiber
+// The work group's shared arena, owned by the worker thread that runs the group.
+extern thread_local std::map<std::string, std::vector<unsigned char>>* tl_shared_arena;
+
+struct RefShaderBase {
+    Bindings* B;
+    uvec3 gl_WorkGroupID, gl_LocalInvocationID, gl_NumWorkGroups, gl_WorkGroupSize;
+    explicit RefShaderBase(Bindings* b) : B(b), gl_NumWorkGroups(b->num_groups), gl_WorkGroupSize(b->local_size) {}
+    template <class T> T uni(const char* n) const {
+        T v{};
+        if (!B->get(n, v)) throw std::runtime_error(std::string("unbound uniform ") + n);
+        return v;
+    }
+    template <class T, class D> T uni(const char* n, const D& def) const {
+        T v{};
+        if (!B->get(n, v)) v = T(def);
+        return v;
+    }
+    template <class T> T* buf(const char* n) const {
+        auto it = B->buffers.find(n);
+        if (it == B->buffers.end()) throw std::runtime_error(std::string("unbound buffer ") + n);
+        return static_cast<T*>(it->second);
+    }
+    template <class T> T* shared_mem(const char* n, size_t count) const {
+        auto& v = (*tl_shared_arena)[n];
+        if (v.size() < count * sizeof(T)) v.resize(count * sizeof(T));
+        return reinterpret_cast<T*>(v.data());
+    }
+};
+
+void barrier();  // yields the current invocation's fiber until every invocation reached it
 inline void memoryBarrierShared() {}
 
 }  // namespace glslref
