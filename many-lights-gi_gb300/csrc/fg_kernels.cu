@@ -299,8 +299,10 @@ __global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
         // ---- gather over the kept list (final_gathering.comp:97-130) ----
         const int nk = s_n;
         if (valid) {
-            for (int q = 0; q < nk; ++q) {
-                const int k = s_list[q];
+            // Two pairs per iteration so that both ISM texel loads are in flight together.
+            const float* atlas32 = reinterpret_cast<const float*>(a.atlas);
+            const __half* atlas16 = reinterpret_cast<const __half*>(a.atlas);
+            auto prepare = [&](int k, float& G, float& vz, size_t& t) -> bool {
                 const float4 A = s_a[k], B = s_b[k];
                 const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
                 const float d2 = dx * dx + dy * dy + dz * dz;
@@ -309,13 +311,14 @@ __global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
                 const float a1 = B.x * ndx + B.y * ndy + B.z * ndz;
                 const float a2 = -(fn.x * ndx + fn.y * ndy + fn.z * ndz);
                 const float angle = fmaxf(0.f, a1) * fmaxf(0.f, a2);
-                if (angle <= 0.f) continue;
+                if (!(angle > 0.f)) return false;
                 const float att = (inv * inv) * (inv * inv);
-                float G = fminf(angle * att, a.clamp_value);
+                G = fminf(angle * att, a.clamp_value);
                 if (a.shadowing) {
                     const float4 C = s_c[k], D = s_d[k];
-                    // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false)
-                    const float rz = __frcp_rn(1.0f + a1);
+                    // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false):
+                    // x = s.d / (1 - (-n).d), texel = floor(((x + 1)/2 + tile) * ismSize)
+                    const float rz = __fdividef(1.0f, 1.0f + a1);
                     const float px = (C.x * ndx + C.y * ndy + C.z * ndz) * rz;
                     const float py = (D.x * ndx + D.y * ndy + D.z * ndz) * rz;
                     const int org = __float_as_int(D.w);
@@ -325,17 +328,52 @@ __global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
                     if (ix < 0) ix += a.atlas_w;
                     if (iy >= a.atlas_h) iy -= a.atlas_h;
                     if (iy < 0) iy += a.atlas_h;
-                    const size_t t = (size_t)iy * a.atlas_w + ix;
-                    const float occ = kAtlasF16 ? __half2float(__ldg(reinterpret_cast<const __half*>(a.atlas) + t))
-                                                : __ldg(reinterpret_cast<const float*>(a.atlas) + t);
-                    const float vz = (d2 * inv) * inv_zfar;
-                    const float sv0 = 1.0f - (vz - occ);
-                    const float tt = __saturatef((sv0 - 0.98f) * 50.0f);
-                    G *= tt * tt * (3.0f - 2.0f * tt);
+                    t = (size_t)iy * a.atlas_w + ix;
+                    vz = (d2 * inv) * inv_zfar;
                 }
-                accx = fmaf(A.w, G, accx);
-                accy = fmaf(B.w, G, accy);
-                accz = fmaf(s_c[k].w, G, accz);
+                return true;
+            };
+            auto occluder = [&](size_t t) -> float {
+                return kAtlasF16 ? __half2float(__ldg(atlas16 + t)) : __ldg(atlas32 + t);
+            };
+            auto shade = [&](float G, float vz, float occ) -> float {
+                if (!a.shadowing) return G;
+                const float sv0 = 1.0f - (vz - occ);
+                const float tt = __saturatef((sv0 - 0.98f) * 50.0f);  // smoothstep(0.98, 1, sv0)
+                return G * (tt * tt * (3.0f - 2.0f * tt));
+            };
+            int q = 0;
+            for (; q + 1 < nk; q += 2) {
+                const int k0 = s_list[q], k1 = s_list[q + 1];
+                float G0 = 0.f, G1 = 0.f, vz0 = 0.f, vz1 = 0.f;
+                size_t t0 = 0, t1 = 0;
+                const bool ok0 = prepare(k0, G0, vz0, t0);
+                const bool ok1 = prepare(k1, G1, vz1, t1);
+                const float o0 = (ok0 && a.shadowing) ? occluder(t0) : 0.f;
+                const float o1 = (ok1 && a.shadowing) ? occluder(t1) : 0.f;
+                if (ok0) {
+                    const float g = shade(G0, vz0, o0);
+                    accx = fmaf(s_a[k0].w, g, accx);
+                    accy = fmaf(s_b[k0].w, g, accy);
+                    accz = fmaf(s_c[k0].w, g, accz);
+                }
+                if (ok1) {
+                    const float g = shade(G1, vz1, o1);
+                    accx = fmaf(s_a[k1].w, g, accx);
+                    accy = fmaf(s_b[k1].w, g, accy);
+                    accz = fmaf(s_c[k1].w, g, accz);
+                }
+            }
+            if (q < nk) {
+                const int k0 = s_list[q];
+                float G0 = 0.f, vz0 = 0.f;
+                size_t t0 = 0;
+                if (prepare(k0, G0, vz0, t0)) {
+                    const float g = shade(G0, vz0, a.shadowing ? occluder(t0) : 0.f);
+                    accx = fmaf(s_a[k0].w, g, accx);
+                    accy = fmaf(s_b[k0].w, g, accy);
+                    accz = fmaf(s_c[k0].w, g, accz);
+                }
             }
         }
         __syncthreads();

@@ -130,14 +130,22 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
                          float((nr >> 16) & 0xFFu) / 255.0f * 2.0f - 1.0f);
         const float pointRadius = float(nr >> 24) / 255.0f * 25.0f;
         const uint32_t rbyte = f2u(pointRadius * 10.0f / 2.0f);  // / sqrt(maxVplCollectCount)
+        // gather up to 4 VPLs that pass the two-sided cull (ism.comp:93-107), as 4-bit indices
+        uint32_t used = 0;
         int found = 0;
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-            if (found >= 4) break;
             const v3 rel = position - s_pos[i];
             const bool cull = dot(s_n[i], rel) < 0.0f || dot(pn, -rel) < 0.0f;
-            if (cull) continue;
-            ++found;
+            if (!cull && found < 4) {
+                used |= (uint32_t)i << (4 * found);
+                ++found;
+            }
+        }
+        // for each found VPL, project and atomicMin (ism.comp:112-137)
+        for (int k = 0; k < found; ++k) {
+            const int i = (used >> (4 * k)) & 15;
+            const v3 rel = position - s_pos[i];
             // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
             const float dist = length(rel);
             const v3 n = s_n[i];
@@ -190,30 +198,16 @@ constexpr int kPullPushThreads = 512;
 
 __device__ __forceinline__ float pow2neg(int level) { return __int_as_float((127 - level) << 23); }
 
-__global__ void __launch_bounds__(kPullPushThreads) pullpush_kernel(PullPushArgs a) {
+__global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int s = a.ism_size, L = a.levels;
-    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);
-    float4* lvl_base = reinterpret_cast<float4*>(smem + (((size_t)s * s * 4 + 15) & ~(size_t)15));
+    // Level-0 keys are read straight from the atlas (each is read once by pull level 1 and once by
+    // push level 0, both coalesced), so shared memory holds only levels 1..L.
+    const uint32_t* keys = a.keys;
+    float4* lvl_base = reinterpret_cast<float4*>(smem);
     const int ism = blockIdx.x;
     const int bx = (ism % a.grid_x) * s, by = (ism / a.grid_x) * s;
     const int nt = blockDim.x, tid = threadIdx.x;
-
-    // level 0 keys
-    if ((s & 3) == 0) {
-        const int s4 = s >> 2;
-        for (int i = tid; i < s * s4; i += nt) {
-            const int r = i / s4, c = i % s4;
-            const uint4 k = __ldg(reinterpret_cast<const uint4*>(a.keys + (size_t)(by + r) * a.atlas_w + bx) + c);
-            reinterpret_cast<uint4*>(keys)[i] = k;
-        }
-    } else {
-        for (int i = tid; i < s * s; i += nt) {
-            const int r = i / s, c = i % s;
-            keys[i] = __ldg(a.keys + (size_t)(by + r) * a.atlas_w + bx + c);
-        }
-    }
-    __syncthreads();
 
     // level l data starts at lvl_off(l) texels from lvl_base
     auto lvl = [&](int l) {
@@ -241,7 +235,7 @@ __global__ void __launch_bounds__(kPullPushThreads) pullpush_kernel(PullPushArgs
                 const int gix = 2 * gox + poff[k][0], giy = 2 * goy + poff[k][1];
                 float depthSample, radius, maxDepth, dx, dy;
                 if (l == 1) {
-                    const uint32_t key = keys[liy * si + lix];
+                    const uint32_t key = __ldg(keys + (size_t)(by + liy) * a.atlas_w + bx + lix);
                     depthSample = float(key >> 8) / 16777216.0f;
                     radius = float(key & 0xFFu) / 10.0f;
                     dx = 0.f;
@@ -387,7 +381,7 @@ __global__ void __launch_bounds__(kPullPushThreads) pullpush_kernel(PullPushArgs
                                    __uint_as_float(pack_half2(dax / wa, day / wa)));
             float4 orig;
             if (l == 0) {
-                orig = make_float4(float(keys[lpy * s + lpx] >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
+                orig = make_float4(float(__ldg(keys + (size_t)py * a.atlas_w + px) >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
             } else {
                 orig = same[i];
             }
@@ -411,7 +405,7 @@ __global__ void __launch_bounds__(kPullPushThreads) pullpush_kernel(PullPushArgs
 }
 
 size_t pullpush_smem_bytes(int ism_size, int levels) {
-    size_t b = (((size_t)ism_size * ism_size * 4) + 15) & ~(size_t)15;
+    size_t b = 0;
     for (int l = 1; l <= levels; ++l) b += (size_t)(ism_size >> l) * (ism_size >> l) * 16;
     return b;
 }
