@@ -268,6 +268,17 @@ mlgi_status mlgi_scene_generate(const mlgi_scene_desc* desc, mlgi_scene_info* in
                                 float* gbuf_normal, uint32_t* gbuf_albedo, float* rsm_depth, uint32_t* rsm_normal,
                                 uint32_t* rsm_diffuse, float* points, uint32_t* counts);
 
+/* The same seeded room generated on the device: the G-buffer and the RSM ray-cast by CUDA
+ * kernels (FP32) and the bucketed points sampled on the GPU, so that a frame needs no host upload.
+ * Buffers are device pointers (any may be NULL); gbuf_normal is 2 x FP32 or 2 x FP16 per pixel
+ * (gbuf_normal_format). The objects and matrices are those of mlgi_scene_generate for the same
+ * descriptor; values agree with the host fixture to FP32 rounding. At most 32 boxes and 16
+ * spheres. Asynchronous on `stream`; allocates nothing. */
+mlgi_status mlgi_scene_generate_device(const mlgi_scene_desc* desc, mlgi_scene_info* info, float* gbuf_depth,
+                                       void* gbuf_normal, int gbuf_normal_format, uint32_t* gbuf_albedo,
+                                       float* rsm_depth, uint32_t* rsm_normal, uint32_t* rsm_diffuse,
+                                       float* points, uint32_t* counts, mlgi_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

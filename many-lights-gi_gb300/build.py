@@ -26,12 +26,14 @@ CUDA_UNITS = [
     ("csrc/fg_kernels.cu", []),
     ("csrc/mlgi_api.cu", []),
     ("csrc/ism_static.cu", []),
+    ("csrc/scene_kernels.cu", []),
     ("csrc/batch.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     ("host/serve.cpp", []),
     ("host/autotune.cpp", []),
 ]
-HOST_UNITS = [("host/scene.cpp", ["-O3", "-fopenmp", "-fPIC", "-std=c++17", f"-I{INCLUDE}"])]
-DEPS = ["csrc/gi_device.cuh", "csrc/kernels.h", "host/serve.h"]
+# The scene fixture must be identical on x86 and Arm hosts: no FMA contraction in its double math.
+HOST_UNITS = [("host/scene.cpp", ["-O3", "-fopenmp", "-fPIC", "-std=c++17", "-ffp-contract=off", f"-I{INCLUDE}"])]
+DEPS = ["csrc/gi_device.cuh", "csrc/kernels.h", "host/serve.h", "host/room.h"]
 
 
 def nvcc() -> str:

@@ -26,6 +26,7 @@
 #endif
 
 #include "mlgi.h"
+#include "room.h"
 
 namespace {
 
@@ -102,11 +103,10 @@ M4 look_at(D3 eye, D3 center, D3 up) {
     r.at(2, 3) = dot(f, eye);
     return r;
 }
-// OpenGL perspective projection, clip z in [-w, w].
-M4 perspective(double fovy, double aspect, double n, double f) {
+// OpenGL perspective projection, clip z in [-w, w]; `t` = cot(fovy / 2).
+M4 perspective(double t, double aspect, double n, double f) {
     M4 r;
     std::memset(r.m, 0, sizeof(r.m));
-    double t = 1.0 / std::tan(fovy / 2);
     r.at(0, 0) = t / aspect;
     r.at(1, 1) = t;
     r.at(2, 2) = (f + n) / (n - f);
@@ -295,10 +295,128 @@ struct Patch {
     double area;
 };
 
+// sin and cos by their Taylor series (|x| <= pi/2 here), with plain multiplies and adds only, so
+// the fixture is identical on every host (libm's trigonometric functions may differ in the last
+// bit between platforms; this file is also built with -ffp-contract=off).
+void sincos_series(double x, double& s, double& c) {
+    double x2 = x * x, term = x, sum = x;
+    for (int k = 1; k < 14; ++k) {
+        term = -term * x2 / double((2 * k) * (2 * k + 1));
+        sum = sum + term;
+    }
+    s = sum;
+    term = 1.0;
+    sum = 1.0;
+    for (int k = 1; k < 14; ++k) {
+        term = -term * x2 / double((2 * k - 1) * (2 * k));
+        sum = sum + term;
+    }
+    c = sum;
+}
+
 // Rotate v about the y axis by angle (radians).
 D3 rot_y(D3 v, double ang) {
-    double c = std::cos(ang), s = std::sin(ang);
+    double c, s;
+    sincos_series(ang, s, c);
     return {c * v.x + s * v.z, v.y, -s * v.x + c * v.z};
+}
+
+struct Setup {
+    M4 view, proj, vp, inv_vp, lview, lproj, lvp, inv_biased, inv_lvp;
+    D3 eye, lpos, ldir;
+    Scene scene;
+    std::vector<Patch> patches;
+    std::vector<double> cdf;
+    double total = 0, r_world = 0, r_boost = 0;
+    int64_t stride = 0;
+};
+
+// Room objects from the seed, camera and light matrices, and the area table for point sampling.
+Setup make_setup(const mlgi_scene_desc& d) {
+    const double pi = 3.14159265358979323846;
+    Setup S;
+    // Camera: inside the open front of the room looking at the back wall, orbiting the room's
+    // vertical axis by camera_orbit_deg.
+    const D3 center{50, 50, 50};
+    const double orbit = d.camera_orbit_deg * pi / 180.0;
+    S.eye = center + rot_y(D3{0, 0, 46}, orbit);
+    D3 target = center + rot_y(D3{0, 0, -50}, orbit);
+    S.view = look_at(S.eye, target, D3{0, 1, 0});
+    double aspect = d.height > 0 ? (double)d.width / d.height : 1.0;
+    const double cot30 = std::sqrt(3.0);  // cot(60 degrees / 2)
+    S.proj = perspective(cot30, aspect, d.z_near, d.z_far);
+    S.vp = mul(S.proj, S.view);
+    S.inv_vp = inverse(S.vp);
+    // Spot light on the ceiling pointing down, direction jittered by yaw/pitch.
+    S.lpos = D3{50, 96, 50};
+    double yaw = d.light_yaw_deg * pi / 180.0, pitch = d.light_pitch_deg * pi / 180.0;
+    double sp, cp, sy, cy;
+    sincos_series(pitch, sp, cp);
+    sincos_series(yaw, sy, cy);
+    S.ldir = normalize(D3{sp * cy, -cp, sp * sy});
+    S.lview = look_at(S.lpos, S.lpos + S.ldir, D3{0, 0, -1});
+    S.lproj = perspective(cot30, 1.0, d.z_near, d.z_far);
+    S.lvp = mul(S.lproj, S.lview);
+    M4 bias = identity();
+    bias.at(0, 0) = bias.at(1, 1) = bias.at(2, 2) = 0.5;
+    bias.at(0, 3) = bias.at(1, 3) = bias.at(2, 3) = 0.5;
+    S.inv_biased = inverse(mul(bias, S.lvp));  // VPLProcessor.cpp:76-82
+    S.inv_lvp = inverse(S.lvp);
+    S.scene = make_scene(d, S.eye, S.lpos);
+    // Surface patches for area-uniform point sampling.
+    auto rect = [&](D3 o, D3 a, D3 b, D3 n) {
+        Patch p{0, o, a, b, n, 0, std::sqrt(dot(cross(a, b), cross(a, b)))};
+        S.patches.push_back(p);
+    };
+    rect({0, 0, 0}, {kRoom, 0, 0}, {0, 0, kRoom}, {0, 1, 0});        // floor
+    rect({0, kRoom, 0}, {kRoom, 0, 0}, {0, 0, kRoom}, {0, -1, 0});   // ceiling
+    rect({0, 0, 0}, {kRoom, 0, 0}, {0, kRoom, 0}, {0, 0, 1});        // back
+    rect({0, 0, 0}, {0, kRoom, 0}, {0, 0, kRoom}, {1, 0, 0});        // left
+    rect({kRoom, 0, 0}, {0, kRoom, 0}, {0, 0, kRoom}, {-1, 0, 0});   // right
+    for (const Box& b : S.scene.boxes) {
+        D3 sz = b.hi - b.lo;
+        rect(b.lo, {sz.x, 0, 0}, {0, sz.y, 0}, {0, 0, -1});
+        rect({b.lo.x, b.lo.y, b.hi.z}, {sz.x, 0, 0}, {0, sz.y, 0}, {0, 0, 1});
+        rect(b.lo, {0, sz.y, 0}, {0, 0, sz.z}, {-1, 0, 0});
+        rect({b.hi.x, b.lo.y, b.lo.z}, {0, sz.y, 0}, {0, 0, sz.z}, {1, 0, 0});
+        rect(b.lo, {sz.x, 0, 0}, {0, 0, sz.z}, {0, -1, 0});
+        rect({b.lo.x, b.hi.y, b.lo.z}, {sz.x, 0, 0}, {0, 0, sz.z}, {0, 1, 0});
+    }
+    for (const Sphere& sph : S.scene.spheres) {
+        Patch p{1, sph.c, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, sph.r, 4 * pi * sph.r * sph.r};
+        S.patches.push_back(p);
+    }
+    S.cdf.resize(S.patches.size());
+    for (size_t i = 0; i < S.patches.size(); ++i) {
+        S.total += S.patches[i].area;
+        S.cdf[i] = S.total;
+    }
+    S.stride = d.n_points == 0 ? 0 : (d.n_points + d.n_buckets - 1) / d.n_buckets;
+    S.r_world = d.n_points > 0 ? std::sqrt(S.total / ((double)d.n_points * pi)) : 0.0;
+    S.r_boost = S.r_world * std::sqrt((double)d.ism_count);
+    return S;
+}
+
+void fill_info(const mlgi_scene_desc& d, const Setup& S, mlgi_scene_info* info) {
+    to_float(S.view, info->view);
+    to_float(S.proj, info->proj);
+    to_float(S.inv_vp, info->inv_view_proj);
+    to_float(S.lview, info->light_view);
+    to_float(S.lproj, info->light_proj);
+    to_float(S.inv_biased, info->inv_biased_light_vp);
+    info->eye[0] = (float)S.eye.x; info->eye[1] = (float)S.eye.y; info->eye[2] = (float)S.eye.z;
+    info->light_pos[0] = (float)S.lpos.x; info->light_pos[1] = (float)S.lpos.y; info->light_pos[2] = (float)S.lpos.z;
+    info->light_dir[0] = (float)S.ldir.x; info->light_dir[1] = (float)S.ldir.y; info->light_dir[2] = (float)S.ldir.z;
+    info->z_near = d.z_near;
+    info->z_far = d.z_far;
+    info->total_area = (float)S.total;
+    info->point_radius = (float)S.r_world;
+    info->bucket_stride = S.stride;
+}
+
+bool bad_desc(const mlgi_scene_desc& d) {
+    return d.width < 0 || d.height < 0 || d.rsm_width < 0 || d.rsm_height < 0 || d.n_points < 0 || d.n_buckets <= 0 ||
+           d.z_near <= 0 || d.z_far <= d.z_near || d.ism_count <= 0;
 }
 
 }  // namespace
@@ -309,50 +427,17 @@ extern "C" mlgi_status mlgi_scene_generate(const mlgi_scene_desc* desc, mlgi_sce
                                            uint32_t* counts) {
     if (!desc || !info) return MLGI_EINVAL;
     const mlgi_scene_desc& d = *desc;
-    if (d.width < 0 || d.height < 0 || d.rsm_width < 0 || d.rsm_height < 0 || d.n_points < 0 || d.n_buckets <= 0 ||
-        d.z_near <= 0 || d.z_far <= d.z_near || d.ism_count <= 0)
-        return MLGI_EINVAL;
+    if (bad_desc(d)) return MLGI_EINVAL;
     const double pi = 3.14159265358979323846;
-
-    // Camera: inside the open front of the room looking at the back wall, orbiting the room's
-    // vertical axis by camera_orbit_deg.
-    const D3 center{50, 50, 50};
-    const double orbit = d.camera_orbit_deg * pi / 180.0;
-    D3 eye = center + rot_y(D3{0, 0, 46}, orbit);
-    D3 target = center + rot_y(D3{0, 0, -50}, orbit);
-    M4 view = look_at(eye, target, D3{0, 1, 0});
-    double aspect = d.height > 0 ? (double)d.width / d.height : 1.0;
-    M4 proj = perspective(60.0 * pi / 180.0, aspect, d.z_near, d.z_far);
-    M4 vp = mul(proj, view);
-    M4 inv_vp = inverse(vp);
-
-    // Spot light on the ceiling pointing down, direction jittered by yaw/pitch.
-    D3 lpos{50, 96, 50};
-    double yaw = d.light_yaw_deg * pi / 180.0, pitch = d.light_pitch_deg * pi / 180.0;
-    D3 ldir{std::sin(pitch) * std::cos(yaw), -std::cos(pitch), std::sin(pitch) * std::sin(yaw)};
-    ldir = normalize(ldir);
-    M4 lview = look_at(lpos, lpos + ldir, D3{0, 0, -1});
-    M4 lproj = perspective(60.0 * pi / 180.0, 1.0, d.z_near, d.z_far);
-    M4 bias = identity();
-    bias.at(0, 0) = bias.at(1, 1) = bias.at(2, 2) = 0.5;
-    bias.at(0, 3) = bias.at(1, 3) = bias.at(2, 3) = 0.5;
-    M4 biased = mul(bias, mul(lproj, lview));  // VPLProcessor.cpp:76-82
-    M4 inv_biased = inverse(biased);
-    M4 inv_lvp = inverse(mul(lproj, lview));
-
-    Scene scene = make_scene(d, eye, lpos);
-
-    to_float(view, info->view);
-    to_float(proj, info->proj);
-    to_float(inv_vp, info->inv_view_proj);
-    to_float(lview, info->light_view);
-    to_float(lproj, info->light_proj);
-    to_float(inv_biased, info->inv_biased_light_vp);
-    info->eye[0] = (float)eye.x; info->eye[1] = (float)eye.y; info->eye[2] = (float)eye.z;
-    info->light_pos[0] = (float)lpos.x; info->light_pos[1] = (float)lpos.y; info->light_pos[2] = (float)lpos.z;
-    info->light_dir[0] = (float)ldir.x; info->light_dir[1] = (float)ldir.y; info->light_dir[2] = (float)ldir.z;
-    info->z_near = d.z_near;
-    info->z_far = d.z_far;
+    const Setup S = make_setup(d);
+    fill_info(d, S, info);
+    const Scene& scene = S.scene;
+    const M4& vp = S.vp;
+    const M4& inv_vp = S.inv_vp;
+    const M4& inv_lvp = S.inv_lvp;
+    const M4& lproj = S.lproj;
+    const M4& lview = S.lview;
+    const D3 ldir = S.ldir;
 
     // Ray cast a view: pixel centres, row 0 at the bottom (GL window convention).
     auto cast = [&](const M4& inv, int w, int h, int x, int y, D3& o, D3& dir) {
@@ -396,7 +481,7 @@ extern "C" mlgi_status mlgi_scene_generate(const mlgi_scene_desc* desc, mlgi_sce
         }
     }
     if (rsm_depth || rsm_normal || rsm_diffuse) {
-        const double cos_cone = std::cos(30.0 * pi / 180.0);
+        const double cos_cone = std::sqrt(3.0) / 2.0;  // cos(30 degrees), the spot's half angle
 #pragma omp parallel for schedule(dynamic, 4)
         for (int y = 0; y < d.rsm_height; ++y) {
             for (int x = 0; x < d.rsm_width; ++x) {
@@ -420,42 +505,11 @@ extern "C" mlgi_status mlgi_scene_generate(const mlgi_scene_desc* desc, mlgi_sce
         }
     }
 
-    // Surface patches for area-uniform point sampling.
-    std::vector<Patch> patches;
-    auto rect = [&](D3 o, D3 a, D3 b, D3 n) {
-        Patch p{0, o, a, b, n, 0, std::sqrt(dot(cross(a, b), cross(a, b)))};
-        patches.push_back(p);
-    };
-    rect({0, 0, 0}, {kRoom, 0, 0}, {0, 0, kRoom}, {0, 1, 0});        // floor
-    rect({0, kRoom, 0}, {kRoom, 0, 0}, {0, 0, kRoom}, {0, -1, 0});   // ceiling
-    rect({0, 0, 0}, {kRoom, 0, 0}, {0, kRoom, 0}, {0, 0, 1});        // back
-    rect({0, 0, 0}, {0, kRoom, 0}, {0, 0, kRoom}, {1, 0, 0});        // left
-    rect({kRoom, 0, 0}, {0, kRoom, 0}, {0, 0, kRoom}, {-1, 0, 0});   // right
-    for (const Box& b : scene.boxes) {
-        D3 s = b.hi - b.lo;
-        rect(b.lo, {s.x, 0, 0}, {0, s.y, 0}, {0, 0, -1});
-        rect({b.lo.x, b.lo.y, b.hi.z}, {s.x, 0, 0}, {0, s.y, 0}, {0, 0, 1});
-        rect(b.lo, {0, s.y, 0}, {0, 0, s.z}, {-1, 0, 0});
-        rect({b.hi.x, b.lo.y, b.lo.z}, {0, s.y, 0}, {0, 0, s.z}, {1, 0, 0});
-        rect(b.lo, {s.x, 0, 0}, {0, 0, s.z}, {0, -1, 0});
-        rect({b.lo.x, b.hi.y, b.lo.z}, {s.x, 0, 0}, {0, 0, s.z}, {0, 1, 0});
-    }
-    for (const Sphere& sp : scene.spheres) {
-        Patch p{1, sp.c, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, sp.r, 4 * pi * sp.r * sp.r};
-        patches.push_back(p);
-    }
-    std::vector<double> cdf(patches.size());
-    double total = 0;
-    for (size_t i = 0; i < patches.size(); ++i) {
-        total += patches[i].area;
-        cdf[i] = total;
-    }
-    const int64_t stride = d.n_points == 0 ? 0 : (d.n_points + d.n_buckets - 1) / d.n_buckets;
-    const double r_world = d.n_points > 0 ? std::sqrt(total / ((double)d.n_points * pi)) : 0.0;
-    const double r_boost = r_world * std::sqrt((double)d.ism_count);
-    info->total_area = (float)total;
-    info->point_radius = (float)r_world;
-    info->bucket_stride = stride;
+    const std::vector<Patch>& patches = S.patches;
+    const std::vector<double>& cdf = S.cdf;
+    const double total = S.total;
+    const int64_t stride = S.stride;
+    const double r_boost = S.r_boost;
 
     if (counts) {
         for (int b = 0; b < d.n_buckets; ++b) {
@@ -478,8 +532,15 @@ extern "C" mlgi_status mlgi_scene_generate(const mlgi_scene_desc* desc, mlgi_sce
                 pos = pt.o + pt.a * u1 + pt.b * u2;
                 n = pt.n;
             } else {
-                double z = 1 - 2 * u1, ph = 2 * pi * u2, rr = std::sqrt(std::max(0.0, 1 - z * z));
-                n = D3{rr * std::cos(ph), rr * std::sin(ph), z};
+                // uniform direction by Marsaglia's method (rejection in the unit disk, sqrt only)
+                double a = 2 * u1 - 1, b = 2 * u2 - 1, q = a * a + b * b;
+                while (q >= 1.0 || q == 0.0) {
+                    a = 2 * u01(st) - 1;
+                    b = 2 * u01(st) - 1;
+                    q = a * a + b * b;
+                }
+                const double r2 = 2 * std::sqrt(1 - q);
+                n = D3{a * r2, b * r2, 1 - 2 * q};
                 pos = pt.o + n * pt.r;
             }
             uint32_t w = pack_unorm4x8(n.x * 0.5 + 0.5, n.y * 0.5 + 0.5, n.z * 0.5 + 0.5, r_boost / 25.0);
@@ -493,3 +554,50 @@ extern "C" mlgi_status mlgi_scene_generate(const mlgi_scene_desc* desc, mlgi_sce
     }
     return MLGI_OK;
 }
+
+namespace mlgi {
+
+mlgi_status build_room(const mlgi_scene_desc& d, RoomGPU* room, mlgi_scene_info* info) {
+    if (!room || bad_desc(d)) return MLGI_EINVAL;
+    const Setup S = make_setup(d);
+    if ((int)S.scene.boxes.size() > kRoomMaxBoxes || (int)S.scene.spheres.size() > kRoomMaxSpheres) return MLGI_EINVAL;
+    std::memset(room, 0, sizeof(*room));
+    auto put3 = [](float* o, D3 v) { o[0] = (float)v.x; o[1] = (float)v.y; o[2] = (float)v.z; };
+    for (int w = 0; w < 5; ++w) put3(room->wall_albedo[w], S.scene.wall_albedo[w]);
+    room->n_boxes = (int)S.scene.boxes.size();
+    room->n_spheres = (int)S.scene.spheres.size();
+    for (int i = 0; i < room->n_boxes; ++i) {
+        put3(room->box_lo[i], S.scene.boxes[i].lo);
+        put3(room->box_hi[i], S.scene.boxes[i].hi);
+        put3(room->box_albedo[i], S.scene.boxes[i].albedo);
+    }
+    for (int i = 0; i < room->n_spheres; ++i) {
+        put3(room->sph_c[i], S.scene.spheres[i].c);
+        room->sph_r[i] = (float)S.scene.spheres[i].r;
+        put3(room->sph_albedo[i], S.scene.spheres[i].albedo);
+    }
+    room->n_patches = (int)S.patches.size();
+    for (int i = 0; i < room->n_patches; ++i) {
+        const Patch& p = S.patches[i];
+        put3(room->patch_o[i], p.o);
+        put3(room->patch_a[i], p.a);
+        put3(room->patch_b[i], p.b);
+        put3(room->patch_n[i], p.n);
+        room->patch_r[i] = (float)p.r;
+        room->patch_kind[i] = p.kind;
+        room->cdf[i] = (float)S.cdf[i];
+    }
+    to_float(S.vp, room->vp);
+    to_float(S.inv_vp, room->inv_vp);
+    to_float(S.lvp, room->lvp);
+    to_float(S.inv_lvp, room->inv_lvp);
+    put3(room->light_dir, S.ldir);
+    room->cos_cone = (float)(std::sqrt(3.0) / 2.0);
+    room->total_area = (float)S.total;
+    room->r_boost = (float)S.r_boost;
+    room->point_seed = splitmix64(d.seed ^ 0x5EEDF00Dull);
+    if (info) fill_info(d, S, info);
+    return MLGI_OK;
+}
+
+}  // namespace mlgi

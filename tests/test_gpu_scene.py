@@ -1,0 +1,93 @@
+"""Device-side scene generation (mlgi_scene_generate_device) against the host fixture, and the GI
+chain on device-generated inputs against the oracle on the same inputs."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import mlgi
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def device_scene(cfg):
+    import torch
+
+    d = mlgi.SceneDesc(cfg.seed, cfg.n_boxes, cfg.n_spheres, cfg.width, cfg.height, cfg.rsm, cfg.rsm, cfg.n_points,
+                       cfg.n_vpl, cfg.n_vpl, cfg.light_yaw_deg, cfg.light_pitch_deg, cfg.camera_orbit_deg,
+                       cfg.z_near, cfg.z_far)
+    info = mlgi.SceneInfo()
+    stride = (cfg.n_points + cfg.n_vpl - 1) // cfg.n_vpl
+    dev = "cuda"
+    t = {"gd": torch.zeros(cfg.height * cfg.width, dtype=torch.float32, device=dev),
+         "gn": torch.zeros(cfg.height * cfg.width * 2, dtype=torch.float32, device=dev),
+         "ga": torch.zeros(cfg.height * cfg.width, dtype=torch.int32, device=dev),
+         "rd": torch.zeros(cfg.rsm * cfg.rsm, dtype=torch.float32, device=dev),
+         "rn": torch.zeros(cfg.rsm * cfg.rsm, dtype=torch.int32, device=dev),
+         "rf": torch.zeros(cfg.rsm * cfg.rsm, dtype=torch.int32, device=dev),
+         "pts": torch.zeros(cfg.n_vpl * stride * 4, dtype=torch.float32, device=dev),
+         "cnt": torch.zeros(cfg.n_vpl, dtype=torch.int32, device=dev)}
+    P = mlgi.ptr
+    st = mlgi.lib().mlgi_scene_generate_device(C.byref(d), C.byref(info), P(t["gd"]), P(t["gn"]), mlgi.F32,
+                                               P(t["ga"]), P(t["rd"]), P(t["rn"]), P(t["rf"]), P(t["pts"]),
+                                               P(t["cnt"]), None)
+    torch.cuda.synchronize()
+    assert st == mlgi.OK
+    H, W, R = cfg.height, cfg.width, cfg.rsm
+    return mlgi.Scene(cfg, info, t["gd"].cpu().numpy().reshape(H, W), t["gn"].cpu().numpy().reshape(H, W, 2),
+                      t["ga"].cpu().numpy().view(np.uint32).reshape(H, W), t["rd"].cpu().numpy().reshape(R, R),
+                      t["rn"].cpu().numpy().view(np.uint32).reshape(R, R),
+                      t["rf"].cpu().numpy().view(np.uint32).reshape(R, R), t["pts"].cpu().numpy().reshape(-1, 4),
+                      t["cnt"].cpu().numpy().view(np.uint32), stride)
+
+
+@pytest.mark.parametrize("cfg", [mlgi.C1, mlgi.C2], ids=lambda c: c.name)
+def test_device_scene_matches_host_fixture(cfg):
+    host = mlgi.make_scene(cfg)
+    dev = device_scene(cfg)
+    assert (dev.counts == host.counts).all()
+    # rasterised buffers agree except at a few silhouette pixels where FP32 and FP64 pick
+    # different surfaces
+    assert (np.abs(dev.gbuf_depth - host.gbuf_depth) < 1e-5).mean() > 0.995
+    assert (np.abs(dev.gbuf_normal - host.gbuf_normal).max(-1) < 1e-5).mean() > 0.995
+    assert (dev.gbuf_albedo == host.gbuf_albedo).mean() > 0.995
+    assert (np.abs(dev.rsm_depth - host.rsm_depth) < 1e-5).mean() > 0.995
+    assert (dev.rsm_normal == host.rsm_normal).mean() > 0.995
+    # points: inside the room, same radius byte, same split over surface orientations
+    p = dev.points[dev.points[:, 3].view(np.uint32) != 0]
+    assert (p[:, :3] > -1e-3).all() and (p[:, :3] < 100 + 1e-3).all()
+    assert ((p[:, 3].view(np.uint32) >> 24) == (host.points[0, 3].view(np.uint32) >> 24)).all()
+    hp = host.points[host.points[:, 3].view(np.uint32) != 0]
+    nb_dev = np.bincount((p[:, 3].view(np.uint32) & 0xFFFFFF) % 97, minlength=97) / len(p)
+    nb_host = np.bincount((hp[:, 3].view(np.uint32) & 0xFFFFFF) % 97, minlength=97) / len(hp)
+    assert np.abs(nb_dev - nb_host).max() < 0.01
+
+
+def test_chain_on_device_generated_inputs_matches_oracle():
+    import torch
+
+    from mlgi.device import DeviceFrame
+
+    cfg = mlgi.C1
+    sc = device_scene(cfg)
+    ctx = mlgi.Context(0)
+    df = DeviceFrame(sc)
+    ctx.gi_frame(df.frame_desc(), df.radiance())
+    ctx.vpl_process(df.rsm_view(), mlgi.vpl_params(cfg, sc), df.vpl_buf())
+    ctx.ism_splat(df.points_view(), df.vpl_buf(), cfg.n_vpl, mlgi.ism_params(cfg), df.atlas_view())
+    torch.cuda.synchronize()
+    perm = mlgi.shuffle_table(cfg.n_vpl)
+    pos, nrm, col, pn = O.vpl_process(sc.rsm_depth, sc.rsm_normal, sc.rsm_diffuse, cfg.n_vpl,
+                                      sc.mat("inv_biased_light_vp"), cfg.light_intensity, 1, perm)
+    keys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, pos, pn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                       cfg.grid_y, cfg.z_far)
+    assert (df.keys_np() == keys).all()
+    fin = O.pullpush(keys, cfg.ism_size, cfg.levels, cfg.z_far)
+    ref = O.final_gather(sc.gbuf_depth, sc.gbuf_normal, sc.mat("inv_view_proj").astype(np.float64),
+                         pos.astype(np.float64), nrm.astype(np.float64), col.astype(np.float64), fin, cfg.ism_size,
+                         cfg.grid_x, cfg.grid_y, cfg.z_far, cfg.gi_intensity, cfg.clamp_value, cfg.interleave,
+                         dtype=np.float64)
+    rgb = df.rgb_np()
+    assert np.linalg.norm(rgb - ref) / np.linalg.norm(ref) < 1e-3
+    ctx.close()
