@@ -150,11 +150,12 @@ __device__ __forceinline__ v3 oct_decode(float ex, float ey) {
 }
 
 template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16>
-__global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
+__global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
     constexpr int NT = T * T;
     constexpr int kRec = kReduced ? 24 : 48;
     __shared__ __align__(128) unsigned char s_raw[kMaxVplChunk * 48];
     __shared__ float4 s_a[kMaxVplChunk], s_b[kMaxVplChunk], s_c[kMaxVplChunk], s_d[kMaxVplChunk];
+    __shared__ float2 s_org[kMaxVplChunk];  // ISM tile origin (texels) + half ISM size folded in
     __shared__ int s_list[kMaxVplChunk];
     __shared__ unsigned char s_flag[kMaxVplChunk];
     __shared__ float s_box[6][NT / 32];
@@ -264,7 +265,8 @@ __global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
             s_a[k] = make_float4(p.x, p.y, p.z, f.x);
             s_b[k] = make_float4(n.x, n.y, n.z, f.y);
             s_c[k] = make_float4(s.x, s.y, s.z, f.z);
-            s_d[k] = make_float4(u.x, u.y, u.z, __int_as_float((tx * a.ism_size) | ((ty * a.ism_size) << 16)));
+            s_d[k] = make_float4(u.x, u.y, u.z, 0.f);
+            s_org[k] = make_float2(float(tx * a.ism_size) + hs, float(ty * a.ism_size) + hs);
             bool keep = true;
             if (a.cull) {
                 // front half-space of the VPL against the box corner farthest along its normal
@@ -302,7 +304,7 @@ __global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
             // Two pairs per iteration so that both ISM texel loads are in flight together.
             const float* atlas32 = reinterpret_cast<const float*>(a.atlas);
             const __half* atlas16 = reinterpret_cast<const __half*>(a.atlas);
-            auto prepare = [&](int k, float& G, float& vz, size_t& t) -> bool {
+            auto prepare = [&](int k, float& G, float& vz, size_t& t, float3& flux) -> bool {
                 const float4 A = s_a[k], B = s_b[k];
                 const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
                 const float d2 = dx * dx + dy * dy + dz * dz;
@@ -314,16 +316,18 @@ __global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
                 if (!(angle > 0.f)) return false;
                 const float att = (inv * inv) * (inv * inv);
                 G = fminf(angle * att, a.clamp_value);
+                const float4 C = s_c[k];
+                flux = make_float3(A.w, B.w, C.w);
                 if (a.shadowing) {
-                    const float4 C = s_c[k], D = s_d[k];
+                    const float4 D = s_d[k];
+                    const float2 org = s_org[k];
                     // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false):
                     // x = s.d / (1 - (-n).d), texel = floor(((x + 1)/2 + tile) * ismSize)
                     const float rz = __fdividef(1.0f, 1.0f + a1);
                     const float px = (C.x * ndx + C.y * ndy + C.z * ndz) * rz;
                     const float py = (D.x * ndx + D.y * ndy + D.z * ndz) * rz;
-                    const int org = __float_as_int(D.w);
-                    int ix = __float2int_rd(fmaf(px, hs, hs) + float(org & 0xFFFF));
-                    int iy = __float2int_rd(fmaf(py, hs, hs) + float((unsigned)org >> 16));
+                    int ix = __float2int_rd(fmaf(px, hs, org.x));
+                    int iy = __float2int_rd(fmaf(py, hs, org.y));
                     if (ix >= a.atlas_w) ix -= a.atlas_w;  // GL_REPEAT
                     if (ix < 0) ix += a.atlas_w;
                     if (iy >= a.atlas_h) iy -= a.atlas_h;
@@ -347,32 +351,34 @@ __global__ void __launch_bounds__(T* T) fg_kernel(FgArgs a) {
                 const int k0 = s_list[q], k1 = s_list[q + 1];
                 float G0 = 0.f, G1 = 0.f, vz0 = 0.f, vz1 = 0.f;
                 size_t t0 = 0, t1 = 0;
-                const bool ok0 = prepare(k0, G0, vz0, t0);
-                const bool ok1 = prepare(k1, G1, vz1, t1);
+                float3 f0, f1;
+                const bool ok0 = prepare(k0, G0, vz0, t0, f0);
+                const bool ok1 = prepare(k1, G1, vz1, t1, f1);
                 const float o0 = (ok0 && a.shadowing) ? occluder(t0) : 0.f;
                 const float o1 = (ok1 && a.shadowing) ? occluder(t1) : 0.f;
                 if (ok0) {
                     const float g = shade(G0, vz0, o0);
-                    accx = fmaf(s_a[k0].w, g, accx);
-                    accy = fmaf(s_b[k0].w, g, accy);
-                    accz = fmaf(s_c[k0].w, g, accz);
+                    accx = fmaf(f0.x, g, accx);
+                    accy = fmaf(f0.y, g, accy);
+                    accz = fmaf(f0.z, g, accz);
                 }
                 if (ok1) {
                     const float g = shade(G1, vz1, o1);
-                    accx = fmaf(s_a[k1].w, g, accx);
-                    accy = fmaf(s_b[k1].w, g, accy);
-                    accz = fmaf(s_c[k1].w, g, accz);
+                    accx = fmaf(f1.x, g, accx);
+                    accy = fmaf(f1.y, g, accy);
+                    accz = fmaf(f1.z, g, accz);
                 }
             }
             if (q < nk) {
                 const int k0 = s_list[q];
                 float G0 = 0.f, vz0 = 0.f;
                 size_t t0 = 0;
-                if (prepare(k0, G0, vz0, t0)) {
+                float3 f0;
+                if (prepare(k0, G0, vz0, t0, f0)) {
                     const float g = shade(G0, vz0, a.shadowing ? occluder(t0) : 0.f);
-                    accx = fmaf(s_a[k0].w, g, accx);
-                    accy = fmaf(s_b[k0].w, g, accy);
-                    accz = fmaf(s_c[k0].w, g, accz);
+                    accx = fmaf(f0.x, g, accx);
+                    accy = fmaf(f0.y, g, accy);
+                    accz = fmaf(f0.z, g, accz);
                 }
             }
         }

@@ -96,7 +96,8 @@ cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s) {
 constexpr int kSplatThreads = 256;
 
 __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
-    __shared__ v3 s_pos[16], s_n[16], s_s[16], s_u[16];
+    __shared__ float4 s_pos[16], s_n[16];  // xyz used; float4 for 16-byte shared loads
+    __shared__ v3 s_s[16], s_u[16];
     __shared__ float s_ism[16];
     const int wg = blockIdx.x;
     const int vplCount = a.vpl_end - a.vpl_start;
@@ -111,8 +112,8 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
         const v3 n = unpack3SN(__float_as_uint(pk.w));
         v3 s, u;
         look_at_rows(n, s, u);
-        s_pos[threadIdx.x] = mk(pk.x, pk.y, pk.z);
-        s_n[threadIdx.x] = n;
+        s_pos[threadIdx.x] = make_float4(pk.x, pk.y, pk.z, 0.f);
+        s_n[threadIdx.x] = make_float4(n.x, n.y, n.z, 0.f);
         s_s[threadIdx.x] = s;
         s_u[threadIdx.x] = u;
         s_ism[threadIdx.x] = a.scale_isms ? float(index) - float(a.vpl_start) : float(index);
@@ -135,8 +136,9 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
         int found = 0;
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-            const v3 rel = position - s_pos[i];
-            const bool cull = dot(s_n[i], rel) < 0.0f || dot(pn, -rel) < 0.0f;
+            const float4 vp = s_pos[i], vn = s_n[i];
+            const v3 rel = position - mk(vp.x, vp.y, vp.z);
+            const bool cull = dot(mk(vn.x, vn.y, vn.z), rel) < 0.0f || dot(pn, -rel) < 0.0f;
             if (!cull && found < 4) {
                 used |= (uint32_t)i << (4 * found);
                 ++found;
@@ -145,10 +147,11 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
         // for each found VPL, project and atomicMin (ism.comp:112-137)
         for (int k = 0; k < found; ++k) {
             const int i = (used >> (4 * k)) & 15;
-            const v3 rel = position - s_pos[i];
+            const float4 vp = s_pos[i], vn = s_n[i];
+            const v3 rel = position - mk(vp.x, vp.y, vp.z);
             // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
             const float dist = length(rel);
-            const v3 n = s_n[i];
+            const v3 n = mk(vn.x, vn.y, vn.z);
             float vx = dot(s_s[i], rel);
             float vy = dot(s_u[i], rel);
             float vz = ((-n.x) * rel.x + (-n.y) * rel.y) + (-n.z) * rel.z;
@@ -195,19 +198,45 @@ cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s) {
 // in place (a push texel reads only its own pull texel at that level). Coordinates entering the
 // displacement arithmetic are global atlas coordinates, as in the level-by-level shaders.
 constexpr int kPullPushThreads = 512;
+constexpr size_t kPullPushTableBytes = 2 * 256 * sizeof(float);  // key-byte tables, see below
 
 __device__ __forceinline__ float pow2neg(int level) { return __int_as_float((127 - level) << 23); }
 
+// x / n for the sample counts and weight sums that occur (n >= 1). Division by a power of two is
+// exact, so it equals the multiply by the reciprocal bit for bit; other n use IEEE division.
+__device__ __forceinline__ float div_count(float x, int n) {
+    switch (n) {
+        case 1: return x;
+        case 2: return x * 0.5f;
+        case 4: return x * 0.25f;
+        case 8: return x * 0.125f;
+        case 16: return x * 0.0625f;
+        default: return x / float(n);
+    }
+}
+
+// Shared memory: two 256-entry tables indexed by the key's radius byte b, then levels 1..L.
+//   s_rad[b] = float(b) / 10                          (pull.comp:39)
+//   s_mdo[b] = ((float(b) / 10) * 2) / zFar * 0.6     (the maxDepth offset of pull.comp:57)
+// Each entry is computed with the shader's own operations, so lookups are bit-identical.
 __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int s = a.ism_size, L = a.levels;
     // Level-0 keys are read straight from the atlas (each is read once by pull level 1 and once by
-    // push level 0, both coalesced), so shared memory holds only levels 1..L.
+    // push level 0, both coalesced), so shared memory holds only the tables and levels 1..L.
     const uint32_t* keys = a.keys;
-    float4* lvl_base = reinterpret_cast<float4*>(smem);
+    float* s_rad = reinterpret_cast<float*>(smem);
+    float* s_mdo = s_rad + 256;
+    float4* lvl_base = reinterpret_cast<float4*>(smem + kPullPushTableBytes);
     const int ism = blockIdx.x;
     const int bx = (ism % a.grid_x) * s, by = (ism / a.grid_x) * s;
     const int nt = blockDim.x, tid = threadIdx.x;
+    for (int b = tid; b < 256; b += nt) {
+        const float r = float(b) / 10.0f;
+        s_rad[b] = r;
+        s_mdo[b] = (r * 2.0f) / a.z_far * 0.6f;
+    }
+    __syncthreads();
 
     // level l data starts at lvl_off(l) texels from lvl_base
     auto lvl = [&](int l) {
@@ -237,12 +266,11 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
                 if (l == 1) {
                     const uint32_t key = __ldg(keys + (size_t)(by + liy) * a.atlas_w + bx + lix);
                     depthSample = float(key >> 8) / 16777216.0f;
-                    radius = float(key & 0xFFu) / 10.0f;
                     dx = 0.f;
                     dy = 0.f;
-                    maxDepth = depthSample + (radius * 2.0f) / a.z_far * 0.6f;
+                    maxDepth = depthSample + s_mdo[key & 0xFFu];
                     const float distToCamera = depthSample * a.z_far;
-                    radius = radius / distToCamera / 3.14f * float(s);
+                    radius = s_rad[key & 0xFFu] / distToCamera / 3.14f * float(s);
                     radius = radius * 1.3f;
                     radius = gmin(radius, 15.0f);
                 } else {
@@ -277,7 +305,7 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
             for (int k = 0; k < 4; ++k)
                 if (depthSamples[k] > maxDepth) valid[k] = false;
             float depthAcc = 0.f, radiusAcc = 0.f, maxValid = 0.f, dax = 0.f, day = 0.f;
-            uint32_t numValid = 0;
+            int numValid = 0;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (!valid[k]) continue;
@@ -290,8 +318,8 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
             }
             float4 r;
             if (numValid > 0) {
-                const float nv = float(numValid);
-                r = make_float4(depthAcc / nv, maxValid, radiusAcc / nv, __uint_as_float(pack_half2(dax / nv, day / nv)));
+                r = make_float4(div_count(depthAcc, numValid), maxValid, div_count(radiusAcc, numValid),
+                                __uint_as_float(pack_half2(div_count(dax, numValid), div_count(day, numValid))));
             } else {
                 r = make_float4(1.0f, 0.f, 0.f, 0.f);
             }
@@ -300,29 +328,25 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
         __syncthreads();
     }
 
-    // ---- push, levels L-1..0 (push.comp) ----
+    // ---- push, levels L-1..0 (push.comp): one thread per 2x2 output quad sharing the same four
+    // coarse texels, as in the shader; outputs outside this ISM are skipped ----
     const int qoff[4][2] = {{0, 0}, {0, 1}, {1, 1}, {1, 0}};
     const int weightsX[4] = {9, 3, 1, 3};
     for (int l = L - 1; l >= 0; --l) {
-        const int sl = s >> l, sc = s >> (l + 1);
-        const int o0x = bx >> l, o0y = by >> l;          // this ISM's origin at level l
+        const int sl = s >> l, sc = s >> (l + 1), nq = sc + 1;
+        const int o0x = bx >> l, o0y = by >> l;              // this ISM's origin at level l
         const int c0x = bx >> (l + 1), c0y = by >> (l + 1);  // and at level l+1
         const float4* coarse = lvl(l + 1);
         float4* same = l == 0 ? nullptr : lvl(l);
         const float scale = pow2neg(l);
-        for (int i = tid; i < sl * sl; i += nt) {
-            const int lpx = i % sl, lpy = i / sl;
-            const int px = o0x + lpx, py = o0y + lpy;  // global output pixel
-            const int gidx = (px + 1) >> 1, gidy = (py + 1) >> 1;
+        for (int q = tid; q < nq * nq; q += nt) {
+            const int gidx = c0x + q % nq, gidy = c0y + q / nq;  // global gid of the quad
             const int cllx = gidx - 1, clly = gidy - 1;
-            const int ofx = px - (2 * gidx - 1), ofy = py - (2 * gidy - 1);
-            const int op = ofx == 0 ? (ofy == 0 ? 0 : 1) : (ofy == 1 ? 2 : 3);
-            float depths[4], maxDepths[4], radiuses[4], dcx[4], dcy[4];
-            int w[4];
+            float depths[4], maxDepths[4], radiuses[4], dcx[4], dcy[4], rs[4];
+            bool usable[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int cx = cllx + qoff[k][0] - c0x, cy = clly + qoff[k][1] - c0y;
-                w[k] = weightsX[(k - op + 4) & 3];
                 if (cx >= 0 && cy >= 0 && cx < sc && cy < sc) {
                     const float4 t = coarse[cy * sc + cx];
                     depths[k] = t.x;
@@ -331,73 +355,87 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
                     const float2 d = unpack_half2(__float_as_uint(t.w));
                     dcx[k] = d.x;
                     dcy[k] = d.y;
+                    // weight 0 for invalid depth (push.comp:88-93)
+                    usable[k] = depths[k] != 1.0f;
                 } else {  // across the ISM border: weight 0 (push.comp:77-86)
-                    depths[k] = 0.f;
-                    maxDepths[k] = 0.f;
-                    radiuses[k] = 0.f;
-                    dcx[k] = 0.f;
-                    dcy[k] = 0.f;
-                    w[k] = 0;
+                    depths[k] = maxDepths[k] = radiuses[k] = dcx[k] = dcy[k] = 0.f;
+                    usable[k] = false;
                 }
+                rs[k] = radiuses[k] * scale;
             }
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (depths[k] == 1.0f) w[k] = 0;
-            float dvx[4], dvy[4];
+            for (int op = 0; op < 4; ++op) {
+                const int px = gidx * 2 - 1 + qoff[op][0], py = gidy * 2 - 1 + qoff[op][1];
+                const int lpx = px - o0x, lpy = py - o0y;
+                if (lpx < 0 || lpy < 0 || lpx >= sl || lpy >= sl) continue;
+                int w[4];
+                float dvx[4], dvy[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float ctx = (float(cllx + qoff[k][0]) + 0.5f) * 2.0f;
-                const float cty = (float(clly + qoff[k][1]) + 0.5f) * 2.0f;
-                const float ttx = float(px) + 0.5f, tty = float(py) + 0.5f;
-                dvx[k] = ctx - ttx + dcx[k] * 2.0f;
-                dvy[k] = cty - tty + dcy[k] * 2.0f;
-                const float dist = sqrtf(dvx[k] * dvx[k] + dvy[k] * dvy[k]);
-                if (dist > radiuses[k] * scale) w[k] = 0;
-            }
-            float minimum = 9001.0f, maxDepth = 0.f;
+                for (int k = 0; k < 4; ++k) {
+                    w[k] = usable[k] ? weightsX[(k - op + 4) & 3] : 0;
+                    const float ctx = (float(cllx + qoff[k][0]) + 0.5f) * 2.0f;
+                    const float cty = (float(clly + qoff[k][1]) + 0.5f) * 2.0f;
+                    dvx[k] = ctx - (float(px) + 0.5f) + dcx[k] * 2.0f;
+                    dvy[k] = cty - (float(py) + 0.5f) + dcy[k] * 2.0f;
+                    if (w[k] != 0 && sqrtf(dvx[k] * dvx[k] + dvy[k] * dvy[k]) > rs[k]) w[k] = 0;
+                }
+                float minimum = 9001.0f, maxDepth = 0.f;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (w[k] == 0) continue;
-                minimum = gmin(depths[k], minimum);
-                if (minimum == depths[k]) maxDepth = maxDepths[k];
-            }
+                for (int k = 0; k < 4; ++k) {
+                    if (w[k] == 0) continue;
+                    minimum = gmin(depths[k], minimum);
+                    if (minimum == depths[k]) maxDepth = maxDepths[k];
+                }
+                int weightAcc = 0;
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (depths[k] > maxDepth) w[k] = 0;
-            float depthAcc = 0.f, maxDepthAcc = 0.f, radiusAcc = 0.f, dax = 0.f, day = 0.f;
-            int weightAcc = 0;
+                for (int k = 0; k < 4; ++k) {
+                    if (depths[k] > maxDepth) w[k] = 0;
+                    weightAcc += w[k];
+                }
+                const int lp = lpy * sl + lpx;
+                float4 orig;
+                if (l == 0) {
+                    orig = make_float4(float(__ldg(keys + (size_t)py * a.atlas_w + px) >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
+                } else {
+                    orig = same[lp];
+                }
+                const bool invalid = orig.x == 1.0f;
+                bool occluded = false;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float wf = float(w[k]);
-                depthAcc = depthAcc + depths[k] * wf;
-                maxDepthAcc = maxDepthAcc + maxDepths[k] * wf;
-                radiusAcc = radiusAcc + radiuses[k] * wf;
-                dax = dax + dvx[k] * wf;
-                day = day + dvy[k] * wf;
-                weightAcc += w[k];
-            }
-            const float wa = float(weightAcc);
-            float4 r = make_float4(depthAcc / wa, maxDepthAcc / wa, radiusAcc / wa,
-                                   __uint_as_float(pack_half2(dax / wa, day / wa)));
-            float4 orig;
-            if (l == 0) {
-                orig = make_float4(float(__ldg(keys + (size_t)py * a.atlas_w + px) >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
-            } else {
-                orig = same[i];
-            }
-            const bool invalid = orig.x == 1.0f;
-            bool occluded = false;
+                for (int k = 0; k < 4; ++k) occluded = occluded || (w[k] > 0 && orig.x > maxDepths[k]);
+                float4 r = orig;
+                // the weighted mean is only needed when it replaces the texel (push.comp:158-161);
+                // zero-weight terms add +0 and are skipped
+                if (!(weightAcc <= 0 || (!invalid && !occluded))) {
+                    float depthAcc = 0.f, maxDepthAcc = 0.f, radiusAcc = 0.f, dax = 0.f, day = 0.f;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) occluded = occluded || (w[k] > 0 && orig.x > maxDepths[k]);
-            if (weightAcc <= 0 || (!invalid && !occluded)) r = orig;
-            if (l == 0) {
-                const size_t o = (size_t)py * a.atlas_w + px;
-                if (a.out_f16)
-                    reinterpret_cast<__half*>(a.out)[o] = __float2half_rn(r.x);
-                else
-                    reinterpret_cast<float*>(a.out)[o] = r.x;
-            } else {
-                same[i] = r;
+                    for (int k = 0; k < 4; ++k) {
+                        if (w[k] == 0) continue;
+                        const float wf = float(w[k]);
+                        depthAcc = depthAcc + depths[k] * wf;
+                        if (l > 0) {
+                            maxDepthAcc = maxDepthAcc + maxDepths[k] * wf;
+                            radiusAcc = radiusAcc + radiuses[k] * wf;
+                            dax = dax + dvx[k] * wf;
+                            day = day + dvy[k] * wf;
+                        }
+                    }
+                    r.x = div_count(depthAcc, weightAcc);
+                    if (l > 0) {  // level 0 writes only the depth channel (push.comp:33-37)
+                        r.y = div_count(maxDepthAcc, weightAcc);
+                        r.z = div_count(radiusAcc, weightAcc);
+                        r.w = __uint_as_float(pack_half2(div_count(dax, weightAcc), div_count(day, weightAcc)));
+                    }
+                }
+                if (l == 0) {
+                    const size_t o = (size_t)py * a.atlas_w + px;
+                    if (a.out_f16)
+                        reinterpret_cast<__half*>(a.out)[o] = __float2half_rn(r.x);
+                    else
+                        reinterpret_cast<float*>(a.out)[o] = r.x;
+                } else {
+                    same[lp] = r;
+                }
             }
         }
         __syncthreads();
@@ -405,7 +443,7 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
 }
 
 size_t pullpush_smem_bytes(int ism_size, int levels) {
-    size_t b = 0;
+    size_t b = kPullPushTableBytes;
     for (int l = 1; l <= levels; ++l) b += (size_t)(ism_size >> l) * (ism_size >> l) * 16;
     return b;
 }
