@@ -35,8 +35,8 @@ PASSES = ["vpl_process", "ism_clear", "ism_splat", "pullpush", "final_gather"]
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="mlgi", choices=["mlgi", "reference"])
     ap.add_argument("--config", default="c2_1920x1080_n1024")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
@@ -221,6 +221,9 @@ def run_gpu(args, cfg, rank, world, local_rank):
             torch.distributed.barrier()
 
     # ---- device-resident frames (value) ----
+    # nvidia-smi samples every 200 ms: it starts before the warm-up and stops after the timed loop
+    sampler = ClockSampler(local_rank)
+    sampler.start()
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             ctx.gi_frame(fd, out, ctx.stream())
@@ -229,8 +232,6 @@ def run_gpu(args, cfg, rank, world, local_rank):
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         passes = np.zeros((args.steps, 5))
-        sampler = ClockSampler(local_rank)
-        sampler.start()
         t0 = time.perf_counter()
         for i in range(args.steps):
             flush.fill_(i & 0xFF)
