@@ -205,6 +205,25 @@ typedef struct {
  * buffers and the atlas are context-owned. */
 mlgi_status mlgi_gi_frame(mlgi_ctx* ctx, const mlgi_frame_desc* frame, mlgi_radiance* out, mlgi_stream stream);
 
+/* ---- batched views ------------------------------------------------------------------------- */
+
+/* A fixed set of independent views (each an mlgi_frame_desc on device buffers plus its radiance
+ * output) rendered together: every pass is ONE persistent launch over a device-resident view table
+ * (work items of all views interleaved across the whole GPU), and the five launches plus the
+ * table upload are captured once into a CUDA graph that mlgi_batch_launch replays. Views may mix
+ * sizes, VPL counts, ISM layouts and precisions (a view is either all FP32 or all reduced: F16
+ * atlas, F16 normals, F16 VPL records). Gathering uses 16 x 16 tiles. The batch owns every
+ * view's VPL buffers and atlas (one device arena). Each view's result equals mlgi_gi_frame's for
+ * the same inputs bit for bit. */
+typedef struct mlgi_batch mlgi_batch;
+mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc* views, const mlgi_radiance* outputs,
+                              mlgi_batch** out);
+/* Replace view i's parameters and buffers (same sizes and formats as at creation); synchronises
+ * the batch's previous launch, takes effect at the next mlgi_batch_launch. */
+mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_desc* desc, const mlgi_radiance* output);
+mlgi_status mlgi_batch_launch(mlgi_batch* b, mlgi_stream stream);
+void mlgi_batch_destroy(mlgi_batch* b);
+
 /* Sizes of the host buffers mlgi_gi_frame_host reads, in bytes. */
 typedef struct {
     size_t rsm_depth, rsm_normal, rsm_diffuse;

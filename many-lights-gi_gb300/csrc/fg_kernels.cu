@@ -149,26 +149,32 @@ __device__ __forceinline__ v3 oct_decode(float ex, float ey) {
     return normalize(n);
 }
 
+// Shared memory of one final-gathering block (one tile of one interleave class).
+template <int NT>
+struct FgSmem {
+    __align__(128) unsigned char raw[kMaxVplChunk * 48];  // VPL records staged by the bulk copy
+    float4 a[kMaxVplChunk], b[kMaxVplChunk], c[kMaxVplChunk], d[kMaxVplChunk];
+    float2 org[kMaxVplChunk];  // ISM tile origin (texels) + half ISM size folded in
+    int list[kMaxVplChunk];
+    unsigned char flag[kMaxVplChunk];
+    float box[6][NT / 32];
+    int n;
+    __align__(8) uint64_t bar;
+};
+
+// One T x T tile of interleave class c. The caller initialises S.bar once and keeps `parity`
+// across calls. Returns false (block-uniform) when the VPL staging wait timed out.
 template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16>
-__global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
+__device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const int c, FgSmem<T * T>& S,
+                                        uint32_t& parity) {
     constexpr int NT = T * T;
     constexpr int kRec = kReduced ? 24 : 48;
-    __shared__ __align__(128) unsigned char s_raw[kMaxVplChunk * 48];
-    __shared__ float4 s_a[kMaxVplChunk], s_b[kMaxVplChunk], s_c[kMaxVplChunk], s_d[kMaxVplChunk];
-    __shared__ float2 s_org[kMaxVplChunk];  // ISM tile origin (texels) + half ISM size folded in
-    __shared__ int s_list[kMaxVplChunk];
-    __shared__ unsigned char s_flag[kMaxVplChunk];
-    __shared__ float s_box[6][NT / 32];
-    __shared__ int s_n;
-    __shared__ __align__(8) uint64_t s_bar;
-
     const int tid = threadIdx.x;
     const int I = a.interleave;
-    const int c = blockIdx.y;
     const int cx = c % I, cy = c / I;
     const int sw = (a.width + I - 1) / I;
     const int ntx = (sw + T - 1) / T;
-    const int tix = blockIdx.x % ntx, tiy = blockIdx.x / ntx;
+    const int tix = tile % ntx, tiy = tile / ntx;
     const int x = (tix * T + tid % T) * I + cx;
     const int y = (tiy * T + tid / T) * I + cy;
     const bool valid = x < a.width && y < a.height;
@@ -206,27 +212,25 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
         }
         if ((tid & 31) == 0)
 #pragma unroll
-            for (int k = 0; k < 6; ++k) s_box[k][tid >> 5] = b[k];
+            for (int k = 0; k < 6; ++k) S.box[k][tid >> 5] = b[k];
         __syncthreads();
         float r[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-            r[k] = s_box[k][0];
-            for (int w = 1; w < NT / 32; ++w) r[k] = fminf(r[k], s_box[k][w]);
+            r[k] = S.box[k][0];
+            for (int w = 1; w < NT / 32; ++w) r[k] = fminf(r[k], S.box[k][w]);
         }
         bmin = mk(r[0], r[1], r[2]);
         bmax = mk(-r[3], -r[4], -r[5]);
     }
 
-    if (tid == 0) mbar_init(&s_bar, 1);
-    __syncthreads();
+    __syncthreads();  // the previous tile's use of S is over
 
     const int vbase = c * a.per_class;
     const bool use_tma = ((size_t)vbase * kRec) % 16 == 0;
     const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
     const float hs = float(a.ism_size) * 0.5f;
     const float inv_zfar = 1.0f / a.z_far;
-    uint32_t parity = 0;
     float accx = 0.f, accy = 0.f, accz = 0.f;
 
     for (int base = 0; base < a.per_class; base += kMaxVplChunk) {
@@ -234,39 +238,39 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
         const size_t bytes = (size_t)cnt * kRec;
         if (use_tma && bytes % 16 == 0) {
             if (tid == 0) {
-                mbar_expect_tx(&s_bar, (uint32_t)bytes);
-                tma_bulk_g2s(s_raw, src + (size_t)(vbase + base) * kRec, (uint32_t)bytes, &s_bar);
+                mbar_expect_tx(&S.bar, (uint32_t)bytes);
+                tma_bulk_g2s(S.raw, src + (size_t)(vbase + base) * kRec, (uint32_t)bytes, &S.bar);
             }
-            const bool ok = __syncthreads_and(mbar_wait(&s_bar, parity));
+            const bool ok = __syncthreads_and(mbar_wait(&S.bar, parity));
             if (!ok) {  // block-uniform: flag the error, give the copy one more bounded wait, leave
                 if (tid == 0) {
                     atomicOr(a.status, kStatusTmaTimeout);
-                    mbar_wait(&s_bar, parity);
+                    mbar_wait(&S.bar, parity);
                 }
-                return;
+                return false;
             }
             parity ^= 1u;
         } else {
             for (size_t k = tid * 4; k < bytes; k += NT * 4)
-                *reinterpret_cast<uint32_t*>(s_raw + k) =
+                *reinterpret_cast<uint32_t*>(S.raw + k) =
                     __ldg(reinterpret_cast<const uint32_t*>(src + (size_t)(vbase + base) * kRec + k));
             __syncthreads();
         }
         // derive per-VPL data and the cull flag
         for (int k = tid; k < cnt; k += NT) {
             v3 p, n, f;
-            decode_vpl<kReduced>(s_raw + (size_t)k * kRec, p, n, f);
+            decode_vpl<kReduced>(S.raw + (size_t)k * kRec, p, n, f);
             v3 s, u;
             look_at_rows(n, s, u);
             const int vid = vbase + base + k;
             const float ismIndex = float(vid) - float(a.ism_index_offset);
             const int ty = int(ismIndex / float(a.gx));
             const int tx = int(ismIndex - float(ty) * float(a.gx));
-            s_a[k] = make_float4(p.x, p.y, p.z, f.x);
-            s_b[k] = make_float4(n.x, n.y, n.z, f.y);
-            s_c[k] = make_float4(s.x, s.y, s.z, f.z);
-            s_d[k] = make_float4(u.x, u.y, u.z, 0.f);
-            s_org[k] = make_float2(float(tx * a.ism_size) + hs, float(ty * a.ism_size) + hs);
+            S.a[k] = make_float4(p.x, p.y, p.z, f.x);
+            S.b[k] = make_float4(n.x, n.y, n.z, f.y);
+            S.c[k] = make_float4(s.x, s.y, s.z, f.z);
+            S.d[k] = make_float4(u.x, u.y, u.z, 0.f);
+            S.org[k] = make_float2(float(tx * a.ism_size) + hs, float(ty * a.ism_size) + hs);
             bool keep = true;
             if (a.cull) {
                 // front half-space of the VPL against the box corner farthest along its normal
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
                     if (dot(dq, dq) > r * r) keep = false;
                 }
             }
-            s_flag[k] = keep ? 1 : 0;
+            S.flag[k] = keep ? 1 : 0;
         }
         __syncthreads();
         // order-preserving compaction of the kept indices by warp 0
@@ -289,23 +293,23 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
             int run = 0;
             for (int w = 0; w < cnt; w += 32) {
                 const int k = w + tid;
-                const bool keep = k < cnt && s_flag[k];
+                const bool keep = k < cnt && S.flag[k];
                 const unsigned ballot = __ballot_sync(0xffffffffu, keep);
-                if (keep) s_list[run + __popc(ballot & ((1u << tid) - 1u))] = k;
+                if (keep) S.list[run + __popc(ballot & ((1u << tid) - 1u))] = k;
                 run += __popc(ballot);
             }
-            if (tid == 0) s_n = run;
+            if (tid == 0) S.n = run;
         }
         __syncthreads();
 
         // ---- gather over the kept list (final_gathering.comp:97-130) ----
-        const int nk = s_n;
+        const int nk = S.n;
         if (valid) {
             // Two pairs per iteration so that both ISM texel loads are in flight together.
             const float* atlas32 = reinterpret_cast<const float*>(a.atlas);
             const __half* atlas16 = reinterpret_cast<const __half*>(a.atlas);
             auto prepare = [&](int k, float& G, float& vz, size_t& t, float3& flux) -> bool {
-                const float4 A = s_a[k], B = s_b[k];
+                const float4 A = S.a[k], B = S.b[k];
                 const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
                 const float d2 = dx * dx + dy * dy + dz * dz;
                 const float inv = rsqrtf(d2);
@@ -316,11 +320,11 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
                 if (!(angle > 0.f)) return false;
                 const float att = (inv * inv) * (inv * inv);
                 G = fminf(angle * att, a.clamp_value);
-                const float4 C = s_c[k];
+                const float4 C = S.c[k];
                 flux = make_float3(A.w, B.w, C.w);
                 if (a.shadowing) {
-                    const float4 D = s_d[k];
-                    const float2 org = s_org[k];
+                    const float4 D = S.d[k];
+                    const float2 org = S.org[k];
                     // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false):
                     // x = s.d / (1 - (-n).d), texel = floor(((x + 1)/2 + tile) * ismSize)
                     const float rz = __fdividef(1.0f, 1.0f + a1);
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
             };
             int q = 0;
             for (; q + 1 < nk; q += 2) {
-                const int k0 = s_list[q], k1 = s_list[q + 1];
+                const int k0 = S.list[q], k1 = S.list[q + 1];
                 float G0 = 0.f, G1 = 0.f, vz0 = 0.f, vz1 = 0.f;
                 size_t t0 = 0, t1 = 0;
                 float3 f0, f1;
@@ -370,7 +374,7 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
                 }
             }
             if (q < nk) {
-                const int k0 = s_list[q];
+                const int k0 = S.list[q];
                 float G0 = 0.f, vz0 = 0.f;
                 size_t t0 = 0;
                 float3 f0;
@@ -391,6 +395,15 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
         a.out[3 * pix + 1] = accy * a.gi_intensity / a.vpl_count_f * a.i2;
         a.out[3 * pix + 2] = accz * a.gi_intensity / a.vpl_count_f * a.i2;
     }
+    return true;
+}
+
+template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16>
+__global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
+    __shared__ FgSmem<T * T> S;
+    if (threadIdx.x == 0) mbar_init(&S.bar, 1);
+    uint32_t parity = 0;
+    fg_tile<T, kReduced, kAtlasF16, kNormalF16>(a, blockIdx.x, blockIdx.y, S, parity);
 }
 
 template <int T>
@@ -416,6 +429,41 @@ cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s) {
     if (a.width <= 0 || a.height <= 0) return cudaSuccess;
     if (a.tile == 8) return launch_fg_t<8>(a, s);
     return launch_fg_t<16>(a, s);
+}
+
+// Persistent final gathering over a view table (16 x 16 tiles). Views are FP32 or fully reduced.
+__global__ void __launch_bounds__(256, 4) batch_fg_kernel(BatchTable t) {
+    __shared__ FgSmem<256> S;
+    __shared__ FgArgs args;  // the item's view arguments, staged once per item
+    __shared__ int mode, tpc;
+    if (threadIdx.x == 0) mbar_init(&S.bar, 1);
+    uint32_t parity = 0;
+    const int* pre = t.prefix + kBpFg * (t.n_views + 1);
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        int lo = 0, hi = t.n_views - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(pre + mid) <= item) lo = mid; else hi = mid - 1;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            args = t.views[lo].fg;
+            mode = t.views[lo].fg_mode;
+            tpc = t.views[lo].fg_tiles_per_class;
+        }
+        __syncthreads();
+        const int local = item - __ldg(pre + lo);
+        const int tile = local % tpc, cls = local / tpc;
+        const bool ok = mode ? fg_tile<16, true, true, true>(args, tile, cls, S, parity)
+                             : fg_tile<16, false, false, false>(args, tile, cls, S, parity);
+        if (!ok) return;  // block-uniform: the staging wait timed out (status word already set)
+    }
+}
+
+cudaError_t launch_batch_fg(const BatchTable& t, int grid, cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    batch_fg_kernel<<<grid, 256, 0, s>>>(t);
+    return cudaGetLastError();
 }
 
 }  // namespace mlgi

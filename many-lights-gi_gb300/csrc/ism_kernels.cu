@@ -16,8 +16,7 @@ namespace mlgi {
 // ---------------------------------------------------------------------------------------------
 // VPL processor: one thread per VPL. Regular RSM sample -> unproject -> flux -> 10:10:10 normal
 // round trip -> optional shuffled slot.
-__global__ void __launch_bounds__(64) vpl_process_kernel(VplArgs a) {
-    const uint32_t idx = blockIdx.x * 64u + threadIdx.x;
+__device__ __forceinline__ void vpl_one(const VplArgs& a, const uint32_t idx) {
     if (idx >= (uint32_t)a.n) return;
     const uint32_t tcx = (idx % a.ax) * (uint32_t)a.rsm_w / a.ax;
     const uint32_t tcy = (idx / a.ax) * (uint32_t)a.rsm_h / a.ay;
@@ -64,6 +63,8 @@ __global__ void __launch_bounds__(64) vpl_process_kernel(VplArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(64) vpl_process_kernel(VplArgs a) { vpl_one(a, blockIdx.x * 64u + threadIdx.x); }
+
 cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
     vpl_process_kernel<<<(a.n + 63) / 64, 64, 0, s>>>(a);
@@ -95,11 +96,15 @@ cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s) {
 // atomicMin's its key into their paraboloid ISMs.
 constexpr int kSplatThreads = 256;
 
-__global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
-    __shared__ float4 s_pos[16], s_n[16];  // xyz used; float4 for 16-byte shared loads
-    __shared__ v3 s_s[16], s_u[16];
-    __shared__ float s_ism[16];
-    const int wg = blockIdx.x;
+struct SplatSmem {
+    float4 pos[16], n[16];  // xyz used; float4 for 16-byte shared loads
+    v3 s[16], u[16];
+    float ism[16];
+};
+
+// Bucket wg (one block of kSplatThreads threads).
+__device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, SplatSmem& S) {
+    __syncthreads();  // the previous bucket's use of S is over
     const int vplCount = a.vpl_end - a.vpl_start;
     if (a.points_only_scaled && wg > vplCount) return;
     if (threadIdx.x < 16) {
@@ -112,11 +117,11 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
         const v3 n = unpack3SN(__float_as_uint(pk.w));
         v3 s, u;
         look_at_rows(n, s, u);
-        s_pos[threadIdx.x] = make_float4(pk.x, pk.y, pk.z, 0.f);
-        s_n[threadIdx.x] = make_float4(n.x, n.y, n.z, 0.f);
-        s_s[threadIdx.x] = s;
-        s_u[threadIdx.x] = u;
-        s_ism[threadIdx.x] = a.scale_isms ? float(index) - float(a.vpl_start) : float(index);
+        S.pos[threadIdx.x] = make_float4(pk.x, pk.y, pk.z, 0.f);
+        S.n[threadIdx.x] = make_float4(n.x, n.y, n.z, 0.f);
+        S.s[threadIdx.x] = s;
+        S.u[threadIdx.x] = u;
+        S.ism[threadIdx.x] = a.scale_isms ? float(index) - float(a.vpl_start) : float(index);
     }
     __syncthreads();
 
@@ -136,7 +141,7 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
         int found = 0;
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-            const float4 vp = s_pos[i], vn = s_n[i];
+            const float4 vp = S.pos[i], vn = S.n[i];
             const v3 rel = position - mk(vp.x, vp.y, vp.z);
             const bool cull = dot(mk(vn.x, vn.y, vn.z), rel) < 0.0f || dot(pn, -rel) < 0.0f;
             if (!cull && found < 4) {
@@ -147,13 +152,13 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
         // for each found VPL, project and atomicMin (ism.comp:112-137)
         for (int k = 0; k < found; ++k) {
             const int i = (used >> (4 * k)) & 15;
-            const float4 vp = s_pos[i], vn = s_n[i];
+            const float4 vp = S.pos[i], vn = S.n[i];
             const v3 rel = position - mk(vp.x, vp.y, vp.z);
             // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
             const float dist = length(rel);
             const v3 n = mk(vn.x, vn.y, vn.z);
-            float vx = dot(s_s[i], rel);
-            float vy = dot(s_u[i], rel);
+            float vx = dot(S.s[i], rel);
+            float vy = dot(S.u[i], rel);
             float vz = ((-n.x) * rel.x + (-n.y) * rel.y) + (-n.z) * rel.z;
             const float signOfV = gsign(vz);
             vx = vx / dist;
@@ -166,7 +171,7 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
             vz = vz * -signOfV;
             vx = (vx + 1.0f) / 2.0f;
             vy = (vy + 1.0f) / 2.0f;
-            const float ismIndex = s_ism[i];
+            const float ismIndex = S.ism[i];
             const float ty = float(f2i(ismIndex / fgx));
             const int tx = f2i(ismIndex - ty * fgx);
             vx = vx + float(tx);
@@ -182,6 +187,11 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
             atomicMin(a.keys + (size_t)py * a.atlas_w + px, key);
         }
     }
+}
+
+__global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
+    __shared__ SplatSmem S;
+    splat_bucket(a, blockIdx.x, S);
 }
 
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s) {
@@ -219,8 +229,9 @@ __device__ __forceinline__ float div_count(float x, int n) {
 //   s_rad[b] = float(b) / 10                          (pull.comp:39)
 //   s_mdo[b] = ((float(b) / 10) * 2) / zFar * 0.6     (the maxDepth offset of pull.comp:57)
 // Each entry is computed with the shader's own operations, so lookups are bit-identical.
-__global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
+// One ISM (one block of kPullPushThreads threads; smem of pullpush_smem_bytes()).
+__device__ __forceinline__ void pullpush_ism(const PullPushArgs& a, const int ism, unsigned char* smem) {
+    __syncthreads();  // the previous ISM's use of smem is over
     const int s = a.ism_size, L = a.levels;
     // Level-0 keys are read straight from the atlas (each is read once by pull level 1 and once by
     // push level 0, both coalesced), so shared memory holds only the tables and levels 1..L.
@@ -228,7 +239,6 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
     float* s_rad = reinterpret_cast<float*>(smem);
     float* s_mdo = s_rad + 256;
     float4* lvl_base = reinterpret_cast<float4*>(smem + kPullPushTableBytes);
-    const int ism = blockIdx.x;
     const int bx = (ism % a.grid_x) * s, by = (ism / a.grid_x) * s;
     const int nt = blockDim.x, tid = threadIdx.x;
     for (int b = tid; b < 256; b += nt) {
@@ -442,6 +452,11 @@ __global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushA
     }
 }
 
+__global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    pullpush_ism(a, blockIdx.x, smem);
+}
+
 size_t pullpush_smem_bytes(int ism_size, int levels) {
     size_t b = kPullPushTableBytes;
     for (int l = 1; l <= levels; ++l) b += (size_t)(ism_size >> l) * (ism_size >> l) * 16;
@@ -454,6 +469,99 @@ cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     pullpush_kernel<<<a.grid_x * a.grid_y, kPullPushThreads, smem, s>>>(a);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Persistent forms over a view table: block b takes work items b, b + gridDim.x, ... of the pass;
+// an item is (view, index inside the view) found from the pass's running item counts. Each item
+// runs exactly the single-view body, so batched results equal single-frame results bit for bit.
+__device__ __forceinline__ int find_view(const int* prefix, int n_views, int item) {
+    int lo = 0, hi = n_views - 1;  // last view whose first item <= item
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) batch_clear_kernel(BatchTable t) {
+    const int* pre = t.prefix + kBpClear * (t.n_views + 1);
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        const int v = find_view(pre, t.n_views, item);
+        const BatchView& V = t.views[v];
+        const size_t first = (size_t)(item - __ldg(pre + v)) * kBatchClearTexels;
+        uint32_t* keys = V.keys;
+        const size_t n = V.atlas_texels;
+        for (size_t i = first + threadIdx.x * 4; i < first + kBatchClearTexels && i < n; i += 256 * 4) {
+            if (i + 4 <= n)
+                *reinterpret_cast<uint4*>(keys + i) = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+            else
+                for (size_t k = i; k < n; ++k) keys[k] = 0xFFFFFFFFu;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBatchVplPerItem) batch_vpl_kernel(BatchTable t) {
+    const int* pre = t.prefix + kBpVpl * (t.n_views + 1);
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        const int v = find_view(pre, t.n_views, item);
+        vpl_one(t.views[v].vpl, (uint32_t)(item - __ldg(pre + v)) * kBatchVplPerItem + threadIdx.x);
+    }
+}
+
+__global__ void __launch_bounds__(kSplatThreads) batch_splat_kernel(BatchTable t) {
+    __shared__ SplatSmem S;
+    __shared__ SplatArgs args;  // the item's view arguments, staged once per item
+    const int* pre = t.prefix + kBpSplat * (t.n_views + 1);
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        const int v = find_view(pre, t.n_views, item);
+        __syncthreads();
+        if (threadIdx.x == 0) args = t.views[v].splat;
+        __syncthreads();
+        splat_bucket(args, item - __ldg(pre + v), S);
+    }
+}
+
+__global__ void __launch_bounds__(kPullPushThreads, 2) batch_pullpush_kernel(BatchTable t) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ PullPushArgs args;
+    const int* pre = t.prefix + kBpPullPush * (t.n_views + 1);
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        const int v = find_view(pre, t.n_views, item);
+        __syncthreads();
+        if (threadIdx.x == 0) args = t.views[v].pp;
+        __syncthreads();
+        pullpush_ism(args, item - __ldg(pre + v), smem);
+    }
+}
+
+cudaError_t launch_batch_ism(const BatchTable& t, int pass, int grid, size_t smem, cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    switch (pass) {
+        case kBpClear: batch_clear_kernel<<<grid, 256, 0, s>>>(t); break;
+        case kBpVpl: batch_vpl_kernel<<<grid, kBatchVplPerItem, 0, s>>>(t); break;
+        case kBpSplat: batch_splat_kernel<<<grid, kSplatThreads, 0, s>>>(t); break;
+        case kBpPullPush:  // the dynamic shared-memory limit was raised by batch_blocks_per_sm()
+            batch_pullpush_kernel<<<grid, kPullPushThreads, smem, s>>>(t);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+int batch_blocks_per_sm(int pass, size_t smem) {
+    int n = 1;
+    switch (pass) {
+        case kBpClear: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_clear_kernel, 256, 0); break;
+        case kBpVpl: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_vpl_kernel, kBatchVplPerItem, 0); break;
+        case kBpSplat: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_splat_kernel, kSplatThreads, 0); break;
+        case kBpPullPush:
+            cudaFuncSetAttribute(batch_pullpush_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pullpush_kernel, kPullPushThreads, smem);
+            break;
+        default: break;
+    }
+    return n > 0 ? n : 1;
 }
 
 }  // namespace mlgi

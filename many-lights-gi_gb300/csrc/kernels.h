@@ -73,6 +73,33 @@ struct FgArgs {
     uint32_t* status;         // device error word (bit 0: VPL staging wait timed out)
 };
 
+// ---- batched frames: one persistent launch per pass over a device-resident view table -------
+struct BatchView {
+    VplArgs vpl;
+    SplatArgs splat;
+    PullPushArgs pp;
+    FgArgs fg;
+    uint32_t* keys;
+    size_t atlas_texels;
+    int fg_tiles_per_class;
+    int fg_mode;  // 0: FP32 records/atlas/normals, 1: reduced (24-byte records, FP16 atlas and normals)
+};
+
+enum BatchPass { kBpClear = 0, kBpVpl, kBpSplat, kBpPullPush, kBpFg, kBpCount };
+
+struct BatchTable {
+    const BatchView* views;  // device
+    const int* prefix;       // device, kBpCount x (n_views + 1) running work-item counts
+    int n_views;
+};
+
+constexpr int kBatchClearTexels = 4096;  // atlas texels cleared per work item
+constexpr int kBatchVplPerItem = 256;
+
+cudaError_t launch_batch_ism(const BatchTable& t, int pass, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_batch_fg(const BatchTable& t, int grid, cudaStream_t s);
+int batch_blocks_per_sm(int pass, size_t smem);
+
 // Error bits written to the device status word.
 constexpr uint32_t kStatusTmaTimeout = 1u;
 

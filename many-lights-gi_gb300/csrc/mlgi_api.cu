@@ -206,9 +206,12 @@ mlgi_status mlgi_shuffle_table(int n, int32_t* out_host) {
     return MLGI_OK;
 }
 
-mlgi_status mlgi_vpl_process(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi_vpl_params* p, mlgi_vpl_buf* out,
-                             mlgi_stream stream) {
-    if (!ctx) return MLGI_EINVAL;
+}  // extern "C"
+
+namespace {
+
+mlgi_status build_vpl_args(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi_vpl_params* p, const mlgi_vpl_buf* out,
+                           mlgi::VplArgs& a) {
     if (!rsm || !p || !out) return fail(ctx, MLGI_EINVAL, "NULL argument");
     if (p->count <= 0 || p->count % 64 != 0)
         return fail(ctx, MLGI_EINVAL, "VPL count %d is not a positive multiple of 64", p->count);
@@ -217,7 +220,7 @@ mlgi_status mlgi_vpl_process(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi
         return fail(ctx, MLGI_EINVAL, "bad RSM view");
     if (!out->vpl || !out->packed || !aligned16(out->vpl) || !aligned16(out->packed))
         return fail(ctx, MLGI_EINVAL, "VPL buffers must be non-NULL and 16-byte aligned");
-    mlgi::VplArgs a{};
+    a = mlgi::VplArgs{};
     a.n = p->count;
     a.ax = (uint32_t)std::ceil(std::sqrt((float)p->count));  // rsmSamples1d = uint(ceil(sqrt(N)))
     a.ay = (uint32_t)p->count / a.ax;
@@ -236,13 +239,11 @@ mlgi_status mlgi_vpl_process(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi
     a.vpl = reinterpret_cast<float4*>(out->vpl);
     a.packed = reinterpret_cast<float4*>(out->packed);
     a.reduced = static_cast<uint8_t*>(out->reduced);
-    MLGI_CUDA(ctx, mlgi::launch_vpl_process(a, pick(ctx, stream)));
     return MLGI_OK;
 }
 
-mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
-                           const mlgi_ism_params* p, mlgi_atlas* atlas, mlgi_stream stream) {
-    if (!ctx) return MLGI_EINVAL;
+mlgi_status build_splat_args(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                             const mlgi_ism_params* p, const mlgi_atlas* atlas, mlgi::SplatArgs& a) {
     mlgi_status st = check_ism(ctx, p);
     if (st != MLGI_OK) return st;
     if ((st = check_atlas(ctx, atlas, p)) != MLGI_OK) return st;
@@ -258,10 +259,7 @@ mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl
         return fail(ctx, MLGI_EINVAL, "point buffer has %d buckets, the splat samples %d", pts->n_buckets, sampled);
     if (pts->n_buckets > 0 && (!pts->points || !pts->counts || pts->bucket_stride < 0 || !aligned16(pts->points)))
         return fail(ctx, MLGI_EINVAL, "bad point buffer");
-    cudaStream_t s = pick(ctx, stream);
-    MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas->keys, (size_t)atlas->width * atlas->height, s));
-    mark(ctx, kIsmClear + 1, s);
-    mlgi::SplatArgs a{};
+    a = mlgi::SplatArgs{};
     a.points = reinterpret_cast<const float4*>(pts->points);
     a.counts = pts->counts;
     a.bucket_stride = pts->bucket_stride;
@@ -278,12 +276,11 @@ mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl
     a.atlas_h = atlas->height;
     a.z_far = p->z_far;
     a.keys = atlas->keys;
-    MLGI_CUDA(ctx, mlgi::launch_ism_splat(a, s));
     return MLGI_OK;
 }
 
-mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* p, mlgi_stream stream) {
-    if (!ctx) return MLGI_EINVAL;
+mlgi_status build_pullpush_args(mlgi_ctx* ctx, const mlgi_atlas* atlas, const mlgi_ism_params* p,
+                                mlgi::PullPushArgs& a) {
     mlgi_status st = check_ism(ctx, p);
     if (st != MLGI_OK) return st;
     if ((st = check_atlas(ctx, atlas, p)) != MLGI_OK) return st;
@@ -292,7 +289,7 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
         return fail(ctx, MLGI_EINVAL, "a %d-texel ISM pyramid exceeds shared memory", p->ism_size);
     if ((p->ism_size & 3) == 0 && !aligned16(atlas->keys))
         return fail(ctx, MLGI_EINVAL, "atlas keys must be 16-byte aligned");
-    mlgi::PullPushArgs a{};
+    a = mlgi::PullPushArgs{};
     a.keys = atlas->keys;
     a.out = atlas->depth;
     a.out_f16 = atlas->format == MLGI_F16;
@@ -303,14 +300,12 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
     a.grid_x = p->grid_x;
     a.grid_y = p->grid_y;
     a.z_far = p->z_far;
-    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream)));
     return MLGI_OK;
 }
 
-mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls,
-                              const mlgi_atlas* atlas, const mlgi_fg_params* p, mlgi_radiance* out,
-                              mlgi_stream stream) {
-    if (!ctx) return MLGI_EINVAL;
+mlgi_status build_fg_args(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls,
+                          const mlgi_atlas* atlas, const mlgi_fg_params* p, const mlgi_radiance* out,
+                          mlgi::FgArgs& a) {
     if (!g || !vpls || !atlas || !p || !out) return fail(ctx, MLGI_EINVAL, "NULL argument");
     if (g->width <= 0 || g->height <= 0 || !g->depth || !g->normal) return fail(ctx, MLGI_EINVAL, "bad G-buffer view");
     if (out->width != g->width || out->height != g->height || !out->rgb)
@@ -333,7 +328,7 @@ mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const m
         return fail(ctx, MLGI_EINVAL, "FG atlas layout does not match the atlas");
     if (p->shadowing && (p->scale_isms ? p->vpl_end - p->vpl_start : p->vpl_count) > p->grid_x * p->grid_y)
         return fail(ctx, MLGI_EINVAL, "more ISMs than grid slots");
-    mlgi::FgArgs a{};
+    a = mlgi::FgArgs{};
     a.width = g->width;
     a.height = g->height;
     a.depth = g->depth;
@@ -364,8 +359,53 @@ mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const m
     a.gx = p->grid_x > 0 ? p->grid_x : 1;
     a.gy = p->grid_y > 0 ? p->grid_y : 1;
     a.ism_size = p->ism_size > 0 ? p->ism_size : 1;
+    return MLGI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mlgi_status mlgi_vpl_process(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi_vpl_params* p, mlgi_vpl_buf* out,
+                             mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi::VplArgs a;
+    const mlgi_status st = build_vpl_args(ctx, rsm, p, out, a);
+    if (st != MLGI_OK) return st;
+    MLGI_CUDA(ctx, mlgi::launch_vpl_process(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                           const mlgi_ism_params* p, mlgi_atlas* atlas, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi::SplatArgs a;
+    const mlgi_status st = build_splat_args(ctx, pts, vpls, n_vpl, p, atlas, a);
+    if (st != MLGI_OK) return st;
     cudaStream_t s = pick(ctx, stream);
-    MLGI_CUDA(ctx, mlgi::launch_final_gather(a, s));
+    MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas->keys, (size_t)atlas->width * atlas->height, s));
+    mark(ctx, kIsmClear + 1, s);
+    MLGI_CUDA(ctx, mlgi::launch_ism_splat(a, s));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* p, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi::PullPushArgs a;
+    const mlgi_status st = build_pullpush_args(ctx, atlas, p, a);
+    if (st != MLGI_OK) return st;
+    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls,
+                              const mlgi_atlas* atlas, const mlgi_fg_params* p, mlgi_radiance* out,
+                              mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi::FgArgs a;
+    const mlgi_status st = build_fg_args(ctx, g, vpls, atlas, p, out, a);
+    if (st != MLGI_OK) return st;
+    MLGI_CUDA(ctx, mlgi::launch_final_gather(a, pick(ctx, stream)));
     return MLGI_OK;
 }
 
@@ -498,6 +538,199 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     MLGI_CUDA(ctx, cudaStreamSynchronize(s));
     ctx->timed_frame = ctx->timed_host_frame = ctx->timing;
     return mlgi_check_device_status(ctx, s);
+}
+
+}  // extern "C"
+
+// ---- batched views --------------------------------------------------------------------------
+
+struct mlgi_batch {
+    mlgi_ctx* ctx = nullptr;
+    int n = 0;
+    std::vector<mlgi_frame_desc> frames;
+    std::vector<size_t> arena_off;  // per view: start of its intermediates in the arena
+    void* arena = nullptr;
+    mlgi::BatchView* h_views = nullptr;  // pinned host copy, uploaded by the graph
+    mlgi::BatchView* d_views = nullptr;
+    int* d_prefix = nullptr;
+    int grid[mlgi::kBpCount] = {};
+    size_t pp_smem = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t view_arena_bytes(const mlgi_frame_desc& f) {
+    const size_t n = (size_t)f.vpl.count, texels = (size_t)f.ism.grid_x * f.ism.ism_size * f.ism.grid_y * f.ism.ism_size;
+    return align256(n * 48) + align256(n * 16) + align256(n * 24) + align256(texels * 4) +
+           align256(texels * (f.atlas_format == MLGI_F16 ? 2 : 4));
+}
+
+// Fill one view-table entry; intermediates live at `base` in the batch arena.
+mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radiance& out, char* base,
+                       mlgi::BatchView& v, int counts[mlgi::kBpCount]) {
+    const size_t n = (size_t)f.vpl.count;
+    const int aw = f.ism.grid_x * f.ism.ism_size, ah = f.ism.grid_y * f.ism.ism_size;
+    const size_t texels = (size_t)aw * ah;
+    char* p = base;
+    float* vpl = reinterpret_cast<float*>(p); p += align256(n * 48);
+    float* packed = reinterpret_cast<float*>(p); p += align256(n * 16);
+    void* reduced = p; p += align256(n * 24);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(p); p += align256(texels * 4);
+    void* depth = p;
+    const bool red = f.fg.vpl_format == MLGI_F16;
+    if (red != (f.atlas_format == MLGI_F16) || red != (f.gbuffer.normal_format == MLGI_F16))
+        return fail(ctx, MLGI_EINVAL, "a batched view must be all FP32 or all reduced precision");
+    mlgi_vpl_buf vb{(int)n, vpl, packed, red ? reduced : nullptr};
+    mlgi_atlas atlas{aw, ah, keys, depth, f.atlas_format};
+    v = mlgi::BatchView{};
+    mlgi_status st = build_vpl_args(ctx, &f.rsm, &f.vpl, &vb, v.vpl);
+    if (st == MLGI_OK) st = build_splat_args(ctx, &f.points, &vb, (int)n, &f.ism, &atlas, v.splat);
+    if (st == MLGI_OK) st = build_pullpush_args(ctx, &atlas, &f.ism, v.pp);
+    mlgi_fg_params fp = f.fg;
+    fp.tile = 16;
+    if (st == MLGI_OK) st = build_fg_args(ctx, &f.gbuffer, &vb, &atlas, &fp, &out, v.fg);
+    if (st != MLGI_OK) return st;
+    if (mlgi::pullpush_smem_bytes(f.ism.ism_size, f.ism.levels) > 200 * 1024)
+        return fail(ctx, MLGI_EINVAL, "ISM size %d too large for the batched pull-push", f.ism.ism_size);
+    v.keys = keys;
+    v.atlas_texels = texels;
+    const int I = f.fg.interleave;
+    const int sw = (f.gbuffer.width + I - 1) / I, sh = (f.gbuffer.height + I - 1) / I;
+    v.fg_tiles_per_class = ((sw + 15) / 16) * ((sh + 15) / 16);
+    v.fg_mode = red ? 1 : 0;
+    counts[mlgi::kBpClear] = (int)((texels + mlgi::kBatchClearTexels - 1) / mlgi::kBatchClearTexels);
+    counts[mlgi::kBpVpl] = (int)((n + mlgi::kBatchVplPerItem - 1) / mlgi::kBatchVplPerItem);
+    counts[mlgi::kBpSplat] = f.points.n_buckets;
+    counts[mlgi::kBpPullPush] = f.ism.grid_x * f.ism.grid_y;
+    counts[mlgi::kBpFg] = v.fg_tiles_per_class * I * I;
+    return MLGI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mlgi_batch_destroy(mlgi_batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->arena) cudaFree(b->arena);
+    if (b->d_views) cudaFree(b->d_views);
+    if (b->d_prefix) cudaFree(b->d_prefix);
+    if (b->h_views) cudaFreeHost(b->h_views);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc* views, const mlgi_radiance* outputs,
+                              mlgi_batch** out) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!out || !views || !outputs || n_views <= 0) return fail(ctx, MLGI_EINVAL, "bad batch arguments");
+    *out = nullptr;
+    mlgi_batch* b = new mlgi_batch();
+    b->ctx = ctx;
+    b->n = n_views;
+    b->frames.assign(views, views + n_views);
+    size_t total = 0;
+    for (int i = 0; i < n_views; ++i) {
+        b->arena_off.push_back(total);
+        total += view_arena_bytes(views[i]);
+    }
+    auto bail = [&](mlgi_status st) {
+        mlgi_batch_destroy(b);
+        return st;
+    };
+    if (cudaMalloc(&b->arena, std::max<size_t>(total, 256)) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(ctx, MLGI_ENOMEM, "batch arena of %zu bytes", total));
+    }
+    if (cudaMallocHost(&b->h_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
+        cudaMalloc(&b->d_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
+        cudaMalloc(&b->d_prefix, sizeof(int) * mlgi::kBpCount * (n_views + 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(ctx, MLGI_ENOMEM, "batch tables"));
+    }
+    std::vector<int> prefix(mlgi::kBpCount * (n_views + 1), 0);
+    for (int i = 0; i < n_views; ++i) {
+        int counts[mlgi::kBpCount];
+        const mlgi_status st = build_view(ctx, views[i], outputs[i], static_cast<char*>(b->arena) + b->arena_off[i],
+                                          b->h_views[i], counts);
+        if (st != MLGI_OK) return bail(st);
+        for (int p = 0; p < mlgi::kBpCount; ++p) prefix[p * (n_views + 1) + i + 1] = prefix[p * (n_views + 1) + i] + counts[p];
+        b->pp_smem = std::max(b->pp_smem, mlgi::pullpush_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    for (int p = 0; p < mlgi::kBpCount; ++p) {
+        const int items = prefix[p * (n_views + 1) + n_views];
+        const int per_sm = p == mlgi::kBpFg ? 4 : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullPush ? b->pp_smem : 0);
+        b->grid[p] = std::min(items, std::max(1, sms) * per_sm);
+    }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMemcpy(b->d_prefix, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(ctx, MLGI_ECUDA, "batch set-up"));
+    }
+    // capture: table upload, then one persistent launch per pass
+    const mlgi::BatchTable t{b->d_views, b->d_prefix, n_views};
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(mlgi::BatchView) * n_views, cudaMemcpyHostToDevice,
+                            b->stream);
+    for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPullPush})
+        if (e == cudaSuccess) e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullPush ? b->pp_smem : 0, b->stream);
+    if (e == cudaSuccess) e = mlgi::launch_batch_fg(t, b->grid[mlgi::kBpFg], b->stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    b->graph = g;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return bail(cuda_fail(ctx, e, "batch graph capture"));
+    }
+    *out = b;
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_desc* desc, const mlgi_radiance* output) {
+    if (!b || !desc || !output || view < 0 || view >= b->n) return MLGI_EINVAL;
+    mlgi_ctx* ctx = b->ctx;
+    const mlgi_frame_desc& old = b->frames[view];
+    if (view_arena_bytes(*desc) != view_arena_bytes(old) || desc->points.n_buckets != old.points.n_buckets ||
+        desc->gbuffer.width != old.gbuffer.width || desc->gbuffer.height != old.gbuffer.height ||
+        desc->fg.interleave != old.fg.interleave || desc->ism.grid_x != old.ism.grid_x ||
+        desc->ism.ism_size != old.ism.ism_size || desc->ism.levels != old.ism.levels)
+        return fail(ctx, MLGI_EINVAL, "a view update must keep its sizes and layout");
+    MLGI_CUDA(ctx, cudaStreamSynchronize(b->stream));
+    int counts[mlgi::kBpCount];
+    mlgi::BatchView v;
+    const mlgi_status st = build_view(ctx, *desc, *output, static_cast<char*>(b->arena) + b->arena_off[view], v, counts);
+    if (st != MLGI_OK) return st;
+    b->h_views[view] = v;
+    b->frames[view] = *desc;
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_batch_launch(mlgi_batch* b, mlgi_stream stream) {
+    if (!b) return MLGI_EINVAL;
+    mlgi_ctx* ctx = b->ctx;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+    MLGI_CUDA(ctx, cudaGraphLaunch(b->exec, s));
+    if (s != b->stream) {  // later updates wait for this launch through the batch stream
+        cudaEvent_t ev;
+        MLGI_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaEventRecord(ev, s);
+        cudaStreamWaitEvent(b->stream, ev, 0);
+        cudaEventDestroy(ev);
+    }
+    return MLGI_OK;
 }
 
 }  // extern "C"

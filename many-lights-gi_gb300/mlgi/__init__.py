@@ -113,6 +113,10 @@ _SIGS = {
     "mlgi_final_gather": (C.c_int32, [_p, C.POINTER(GBufferView), C.POINTER(VplBuf), C.POINTER(Atlas),
                                       C.POINTER(FgParams), C.POINTER(Radiance), _p]),
     "mlgi_gi_frame": (C.c_int32, [_p, C.POINTER(FrameDesc), C.POINTER(Radiance), _p]),
+    "mlgi_batch_create": (C.c_int32, [_p, C.c_int, _p, _p, C.POINTER(C.c_void_p)]),
+    "mlgi_batch_update_view": (C.c_int32, [_p, C.c_int, C.POINTER(FrameDesc), C.POINTER(Radiance)]),
+    "mlgi_batch_launch": (C.c_int32, [_p, _p]),
+    "mlgi_batch_destroy": (None, [_p]),
     "mlgi_frame_host_sizes_get": (C.c_int32, [C.POINTER(FrameDesc), C.POINTER(FrameHostSizes)]),
     "mlgi_gi_frame_host": (C.c_int32, [_p, C.POINTER(FrameDesc), _p]),
     "mlgi_set_timing": (C.c_int32, [_p, C.c_int]),

@@ -41,6 +41,8 @@ class DeviceFrame:
         self.atlas = torch.zeros(cfg.atlas_h * cfg.atlas_w, dtype=torch.float16 if cfg.reduced else torch.float32,
                                  device=device)
         self.rgb = torch.zeros(cfg.height * cfg.width * 3, dtype=torch.float32, device=device)
+        # the library works on its own (non-blocking) streams: the uploads above must be complete
+        torch.cuda.synchronize(device)
 
     # -- C structs ---------------------------------------------------------------------------
     def rsm_view(self) -> RsmView:
@@ -115,3 +117,46 @@ def pinned_inputs(scene: Scene) -> dict:
     out = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in arrs.items()}
     out["rgb"] = torch.zeros(c.height * c.width * 3, dtype=torch.float32).pin_memory()
     return out
+
+
+class Batch:
+    """mlgi_batch over DeviceFrames: one persistent launch per pass, replayed from a CUDA graph."""
+
+    def __init__(self, ctx, frames):
+        import ctypes as C
+
+        from . import FrameDesc, Radiance, lib
+
+        self.ctx, self.frames = ctx, list(frames)
+        self.descs = (FrameDesc * len(self.frames))(*[f.frame_desc() for f in self.frames])
+        self.outs = (Radiance * len(self.frames))(*[f.radiance() for f in self.frames])
+        self.h = C.c_void_p()
+        ctx._chk(lib().mlgi_batch_create(ctx.h, len(self.frames), C.cast(self.descs, C.c_void_p),
+                                         C.cast(self.outs, C.c_void_p), C.byref(self.h)))
+
+    def launch(self, stream: int = 0):
+        from . import lib
+
+        return self.ctx._chk(lib().mlgi_batch_launch(self.h, stream))
+
+    def update(self, i: int):
+        """Re-read frame i's parameters (e.g. after changing its scene matrices)."""
+        import ctypes as C
+
+        from . import lib
+
+        self.descs[i] = self.frames[i].frame_desc()
+        return self.ctx._chk(lib().mlgi_batch_update_view(self.h, i, C.byref(self.descs[i]), C.byref(self.outs[i])))
+
+    def close(self):
+        from . import lib
+
+        if self.h:
+            lib().mlgi_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

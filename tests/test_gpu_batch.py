@@ -1,0 +1,70 @@
+"""Batched views (mlgi_batch_*): one persistent launch per pass over mixed views, replayed from a
+CUDA graph, must give each view exactly its single-frame (mlgi_gi_frame) result."""
+import numpy as np
+import pytest
+
+import mlgi
+from mlgi.device import Batch, DeviceFrame
+
+pytestmark = pytest.mark.gpu
+
+VIEWS = [mlgi.C0, mlgi.C1.replace(seed=2), mlgi.C3.replace(seed=3),
+         mlgi.C1.replace(seed=4, interleave=8, tile=8, name="c1_i8"),
+         mlgi.C0.replace(seed=7, reduced=True, name="c0_fp16"), mlgi.C2.replace(seed=5)]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = mlgi.Context(0)
+    yield c
+    c.close()
+
+
+def single(ctx, df):
+    import torch
+
+    ctx.gi_frame(df.frame_desc(), df.radiance())
+    torch.cuda.synchronize()
+    return df.rgb_np().copy()
+
+
+def test_batch_equals_single_frames_and_replays(ctx):
+    import torch
+
+    frames = [DeviceFrame(mlgi.make_scene(c)) for c in VIEWS]
+    ref = [single(ctx, f) for f in frames]
+    for f in frames:
+        f.rgb.zero_()
+    torch.cuda.synchronize()  # the batch runs on its own stream
+    b = Batch(ctx, frames)
+    for _ in range(2):  # the graph replays
+        b.launch()
+        torch.cuda.synchronize()
+        for f, r in zip(frames, ref):
+            got = f.rgb_np()
+            assert (got.view(np.uint32) == r.view(np.uint32)).all(), f.cfg.name
+            f.rgb.zero_()
+        torch.cuda.synchronize()
+    ctx.check_device_status()
+    # a parameter update takes effect at the next launch
+    frames[1].cfg = frames[1].cfg.replace(light_intensity=2.5)
+    b.update(1)
+    b.launch()
+    torch.cuda.synchronize()
+    got = frames[1].rgb_np().copy()
+    assert (got.view(np.uint32) == single(ctx, frames[1]).view(np.uint32)).all()
+    assert not (got == ref[1]).all()
+    b.close()
+
+
+def test_batch_rejects_mixed_precision_view(ctx):
+    df = DeviceFrame(mlgi.make_scene(mlgi.C0))
+    fd = df.frame_desc()
+    fd.atlas_format = mlgi.F16  # FP32 records and normals with an FP16 atlas
+    import ctypes as C
+
+    descs = (mlgi.FrameDesc * 1)(fd)
+    outs = (mlgi.Radiance * 1)(df.radiance())
+    h = C.c_void_p()
+    st = mlgi.lib().mlgi_batch_create(ctx.h, 1, C.cast(descs, C.c_void_p), C.cast(outs, C.c_void_p), C.byref(h))
+    assert st == mlgi.EINVAL
