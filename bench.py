@@ -313,6 +313,91 @@ def run_gpu(args, cfg, rank, world, local_rank):
     ctx.close()
 
 
+def c4_views(ctx, n_views=32, n_rooms=8, seed=4):
+    """BASELINE form 4: views of seeded rooms with resolutions, VPL counts, point counts and precision
+    drawn from the stated sets; interleave and ISM edge chosen by the autotuner."""
+    import numpy as np
+
+    import mlgi
+
+    rng = np.random.default_rng(seed)
+    views = []
+    for v in range(n_views):
+        w, h = [(854, 480), (1280, 720), (1920, 1080), (2560, 1440)][rng.integers(4)]
+        n = int(rng.choice([256, 512, 1024, 2048, 4096]))
+        pts = int(2 ** rng.integers(20, 24))
+        reduced = bool(rng.integers(2))
+        tune = ctx.autotune(w, h, n, pts, reduced=reduced, batched=True, min_vpls_per_pixel=16, min_ism_size=64,
+                            seed=1000 + v % n_rooms)
+        cfg = mlgi.Config(f"c4_view{v}_{w}x{h}_n{n}", w, h, 512, n, pts, tune.ism_size, tune.grid_x, tune.grid_y,
+                          tune.levels, tune.interleave, 16, 8, tile=16, cull=1, reduced=reduced,
+                          seed=1000 + v % n_rooms, light_yaw_deg=float(rng.uniform(-5, 5)),
+                          light_pitch_deg=float(rng.uniform(-5, 5)), camera_orbit_deg=float(rng.uniform(-10, 10)))
+        views.append(cfg)
+    return views
+
+
+def run_batch(args, rank, world, local_rank):
+    """Batched views (BASELINE form 4): graph-replayed persistent launches vs one launch per view."""
+    import numpy as np
+    import torch
+
+    import mlgi
+    from mlgi.device import Batch, DeviceFrame
+
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    ctx = mlgi.Context(local_rank)
+    t_tune = time.perf_counter()
+    cfgs = c4_views(ctx)
+    t_tune = time.perf_counter() - t_tune
+    frames = [DeviceFrame.generated(c, dev) for c in cfgs]
+    batch = Batch(ctx, frames)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            batch.launch(ctx.stream())
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            batch.launch(ctx.stream())
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        batched_ms = ev[0].elapsed_time(ev[1]) / args.steps
+        # plain: the same 32 views, one mlgi_gi_frame per view
+        for f in frames:
+            ctx.gi_frame(f.frame_desc(), f.radiance(), ctx.stream())
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            for f in frames:
+                ctx.gi_frame(f.frame_desc(), f.radiance(), ctx.stream())
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        plain_ms = ev[0].elapsed_time(ev[1]) / args.steps
+    clocks = sampler.stop()
+    ctx.check_device_status()
+    if rank == 0:
+        n = len(frames)
+        print(json.dumps({
+            "metric": "batched GI ms per 32-view batch", "value": batched_ms, "unit": "ms/batch", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "dtype": "f32 / fp16-bf16 mixed",
+            "data": "synthetic (seeded procedural rooms, generated on the GPU)",
+            "config": {"workload": "c4_batch32", "views": n, "rooms": 8,
+                       "views_detail": [f"{c.width}x{c.height} N={c.n_vpl} pts=2^{int(np.log2(c.n_points))} "
+                                        f"I={c.interleave} ism={c.ism_size} {'fp16' if c.reduced else 'fp32'}"
+                                        for c in cfgs],
+                       "l2": "inputs larger than L2"},
+            "frames_per_s": n / (batched_ms * 1e-3), "plain_ms_per_batch": plain_ms,
+            "plain_frames_per_s": n / (plain_ms * 1e-3), "speedup_vs_plain": plain_ms / batched_ms,
+            "gpu_launches": 5 * args.steps, "autotune_s": t_tune, "clocks": clocks}), flush=True)
+    batch.close()
+    ctx.close()
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -320,7 +405,7 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     import mlgi
 
-    cfg = mlgi.CONFIGS[args.config]
+    cfg = mlgi.CONFIGS.get(args.config, mlgi.C2)
     if world > 1:
         import torch.distributed as dist
 
@@ -328,6 +413,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, cfg, rank, world)
+        elif args.config == "c4_batch32":
+            run_batch(args, rank, world, local_rank)
         else:
             run_gpu(args, cfg, rank, world, local_rank)
     finally:

@@ -224,6 +224,35 @@ mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_des
 mlgi_status mlgi_batch_launch(mlgi_batch* b, mlgi_stream stream);
 void mlgi_batch_destroy(mlgi_batch* b);
 
+/* ---- autotuner ------------------------------------------------------------------------------ */
+
+/* Picks the interleave factor, ISM edge (with its pull-push levels and a power-of-two-wide ISM
+ * grid) and gathering tile for a view shape by timing candidates on this GPU with the real kernels
+ * (on a device-generated seeded room of that shape). budget_ms == 0: the fastest candidate meeting
+ * the quality floor (n_vpl / I^2 >= min_vpls_per_pixel, ISM edge >= min_ism_size); budget_ms > 0:
+ * the highest-quality candidate (most VPLs per pixel, then largest ISM) that fits the budget, or
+ * the fastest if none does. batched != 0 restricts the tile to the batched gather's 16. Results
+ * are cached per query for the life of the process. Synchronises the context's stream. */
+typedef struct {
+    int width, height, n_vpl;
+    int64_t n_points;
+    int reduced;
+    int rsm_size;            /* 0 selects 512 */
+    int min_vpls_per_pixel;  /* e.g. 16 */
+    int min_ism_size;        /* e.g. 64 */
+    int batched;
+    float budget_ms;
+    uint64_t seed;
+} mlgi_autotune_query;
+
+typedef struct {
+    int interleave, ism_size, grid_x, grid_y, levels, tile;
+    float ms;                /* measured frame time of the pick */
+    int candidates_timed;
+} mlgi_autotune_result;
+
+mlgi_status mlgi_autotune(mlgi_ctx* ctx, const mlgi_autotune_query* query, mlgi_autotune_result* result);
+
 /* Sizes of the host buffers mlgi_gi_frame_host reads, in bytes. */
 typedef struct {
     size_t rsm_depth, rsm_normal, rsm_diffuse;

@@ -76,6 +76,17 @@ class FrameHostSizes(C.Structure):
                                            "gbuf_depth", "gbuf_normal", "radiance")]
 
 
+class AutotuneQuery(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("n_vpl", C.c_int), ("n_points", C.c_int64),
+                ("reduced", C.c_int), ("rsm_size", C.c_int), ("min_vpls_per_pixel", C.c_int),
+                ("min_ism_size", C.c_int), ("batched", C.c_int), ("budget_ms", C.c_float), ("seed", C.c_uint64)]
+
+
+class AutotuneResult(C.Structure):
+    _fields_ = [("interleave", C.c_int), ("ism_size", C.c_int), ("grid_x", C.c_int), ("grid_y", C.c_int),
+                ("levels", C.c_int), ("tile", C.c_int), ("ms", C.c_float), ("candidates_timed", C.c_int)]
+
+
 class CtxDesc(C.Structure):
     _fields_ = [("device", C.c_int), ("flags", C.c_uint32)]
 
@@ -117,6 +128,7 @@ _SIGS = {
     "mlgi_batch_update_view": (C.c_int32, [_p, C.c_int, C.POINTER(FrameDesc), C.POINTER(Radiance)]),
     "mlgi_batch_launch": (C.c_int32, [_p, _p]),
     "mlgi_batch_destroy": (None, [_p]),
+    "mlgi_autotune": (C.c_int32, [_p, C.POINTER(AutotuneQuery), C.POINTER(AutotuneResult)]),
     "mlgi_frame_host_sizes_get": (C.c_int32, [C.POINTER(FrameDesc), C.POINTER(FrameHostSizes)]),
     "mlgi_gi_frame_host": (C.c_int32, [_p, C.POINTER(FrameDesc), _p]),
     "mlgi_set_timing": (C.c_int32, [_p, C.c_int]),
@@ -229,6 +241,14 @@ class Context:
 
     def check_device_status(self, stream: int = 0):
         return self._chk(lib().mlgi_check_device_status(self.h, stream))
+
+    def autotune(self, width, height, n_vpl, n_points, reduced=False, min_vpls_per_pixel=16, min_ism_size=64,
+                 batched=False, budget_ms=0.0, seed=1, rsm_size=512) -> AutotuneResult:
+        q = AutotuneQuery(width, height, n_vpl, n_points, int(reduced), rsm_size, min_vpls_per_pixel, min_ism_size,
+                          int(batched), budget_ms, seed)
+        r = AutotuneResult()
+        self._chk(lib().mlgi_autotune(self.h, C.byref(q), C.byref(r)))
+        return r
 
 
 def shuffle_table(n: int) -> np.ndarray:

@@ -20,29 +20,66 @@ def _t(a: np.ndarray, device):
 class DeviceFrame:
     """Inputs, intermediate buffers and output of one frame on the GPU."""
 
-    def __init__(self, scene: Scene, device: str = "cuda"):
+    def __init__(self, scene: Scene, device: str = "cuda", generated: bool = False, intermediates: bool = True):
         import torch
 
         cfg: Config = scene.cfg
         self.cfg, self.scene, self.device = cfg, scene, device
-        self.rsm_depth = _t(scene.rsm_depth, device)
-        self.rsm_normal = _t(scene.rsm_normal.view(np.int32), device)
-        self.rsm_diffuse = _t(scene.rsm_diffuse.view(np.int32), device)
-        self.points = _t(scene.points, device)
-        self.counts = _t(scene.counts.view(np.int32), device)
-        self.gbuf_depth = _t(scene.gbuf_depth, device)
-        gn = scene.gbuf_normal.astype(np.float16) if cfg.reduced else scene.gbuf_normal
-        self.gbuf_normal = _t(gn, device)
-        n = cfg.n_vpl
+        if generated:  # inputs produced on the GPU by mlgi_scene_generate_device
+            R, px = cfg.rsm, cfg.width * cfg.height
+            self.rsm_depth = torch.empty(R * R, dtype=torch.float32, device=device)
+            self.rsm_normal = torch.empty(R * R, dtype=torch.int32, device=device)
+            self.rsm_diffuse = torch.empty(R * R, dtype=torch.int32, device=device)
+            self.points = torch.zeros(cfg.n_vpl * scene.bucket_stride * 4, dtype=torch.float32, device=device)
+            self.counts = torch.empty(cfg.n_vpl, dtype=torch.int32, device=device)
+            self.gbuf_depth = torch.empty(px, dtype=torch.float32, device=device)
+            self.gbuf_normal = torch.empty(px * 2, dtype=torch.float16 if cfg.reduced else torch.float32, device=device)
+        else:
+            self.rsm_depth = _t(scene.rsm_depth, device)
+            self.rsm_normal = _t(scene.rsm_normal.view(np.int32), device)
+            self.rsm_diffuse = _t(scene.rsm_diffuse.view(np.int32), device)
+            self.points = _t(scene.points, device)
+            self.counts = _t(scene.counts.view(np.int32), device)
+            self.gbuf_depth = _t(scene.gbuf_depth, device)
+            gn = scene.gbuf_normal.astype(np.float16) if cfg.reduced else scene.gbuf_normal
+            self.gbuf_normal = _t(gn, device)
+        n = cfg.n_vpl if intermediates else 1
         self.vpl = torch.zeros(n * 12, dtype=torch.float32, device=device)
         self.packed = torch.zeros(n * 4, dtype=torch.float32, device=device)
         self.reduced = torch.zeros(n * 24, dtype=torch.uint8, device=device)
-        self.keys = torch.zeros(cfg.atlas_h * cfg.atlas_w, dtype=torch.int32, device=device)
-        self.atlas = torch.zeros(cfg.atlas_h * cfg.atlas_w, dtype=torch.float16 if cfg.reduced else torch.float32,
-                                 device=device)
+        texels = cfg.atlas_h * cfg.atlas_w if intermediates else 1
+        self.keys = torch.zeros(texels, dtype=torch.int32, device=device)
+        self.atlas = torch.zeros(texels, dtype=torch.float16 if cfg.reduced else torch.float32, device=device)
         self.rgb = torch.zeros(cfg.height * cfg.width * 3, dtype=torch.float32, device=device)
+        if generated:
+            self.generate()
         # the library works on its own (non-blocking) streams: the uploads above must be complete
         torch.cuda.synchronize(device)
+
+    @classmethod
+    def generated(cls, cfg: Config, device: str = "cuda", intermediates: bool = True) -> "DeviceFrame":
+        """A frame whose inputs are generated on the GPU (no host-side scene arrays)."""
+        from . import SceneInfo
+
+        stride = (cfg.n_points + cfg.n_vpl - 1) // cfg.n_vpl
+        scene = Scene(cfg, SceneInfo(), None, None, None, None, None, None, None, None, stride)
+        return cls(scene, device, generated=True, intermediates=intermediates)
+
+    def generate(self, stream: int = 0):
+        """(Re)generate this frame's inputs on the GPU from cfg (room seed, light and camera pose)."""
+        import ctypes as C
+
+        from . import SceneDesc, lib
+
+        c = self.cfg
+        d = SceneDesc(c.seed, c.n_boxes, c.n_spheres, c.width, c.height, c.rsm, c.rsm, c.n_points, c.n_vpl, c.n_vpl,
+                      c.light_yaw_deg, c.light_pitch_deg, c.camera_orbit_deg, c.z_near, c.z_far)
+        st = lib().mlgi_scene_generate_device(C.byref(d), C.byref(self.scene.info), ptr(self.gbuf_depth),
+                                              ptr(self.gbuf_normal), F16 if c.reduced else F32, None,
+                                              ptr(self.rsm_depth), ptr(self.rsm_normal), ptr(self.rsm_diffuse),
+                                              ptr(self.points), ptr(self.counts), stream or None)
+        if st != 0:
+            raise RuntimeError(f"mlgi_scene_generate_device failed: {st}")
 
     # -- C structs ---------------------------------------------------------------------------
     def rsm_view(self) -> RsmView:

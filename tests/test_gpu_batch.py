@@ -68,3 +68,16 @@ def test_batch_rejects_mixed_precision_view(ctx):
     h = C.c_void_p()
     st = mlgi.lib().mlgi_batch_create(ctx.h, 1, C.cast(descs, C.c_void_p), C.cast(outs, C.c_void_p), C.byref(h))
     assert st == mlgi.EINVAL
+
+
+def test_autotune_picks_measured_candidates(ctx):
+    r = ctx.autotune(640, 360, 256, 1 << 18)
+    assert 256 // (r.interleave ** 2) >= 16 and r.ism_size in (64, 96, 128) and r.tile in (8, 16)
+    assert r.ms > 0 and r.candidates_timed > 4
+    again = ctx.autotune(640, 360, 256, 1 << 18)  # cached
+    assert (again.interleave, again.ism_size, again.tile, again.ms) == (r.interleave, r.ism_size, r.tile, r.ms)
+    # a generous budget buys the highest quality: every VPL at every pixel, the largest ISMs
+    best = ctx.autotune(640, 360, 256, 1 << 18, budget_ms=1000.0)
+    assert best.interleave == 1 and best.ism_size == 128
+    batched = ctx.autotune(640, 360, 256, 1 << 18, batched=True)
+    assert batched.tile == 16
