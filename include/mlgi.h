@@ -253,6 +253,101 @@ typedef struct {
 
 mlgi_status mlgi_autotune(mlgi_ctx* ctx, const mlgi_autotune_query* query, mlgi_autotune_result* result);
 
+/* Size the context's frame buffers (VPL records, key and depth atlases) for frames of up to
+ * max_vpl VPLs and max_atlas_texels atlas texels, so that later frames within those bounds
+ * allocate nothing. Synchronous. */
+mlgi_status mlgi_ctx_reserve(mlgi_ctx* ctx, int max_vpl, size_t max_atlas_texels);
+
+/* ---- request server ------------------------------------------------------------------------- */
+
+/* Continuous-batching server of GI frames on one GPU (served form of the frame driver; the
+ * reference renders one view per frame and has no server). A request names a room seed, a frame
+ * shape and a pose; a scheduler thread admits queued requests FIFO into free slots (each slot a
+ * context with its own stream and per-frame buffers), so frames of different requests overlap on
+ * the device. Per-room state -- the bucketed surface points of (room seed, VPL count, point
+ * count) -- is generated on the GPU on first use and stays resident, evicted least-recently-used
+ * when the HBM budget (slots + resident rooms) would be exceeded; a request waits in the queue
+ * while its room does not fit. Each frame's G-buffer and RSM are ray-cast on the device for its
+ * pose, the chain runs with the autotuned configuration of its shape (16 VPLs per pixel floor,
+ * 64^2 ISM floor; per-tile culling), and the radiance is reduced to an order-independent 64-bit
+ * digest and an FP64 sum, and optionally copied to the request's host buffer. The results of a
+ * request do not depend on what else is in flight. */
+typedef struct mlgi_server mlgi_server;
+
+typedef struct {
+    int device;
+    int slots;                  /* frames in flight */
+    int max_width, max_height;  /* largest frame a request may ask for */
+    int rsm_size;               /* 0 selects 512 */
+    size_t hbm_budget;          /* bytes for slots + resident rooms */
+} mlgi_server_desc;
+
+typedef struct {
+    uint64_t id;
+    uint64_t room_seed;
+    int width, height, n_vpl;   /* n_vpl a multiple of 64 */
+    int64_t n_points;
+    int reduced;                /* FP16 atlas, G-buffer normals and VPL attributes */
+    float light_yaw_deg, light_pitch_deg, camera_orbit_deg;
+    double arrival_s;           /* steady-clock seconds; <= 0 takes the submit time */
+    float* out_host;            /* optional: width*height*3 floats, written before completion */
+} mlgi_request;
+
+typedef struct {
+    uint64_t id;
+    mlgi_status status;         /* MLGI_ECANCELED for a cancelled request */
+    double latency_ms;          /* arrival -> completion observed by the scheduler */
+    double queue_ms;            /* arrival -> admission */
+    uint64_t digest;            /* order-independent digest of the radiance bits */
+    double sum;                 /* FP64 sum of the radiance components */
+} mlgi_completion;
+
+typedef struct {
+    int64_t queued, inflight, admitted, rooms_resident, budget_waits, evictions;
+    size_t room_bytes, slot_bytes;
+} mlgi_server_stats;
+
+/* Create the server and its slots (allocations sized by max_width/max_height and rsm_size). */
+mlgi_status mlgi_server_create(const mlgi_server_desc* desc, mlgi_server** out);
+/* Autotune the given shapes (width, height, n_vpl, n_points, reduced of each entry) and reserve
+ * every slot's buffers for the largest, so that serving allocates nothing but room state. */
+mlgi_status mlgi_server_prepare(mlgi_server* sv, const mlgi_request* shapes, int n);
+/* Queue a request (copied). MLGI_EINVAL for a malformed request; a frame larger than the
+ * server's maximum completes with MLGI_EINVAL. */
+mlgi_status mlgi_server_submit(mlgi_server* sv, const mlgi_request* req);
+/* Cancel a request still in the queue (completes with MLGI_ECANCELED); MLGI_EINVAL if it is
+ * unknown or already admitted. */
+mlgi_status mlgi_server_cancel(mlgi_server* sv, uint64_t id);
+/* Move up to `max` completions into `out`; returns how many. */
+int mlgi_server_poll(mlgi_server* sv, mlgi_completion* out, int max);
+/* Wait until every submitted request has completed (MLGI_ETIMEDOUT after timeout_s). */
+mlgi_status mlgi_server_drain(mlgi_server* sv, double timeout_s);
+mlgi_status mlgi_server_stats_get(mlgi_server* sv, mlgi_server_stats* stats);
+/* Drains, then frees everything. */
+void mlgi_server_destroy(mlgi_server* sv);
+
+/* Open-loop Poisson load: arrivals at rate_hz for duration_s (seeded exponential gaps), each
+ * request a shape drawn uniformly from `shapes`, a room drawn uniformly from n_rooms seeds
+ * (room_seed_base + k), light yaw and pitch uniform in +-light_jitter_deg, and the room's camera
+ * orbit advanced by orbit_step_deg per request (wrapping within +-10 degrees). Requests are
+ * submitted at their arrival times from the calling thread; completions go to `out` (capacity
+ * max_out). mode 0 serves through the server; mode 1 is the plain arm on the same request
+ * sequence: one frame at a time on one stream, each issued when it has arrived and the previous
+ * one has completed. */
+typedef struct {
+    uint64_t seed;
+    double rate_hz, duration_s;
+    const mlgi_request* shapes;
+    int n_shapes;
+    int n_rooms;
+    uint64_t room_seed_base;
+    float light_jitter_deg, orbit_step_deg;
+    double drain_timeout_s;     /* 0 selects 600 */
+    int mode;
+} mlgi_poisson_desc;
+mlgi_status mlgi_server_run_poisson(mlgi_server* sv, const mlgi_poisson_desc* desc, mlgi_completion* out,
+                                    int max_out, int* n_out, double* wall_s);
+
 /* Sizes of the host buffers mlgi_gi_frame_host reads, in bytes. */
 typedef struct {
     size_t rsm_depth, rsm_normal, rsm_diffuse;

@@ -27,13 +27,12 @@ CUDA_UNITS = [
     ("csrc/mlgi_api.cu", []),
     ("csrc/ism_static.cu", []),
     ("csrc/scene_kernels.cu", []),
-    ("csrc/batch.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     ("host/serve.cpp", []),
     ("host/autotune.cpp", []),
 ]
 # The scene fixture must be identical on x86 and Arm hosts: no FMA contraction in its double math.
 HOST_UNITS = [("host/scene.cpp", ["-O3", "-fopenmp", "-fPIC", "-std=c++17", "-ffp-contract=off", f"-I{INCLUDE}"])]
-DEPS = ["csrc/gi_device.cuh", "csrc/kernels.h", "host/serve.h", "host/room.h"]
+DEPS = ["csrc/gi_device.cuh", "csrc/kernels.h", "host/room.h"]
 
 
 def nvcc() -> str:
@@ -49,8 +48,7 @@ def _run(cmd):
 
 
 def _sources():
-    units = [(u, f) for u, f in CUDA_UNITS if os.path.exists(os.path.join(HERE, u))]
-    return units
+    return list(CUDA_UNITS)
 
 
 def _stale() -> bool:
@@ -73,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(BUILD, os.path.basename(unit) + ".o")
         if unit.endswith(".cu"):
             cmd = [nvcc()] + ARCH + NVCC_COMMON + flags + ["-c", src, "-o", obj]
-        else:  # host C++ compiled by nvcc's host compiler with the CUDA include path
+        else:  # host-side C++ that also holds small kernels: compiled as CUDA
             cmd = [nvcc()] + NVCC_COMMON + flags + ["-x", "cu", "-c", src, "-o", obj] + ARCH
         jobs.append((cmd, obj))
     for unit, flags in HOST_UNITS:

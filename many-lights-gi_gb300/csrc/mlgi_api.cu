@@ -200,6 +200,20 @@ const char* mlgi_last_error(const mlgi_ctx* ctx) { return ctx ? ctx->err.c_str()
 
 mlgi_stream mlgi_ctx_stream(mlgi_ctx* ctx) { return ctx ? static_cast<mlgi_stream>(ctx->stream) : nullptr; }
 
+mlgi_status mlgi_ctx_reserve(mlgi_ctx* ctx, int max_vpl, size_t max_atlas_texels) {
+    if (!ctx || max_vpl <= 0 || max_atlas_texels == 0) return MLGI_EINVAL;
+    MLGI_CUDA(ctx, cudaSetDevice(ctx->device));
+    MLGI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    mlgi_status st = ensure(ctx, ctx->vpl, (size_t)max_vpl * 48);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->packed, (size_t)max_vpl * 16);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->reduced, (size_t)max_vpl * 24);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->keys, max_atlas_texels * 4);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->depth, max_atlas_texels * 4);
+    const int32_t* shuffle = nullptr;
+    for (int n = 64; st == MLGI_OK && n <= max_vpl; n *= 2) st = get_shuffle(ctx, n, &shuffle);
+    return st;
+}
+
 mlgi_status mlgi_shuffle_table(int n, int32_t* out_host) {
     if (n <= 0 || !out_host) return MLGI_EINVAL;
     shuffle_host(n, out_host);

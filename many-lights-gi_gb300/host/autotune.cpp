@@ -1,7 +1,8 @@
 // Autotuner for a view's GI configuration: interleave factor I, ISM edge and pull-push levels,
 // and the gathering tile. Candidates are timed on the GPU with the real kernels (mlgi_gi_frame on
-// a device-generated room of the requested shape, best of three after one warm-up) and cached per
-// query. Two objectives:
+// a device-generated room of the requested shape, best of three after one warm-up; a candidate
+// whose warm-up is 3x slower than the best so far keeps its warm-up time) and cached per query.
+// Two objectives:
 //   budget_ms == 0: the fastest candidate that meets the quality floor
 //                   (N / I^2 >= min_vpls_per_pixel, ISM edge >= min_ism_size);
 //   budget_ms  > 0: among candidates meeting the floor, the highest quality (most VPLs per pixel,
@@ -68,9 +69,14 @@ extern "C" mlgi_status mlgi_autotune(mlgi_ctx* ctx, const mlgi_autotune_query* q
     const int N = q->n_vpl;
     const int gx = 1 << (int)std::ceil(std::log2((double)N) / 2.0);
     const int gy = (N + gx - 1) / gx;
+    // Interleave factors meeting the floor, largest first. Without a budget only the two largest are
+    // timed: a smaller I evaluates at least 4x the pixel-VPL pairs with the same ISM work.
+    std::vector<int> Is;
+    for (int I : {16, 8, 4, 2, 1})
+        if (N % (I * I) == 0 && N / (I * I) >= std::max(1, q->min_vpls_per_pixel)) Is.push_back(I);
+    if (q->budget_ms <= 0.f && Is.size() > 2) Is.resize(2);
     std::vector<Cand> cands;
-    for (int I : {1, 2, 4, 8, 16}) {
-        if (N % (I * I) || N / (I * I) < std::max(1, q->min_vpls_per_pixel)) continue;
+    for (int I : Is) {
         for (int s : {64, 96, 128}) {
             if (s < q->min_ism_size) continue;
             if ((long long)gx * s > 16384 || (long long)gy * s > 16384) continue;
@@ -132,6 +138,10 @@ extern "C" mlgi_status mlgi_autotune(mlgi_ctx* ctx, const mlgi_autotune_query* q
     f.fg.vpl_format = q->reduced ? MLGI_F16 : MLGI_F32;
     mlgi_radiance out_rgb{q->width, q->height, static_cast<float*>(rgb.p)};
 
+    size_t max_texels = 0;
+    for (const Cand& c : cands) max_texels = std::max(max_texels, (size_t)c.gx * c.gy * c.s * c.s);
+    if ((st = mlgi_ctx_reserve(ctx, N, max_texels)) != MLGI_OK) return st;  // no allocation inside a timing
+    float best_so_far = 1e30f;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -150,10 +160,18 @@ extern "C" mlgi_status mlgi_autotune(mlgi_ctx* ctx, const mlgi_autotune_query* q
             cudaEventSynchronize(e1);
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
-            if (rep > 0) best = std::min(best, ms);  // rep 0 warms up
+            if (rep == 0) {  // warm-up; a candidate already 3x slower than the best so far is not refined
+                if (ms > 3.f * best_so_far) {
+                    best = ms;
+                    break;
+                }
+                continue;
+            }
+            best = std::min(best, ms);
         }
         if (st != MLGI_OK) break;
         c.ms = best;
+        best_so_far = std::min(best_so_far, best);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

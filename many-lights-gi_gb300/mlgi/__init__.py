@@ -107,6 +107,37 @@ class SceneInfo(C.Structure):
                 ("bucket_stride", C.c_int64)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int),
+                ("rsm_size", C.c_int), ("hbm_budget", C.c_size_t)]
+
+
+class Request(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("room_seed", C.c_uint64), ("width", C.c_int), ("height", C.c_int),
+                ("n_vpl", C.c_int), ("n_points", C.c_int64), ("reduced", C.c_int), ("light_yaw_deg", C.c_float),
+                ("light_pitch_deg", C.c_float), ("camera_orbit_deg", C.c_float), ("arrival_s", C.c_double),
+                ("out_host", _p)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("latency_ms", C.c_double), ("queue_ms", C.c_double),
+                ("digest", C.c_uint64), ("sum", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int64), ("inflight", C.c_int64), ("admitted", C.c_int64),
+                ("rooms_resident", C.c_int64), ("budget_waits", C.c_int64), ("evictions", C.c_int64),
+                ("room_bytes", C.c_size_t),
+                ("slot_bytes", C.c_size_t)]
+
+
+class PoissonDesc(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("rate_hz", C.c_double), ("duration_s", C.c_double), ("shapes", _p),
+                ("n_shapes", C.c_int), ("n_rooms", C.c_int), ("room_seed_base", C.c_uint64),
+                ("light_jitter_deg", C.c_float), ("orbit_step_deg", C.c_float), ("drain_timeout_s", C.c_double),
+                ("mode", C.c_int)]
+
+
 # Every entry point of include/mlgi.h with its ctypes signature.
 _SIGS = {
     "mlgi_create": (C.c_int32, [C.POINTER(C.c_void_p), C.POINTER(CtxDesc)]),
@@ -129,6 +160,17 @@ _SIGS = {
     "mlgi_batch_launch": (C.c_int32, [_p, _p]),
     "mlgi_batch_destroy": (None, [_p]),
     "mlgi_autotune": (C.c_int32, [_p, C.POINTER(AutotuneQuery), C.POINTER(AutotuneResult)]),
+    "mlgi_ctx_reserve": (C.c_int32, [_p, C.c_int, C.c_size_t]),
+    "mlgi_server_create": (C.c_int32, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
+    "mlgi_server_prepare": (C.c_int32, [_p, _p, C.c_int]),
+    "mlgi_server_submit": (C.c_int32, [_p, C.POINTER(Request)]),
+    "mlgi_server_cancel": (C.c_int32, [_p, C.c_uint64]),
+    "mlgi_server_poll": (C.c_int, [_p, _p, C.c_int]),
+    "mlgi_server_drain": (C.c_int32, [_p, C.c_double]),
+    "mlgi_server_stats_get": (C.c_int32, [_p, C.POINTER(ServerStats)]),
+    "mlgi_server_destroy": (None, [_p]),
+    "mlgi_server_run_poisson": (C.c_int32, [_p, C.POINTER(PoissonDesc), _p, C.c_int, C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double)]),
     "mlgi_frame_host_sizes_get": (C.c_int32, [C.POINTER(FrameDesc), C.POINTER(FrameHostSizes)]),
     "mlgi_gi_frame_host": (C.c_int32, [_p, C.POINTER(FrameDesc), _p]),
     "mlgi_set_timing": (C.c_int32, [_p, C.c_int]),

@@ -23,7 +23,36 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 15
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
-    assert sorted(mlgi.declared_symbols()) == sorted(n for n in names if n in mlgi.declared_symbols())
+    assert sorted(mlgi.declared_symbols()) == names
+
+
+# ctypes mirror of every struct in include/mlgi.h
+STRUCTS = {"mlgi_ctx_desc": "CtxDesc", "mlgi_rsm_view": "RsmView", "mlgi_vpl_params": "VplParams",
+           "mlgi_vpl_buf": "VplBuf", "mlgi_points": "Points", "mlgi_ism_params": "IsmParams", "mlgi_atlas": "Atlas",
+           "mlgi_gbuffer_view": "GBufferView", "mlgi_fg_params": "FgParams", "mlgi_radiance": "Radiance",
+           "mlgi_frame_desc": "FrameDesc", "mlgi_autotune_query": "AutotuneQuery",
+           "mlgi_autotune_result": "AutotuneResult", "mlgi_frame_host_sizes": "FrameHostSizes",
+           "mlgi_scene_desc": "SceneDesc", "mlgi_scene_info": "SceneInfo", "mlgi_server_desc": "ServerDesc",
+           "mlgi_request": "Request", "mlgi_completion": "Completion", "mlgi_server_stats": "ServerStats",
+           "mlgi_poisson_desc": "PoissonDesc"}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """sizeof of every header struct (from the C compiler) equals its ctypes mirror's size."""
+    import subprocess
+
+    src = open(os.path.join(ROOT, "include", "mlgi.h")).read()
+    declared = set(re.findall(r"\}\s*(mlgi_[a-z0-9_]+)\s*;", src))
+    assert declared == set(STRUCTS), declared ^ set(STRUCTS)
+    prog = tmp_path / "sizes.c"
+    prog.write_text('#include <stdio.h>\n#include "mlgi.h"\nint main(void){\n' +
+                    "".join(f'printf("{k} %zu\\n", sizeof({k}));\n' for k in STRUCTS) + "return 0;}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-std=c99", f"-I{os.path.join(ROOT, 'include')}", str(prog), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    sizes = dict(zip(out[0::2], map(int, out[1::2])))
+    for k, py in STRUCTS.items():
+        assert C.sizeof(getattr(mlgi, py)) == sizes[k], (k, C.sizeof(getattr(mlgi, py)), sizes[k])
 
 
 def test_status_strings():
