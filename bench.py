@@ -48,6 +48,13 @@ def parse():
     return ap.parse_args()
 
 
+def launches_per_frame(cfg):
+    """Kernels of one mlgi_gi_frame: VPL processing, atlas clear, splat, pull-push (level 1, the
+    per-ISM middle levels and push level 1 when there are two or more levels, push level 0) and
+    final gathering."""
+    return 3 + (4 if cfg.levels >= 2 else 2) + 1
+
+
 # ---- algorithmic bytes per pass (one launch each per frame) -------------------------------------
 def algorithmic_bytes(cfg, bucket_stride):
     px = cfg.width * cfg.height
@@ -296,7 +303,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
         "gpixel_vpl_per_s": frames * cfg.width * cfg.height * cfg.n_vpl / (total_ms * 1e-3) / 1e9,
         "evaluated_pairs_per_s": frames * cfg.pairs / (total_ms * 1e-3),
         "passes_ms": {n: float(v) for n, v in zip(PASSES, mean_pass)},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": launches_per_frame(cfg) * args.steps,
         "e2e": {"value": e2e_total / frames, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -397,7 +404,7 @@ def run_batch(args, rank, world, local_rank):
                        "l2": "inputs larger than L2"},
             "frames_per_s": n / (batched_ms * 1e-3), "plain_ms_per_batch": plain_ms,
             "plain_frames_per_s": n / (plain_ms * 1e-3), "speedup_vs_plain": plain_ms / batched_ms,
-            "gpu_launches": 5 * args.steps, "autotune_s": t_tune, "clocks": clocks}), flush=True)
+            "gpu_launches": launches_per_frame(cfg) * args.steps, "autotune_s": t_tune, "clocks": clocks}), flush=True)
     batch.close()
     ctx.close()
 

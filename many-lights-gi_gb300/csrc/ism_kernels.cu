@@ -99,8 +99,15 @@ constexpr int kSplatThreads = 256;
 struct SplatSmem {
     float4 pos[16], n[16];  // xyz used; float4 for 16-byte shared loads
     v3 s[16], u[16];
-    float ism[16];
+    float tx[16], ty[16];   // the VPL's ISM tile offsets, float(x) and float(y) (ism_utils.glsl:35-37)
 };
+
+// 1/x when x is a power of two (then v / x == v * (1/x) bit for bit: both are the rounding of the
+// same real number), else 0.
+__device__ __forceinline__ float pow2_recip(int x) {
+    if (x <= 0 || (x & (x - 1))) return 0.f;
+    return __int_as_float((127 - (31 - __clz(x))) << 23);
+}
 
 // Bucket wg (one block of kSplatThreads threads).
 __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, SplatSmem& S) {
@@ -121,13 +128,18 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, S
         S.n[threadIdx.x] = make_float4(n.x, n.y, n.z, 0.f);
         S.s[threadIdx.x] = s;
         S.u[threadIdx.x] = u;
-        S.ism[threadIdx.x] = a.scale_isms ? float(index) - float(a.vpl_start) : float(index);
+        const float ismIndex = a.scale_isms ? float(index) - float(a.vpl_start) : float(index);
+        const float fgx = float(a.gx);
+        const float ty = float(f2i(ismIndex / fgx));
+        S.tx[threadIdx.x] = float(f2i(ismIndex - ty * fgx));
+        S.ty[threadIdx.x] = float(f2i(ty));
     }
     __syncthreads();
 
     const uint32_t cnt = __ldg(a.counts + wg);
     const float4* bucket = a.points + (int64_t)wg * a.bucket_stride;
     const float fw = float(a.atlas_w), fh = float(a.atlas_h), fgx = float(a.gx), fgy = float(a.gy);
+    const float rgx = pow2_recip(a.gx), rgy = pow2_recip(a.gy);
     for (uint32_t j = threadIdx.x; j < cnt; j += kSplatThreads) {
         const float4 pt = __ldg(bucket + j);
         const v3 position = mk(pt.x, pt.y, pt.z);
@@ -141,10 +153,11 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, S
         int found = 0;
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
+            if (found == 4) break;  // later VPLs are not used (ism.comp:103-106)
             const float4 vp = S.pos[i], vn = S.n[i];
             const v3 rel = position - mk(vp.x, vp.y, vp.z);
             const bool cull = dot(mk(vn.x, vn.y, vn.z), rel) < 0.0f || dot(pn, -rel) < 0.0f;
-            if (!cull && found < 4) {
+            if (!cull) {
                 used |= (uint32_t)i << (4 * found);
                 ++found;
             }
@@ -171,13 +184,10 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, S
             vz = vz * -signOfV;
             vx = (vx + 1.0f) / 2.0f;
             vy = (vy + 1.0f) / 2.0f;
-            const float ismIndex = S.ism[i];
-            const float ty = float(f2i(ismIndex / fgx));
-            const int tx = f2i(ismIndex - ty * fgx);
-            vx = vx + float(tx);
-            vy = vy + float(f2i(ty));
-            vx = vx / fgx;
-            vy = vy / fgy;
+            vx = vx + S.tx[i];
+            vy = vy + S.ty[i];
+            vx = rgx != 0.f ? vx * rgx : vx / fgx;
+            vy = rgy != 0.f ? vy * rgy : vy / fgy;
             vx = vx * fw;
             vy = vy * fh;
             vz = vz * 16777216.0f;
@@ -201,16 +211,40 @@ cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Fused pull-push: one block per ISM. Pull levels and push levels never mix texels of different
-// ISMs (2x2 pulls stay inside an ISM because its edge is divisible by 2^levels, and push gives
-// weight 0 to every coarse texel across an ISM border), so a whole ISM's pyramid lives in shared
-// memory: keys (level 0) plus RGBA texels of levels 1..L. Push level l overwrites pull level l
-// in place (a push texel reads only its own pull texel at that level). Coordinates entering the
-// displacement arithmetic are global atlas coordinates, as in the level-by-level shaders.
-constexpr int kPullPushThreads = 512;
+// Pull-push in up to four launches. Pull and push never mix texels of different ISMs (2x2 pulls
+// stay inside an ISM because its edge is divisible by 2^levels, and push gives weight 0 to every
+// coarse texel across an ISM border), and each texel of a level depends only on texels of the
+// next finer (pull) or next coarser (push) level of its own ISM:
+//   pull1_kernel    level 1 from the keys, one thread per level-1 texel            -> lv1
+//   pullmid_kernel  one block per ISM: pull 2..L, push L-1..2 in shared memory     -> lv2
+//   push1_kernel    push level 1 from lv2 onto lv1 in place, one thread per texel
+//   push0_kernel    push level 0 (depth only) from lv1 and the keys, one thread per texel -> out
+// Texels of levels >= 1 are (depth, maxDepth, radius, packHalf2x16(dx, dy)), the reference's
+// RGBA32F pyramid. Coordinates entering the displacement arithmetic are global coordinates of the
+// level, as in the level-by-level shaders.
+constexpr int kPpTileW = 32, kPpTileH = 8;  // texel tile of the per-texel kernels (256 threads)
+constexpr int kPullMidThreads = 256;
+constexpr int kPpBatchTiles = 4;  // texel tiles per work item of the batched per-texel passes
 constexpr size_t kPullPushTableBytes = 2 * 256 * sizeof(float);  // key-byte tables, see below
 
 __device__ __forceinline__ float pow2neg(int level) { return __int_as_float((127 - level) << 23); }
+
+// sqrt(d2) > r with sqrt correctly rounded, for finite d2 >= 0 and finite r. RN(sqrt(d2)) > r
+// exactly when sqrt(d2) exceeds the midpoint between r and the next float up (a square root of a
+// float is never such a midpoint), i.e. when d2 > r^2 (1 + 2^-24)^2 at most. With p = RN(r*r):
+// d2 > RN(p (1 + 2^-20)) implies d2 > r^2 (1 + 2^-21), above that threshold; d2 < RN(p (1 - 2^-20))
+// implies d2 < r^2, so sqrt(d2) < r and RN(sqrt(d2)) <= r. Only the band in between takes sqrtf,
+// out of line so that the unrolled callers stay small.
+__device__ __noinline__ bool sqrt_gt_band(float d2, float r) { return sqrtf(d2) > r; }
+
+__device__ __forceinline__ bool sqrt_gt(float d2, float r) {
+    const float p = r * r;
+    if (r > 0.f && p >= 1e-30f) {
+        if (d2 > p * 1.00000095367431640625f) return true;
+        if (d2 < p * 0.99999904632568359375f) return false;
+    }
+    return sqrt_gt_band(d2, r);
+}
 
 // x / n for the sample counts and weight sums that occur (n >= 1). Division by a power of two is
 // exact, so it equals the multiply by the reciprocal bit for bit; other n use IEEE division.
@@ -225,249 +259,335 @@ __device__ __forceinline__ float div_count(float x, int n) {
     }
 }
 
-// Shared memory: two 256-entry tables indexed by the key's radius byte b, then levels 1..L.
+// Two 256-entry tables indexed by a key's radius byte b, each entry computed with the shader's own
+// operations so that lookups are bit-identical:
 //   s_rad[b] = float(b) / 10                          (pull.comp:39)
 //   s_mdo[b] = ((float(b) / 10) * 2) / zFar * 0.6     (the maxDepth offset of pull.comp:57)
-// Each entry is computed with the shader's own operations, so lookups are bit-identical.
-// One ISM (one block of kPullPushThreads threads; smem of pullpush_smem_bytes()).
-__device__ __forceinline__ void pullpush_ism(const PullPushArgs& a, const int ism, unsigned char* smem) {
-    __syncthreads();  // the previous ISM's use of smem is over
-    const int s = a.ism_size, L = a.levels;
-    // Level-0 keys are read straight from the atlas (each is read once by pull level 1 and once by
-    // push level 0, both coalesced), so shared memory holds only the tables and levels 1..L.
-    const uint32_t* keys = a.keys;
-    float* s_rad = reinterpret_cast<float*>(smem);
-    float* s_mdo = s_rad + 256;
-    float4* lvl_base = reinterpret_cast<float4*>(smem + kPullPushTableBytes);
-    const int bx = (ism % a.grid_x) * s, by = (ism / a.grid_x) * s;
-    const int nt = blockDim.x, tid = threadIdx.x;
-    for (int b = tid; b < 256; b += nt) {
+__device__ __forceinline__ void fill_key_tables(float* s_rad, float* s_mdo, float z_far) {
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) {
         const float r = float(b) / 10.0f;
         s_rad[b] = r;
-        s_mdo[b] = (r * 2.0f) / a.z_far * 0.6f;
+        s_mdo[b] = (r * 2.0f) / z_far * 0.6f;
     }
-    __syncthreads();
+}
 
-    // level l data starts at lvl_off(l) texels from lvl_base
-    auto lvl = [&](int l) {
+struct PullSample {
+    float depth, maxDepth, radius, ndx, ndy;
+};
+
+// One pull output from its four samples in the order (0,0), (0,1), (1,0), (1,1) (pull.comp:60-120).
+__device__ __forceinline__ float4 pull_combine(const PullSample (&q)[4], const float scale) {
+    bool valid[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)  // dist <= radius * scale, dist = length(displacement)
+        valid[k] = q[k].depth != 1.0f && !sqrt_gt(q[k].ndx * q[k].ndx + q[k].ndy * q[k].ndy, q[k].radius * scale);
+    float minimum = __int_as_float(0x7f800000);
+    float maxDepth = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!valid[k]) continue;
+        minimum = gmin(q[k].depth, minimum);
+        if (minimum == q[k].depth) maxDepth = q[k].maxDepth;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (q[k].depth > maxDepth) valid[k] = false;
+    float depthAcc = 0.f, radiusAcc = 0.f, maxValid = 0.f, dax = 0.f, day = 0.f;
+    int numValid = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!valid[k]) continue;
+        depthAcc = depthAcc + q[k].depth;
+        dax = dax + q[k].ndx;
+        day = day + q[k].ndy;
+        radiusAcc = radiusAcc + q[k].radius;
+        maxValid = gmax(maxValid, q[k].maxDepth);
+        numValid++;
+    }
+    if (numValid == 0) return make_float4(1.0f, 0.f, 0.f, 0.f);
+    return make_float4(div_count(depthAcc, numValid), maxValid, div_count(radiusAcc, numValid),
+                       __uint_as_float(pack_half2(div_count(dax, numValid), div_count(day, numValid))));
+}
+
+__device__ constexpr int kPullOff[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};
+
+// Pull level 1 at global level-1 texel (gox, goy) from the four keys below it. The displacement
+// of a key sample is exactly (+-0.25, +-0.25) (dx = dy = 0 at level 0).
+__device__ __forceinline__ float4 pull1_texel(const PullPushArgs& a, const float* s_rad, const float* s_mdo,
+                                              const int gox, const int goy) {
+    const uint2 r0 = __ldg(reinterpret_cast<const uint2*>(a.keys + (size_t)(2 * goy) * a.atlas_w + 2 * gox));
+    const uint2 r1 = __ldg(reinterpret_cast<const uint2*>(a.keys + (size_t)(2 * goy + 1) * a.atlas_w + 2 * gox));
+    const uint32_t key[4] = {r0.x, r1.x, r0.y, r1.y};  // (0,0), (0,1), (1,0), (1,1)
+    const float fs = float(a.ism_size);
+    PullSample q[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float depthSample = float(key[k] >> 8) / 16777216.0f;
+        q[k].depth = depthSample;
+        q[k].maxDepth = depthSample + s_mdo[key[k] & 0xFFu];
+        const float distToCamera = depthSample * a.z_far;
+        float radius = s_rad[key[k] & 0xFFu] / distToCamera / 3.14f * fs;
+        radius = radius * 1.3f;
+        q[k].radius = gmin(radius, 15.0f);
+        q[k].ndx = kPullOff[k][0] ? 0.25f : -0.25f;
+        q[k].ndy = kPullOff[k][1] ? 0.25f : -0.25f;
+    }
+    return pull_combine(q, 0.5f);
+}
+
+// Pull level l >= 2 at global level-l texel (gox, goy); `in` is level l-1 with row pitch `pin`
+// and origin (ix0, iy0) in global level-(l-1) coordinates.
+__device__ __forceinline__ float4 pull_texel(const float4* in, const int pin, const int ix0, const int iy0,
+                                             const int gox, const int goy, const float scale) {
+    PullSample q[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int gix = 2 * gox + kPullOff[k][0], giy = 2 * goy + kPullOff[k][1];
+        const float4 t = in[(giy - iy0) * pin + (gix - ix0)];
+        const float2 d = unpack_half2(__float_as_uint(t.w));
+        q[k].depth = t.x;
+        q[k].maxDepth = t.y;
+        q[k].radius = t.z;
+        q[k].ndx = (float(gix) + 0.5f + d.x) / 2.0f - (float(gox) + 0.5f);
+        q[k].ndy = (float(giy) + 0.5f + d.y) / 2.0f - (float(goy) + 0.5f);
+    }
+    return pull_combine(q, scale);
+}
+
+__device__ constexpr int kPushOff[4][2] = {{0, 0}, {0, 1}, {1, 1}, {1, 0}};
+
+// floor(n / d) for n < 2^16 and 2 <= d < 2^16 from m = ceil(2^32 / d): the error of n * m / 2^32
+// is below n / 2^32 < 1 / d, too small to cross an integer.
+__device__ __forceinline__ int div_small(int n, uint32_t m) { return (int)__umulhi((uint32_t)n, m); }
+
+// Push at level l for a level-l texel at position (qx, qy) = ((px + 1) & 1, (py + 1) & 1) of its
+// 2x2 quad gid = ((px + 1) >> 1, (py + 1) >> 1) (push.comp:44-165). Coarse texel k is
+// gid - 1 + kPushOff[k] at level l+1, zero when it lies outside this ISM (`inside[k]` false:
+// weight 0, push.comp:77-86). The shader's weight of coarse texel k for quad output op,
+// {9, 3, 1, 3}[(k - op) & 3], is 3 per coordinate that k shares with the output's quad position
+// times 1 per coordinate it does not. `orig` is the texel's pull value; kFull: all four channels
+// (levels >= 1), else the depth channel only (level 0, push.comp:33-37).
+template <bool kFull>
+__device__ __forceinline__ float4 push_texel(const float4 (&coarse)[4], const bool (&inside)[4], const int qx,
+                                             const int qy, const float4 orig, const float scale) {
+    float depths[4], maxDepths[4], radiuses[4], dvx[4], dvy[4];
+    int w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int kx = kPushOff[k][0], ky = kPushOff[k][1];
+        const float4 t = coarse[k];
+        const float2 d = unpack_half2(__float_as_uint(t.w));
+        depths[k] = t.x;
+        maxDepths[k] = t.y;
+        radiuses[k] = t.z;
+        // weight 0 for invalid depth (push.comp:88-93)
+        w[k] = inside[k] && t.x != 1.0f ? (kx == qx ? 3 : 1) * (ky == qy ? 3 : 1) : 0;
+        // (ctx - (px + 0.5)) with ctx = (gid - 1 + kx + 0.5) * 2 and px = 2 gid - 1 + qx is exactly
+        // 2 kx - qx - 0.5 (all integers below 2^24)
+        const float ox = qx ? float(2 * kx) - 1.5f : float(2 * kx) - 0.5f;
+        const float oy = qy ? float(2 * ky) - 1.5f : float(2 * ky) - 0.5f;
+        dvx[k] = ox + d.x * 2.0f;
+        dvy[k] = oy + d.y * 2.0f;
+        if (w[k] != 0 && sqrt_gt(dvx[k] * dvx[k] + dvy[k] * dvy[k], radiuses[k] * scale)) w[k] = 0;
+    }
+    float minimum = 9001.0f, maxDepth = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (w[k] == 0) continue;
+        minimum = gmin(depths[k], minimum);
+        if (minimum == depths[k]) maxDepth = maxDepths[k];
+    }
+    int weightAcc = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (depths[k] > maxDepth) w[k] = 0;
+        weightAcc += w[k];
+    }
+    const bool invalid = orig.x == 1.0f;
+    bool occluded = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) occluded = occluded || (w[k] > 0 && orig.x > maxDepths[k]);
+    float4 r = orig;
+    // the weighted mean is only needed when it replaces the texel (push.comp:158-161);
+    // zero-weight terms add +0 and are skipped
+    if (!(weightAcc <= 0 || (!invalid && !occluded))) {
+        float depthAcc = 0.f, maxDepthAcc = 0.f, radiusAcc = 0.f, dax = 0.f, day = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (w[k] == 0) continue;
+            const float wf = float(w[k]);
+            depthAcc = depthAcc + depths[k] * wf;
+            if (kFull) {
+                maxDepthAcc = maxDepthAcc + maxDepths[k] * wf;
+                radiusAcc = radiusAcc + radiuses[k] * wf;
+                dax = dax + dvx[k] * wf;
+                day = day + dvy[k] * wf;
+            }
+        }
+        r.x = div_count(depthAcc, weightAcc);
+        if (kFull) {
+            r.y = div_count(maxDepthAcc, weightAcc);
+            r.z = div_count(radiusAcc, weightAcc);
+            r.w = __uint_as_float(pack_half2(div_count(dax, weightAcc), div_count(day, weightAcc)));
+        }
+    }
+    return r;
+}
+
+// The coarse texels of level-l texel (px, py): level l+1 is `c` (row pitch pc) and this ISM covers
+// [c0x, c0x + sc) x [c0y, c0y + sc) of it. Indices fit 32 bits: atlas sides are below 65536.
+__device__ __forceinline__ void push_gather(const float4* c, const uint32_t pc, const int px, const int py,
+                                            const int c0x, const int c0y, const int sc, float4 (&coarse)[4],
+                                            bool (&inside)[4]) {
+    const int gidx = (px + 1) >> 1, gidy = (py + 1) >> 1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int cx = gidx - 1 + kPushOff[k][0], cy = gidy - 1 + kPushOff[k][1];
+        inside[k] = cx >= c0x && cy >= c0y && cx < c0x + sc && cy < c0y + sc;
+        coarse[k] = inside[k] ? c[(uint32_t)cy * pc + (uint32_t)cx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// Per-texel passes on a kPpTileW x kPpTileH tile (tx, ty) of their level.
+__device__ __forceinline__ void pull1_tile(const PullPushArgs& a, const int tx, const int ty, const float* s_rad,
+                                           const float* s_mdo) {
+    const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = ty * kPpTileH + (threadIdx.x / kPpTileW);
+    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
+    if (x < w1 && y < h1) a.lv1[(uint32_t)y * w1 + x] = pull1_texel(a, s_rad, s_mdo, x, y);
+}
+
+__device__ __forceinline__ void push1_tile(const PullPushArgs& a, const int tx, const int ty) {
+    const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = ty * kPpTileH + (threadIdx.x / kPpTileW);
+    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
+    if (x >= w1 || y >= h1) return;
+    const int sc = a.ism_size >> 2;  // ISM edge at level 2
+    float4 coarse[4];
+    bool inside[4];
+    push_gather(a.lv2, a.atlas_w >> 2, x, y, div_small(x, a.m_s1) * sc, div_small(y, a.m_s1) * sc, sc, coarse, inside);
+    float4* t = a.lv1 + (uint32_t)y * w1 + x;
+    *t = push_texel<true>(coarse, inside, (x + 1) & 1, (y + 1) & 1, *t, 0.5f);
+}
+
+__device__ __forceinline__ void push0_tile(const PullPushArgs& a, const int tx, const int ty) {
+    const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = ty * kPpTileH + (threadIdx.x / kPpTileW);
+    if (x >= a.atlas_w || y >= a.atlas_h) return;
+    const int sc = a.ism_size >> 1;  // ISM edge at level 1
+    float4 coarse[4];
+    bool inside[4];
+    push_gather(a.lv1, a.atlas_w >> 1, x, y, div_small(x, a.m_s0) * sc, div_small(y, a.m_s0) * sc, sc, coarse, inside);
+    const uint32_t o = (uint32_t)y * a.atlas_w + x;
+    const float4 orig = make_float4(float(__ldg(a.keys + o) >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
+    const float d = push_texel<false>(coarse, inside, (x + 1) & 1, (y + 1) & 1, orig, 1.0f).x;
+    if (a.out_f16)
+        reinterpret_cast<__half*>(a.out)[o] = __float2half_rn(d);
+    else
+        reinterpret_cast<float*>(a.out)[o] = d;
+}
+
+// Levels 2..L of one ISM in shared memory (tables first, then level 2, 3, ...): pull from lv1,
+// push back down to level 2, which is written to lv2.
+__device__ __forceinline__ void pullmid_ism(const PullPushArgs& a, const int ism, unsigned char* smem) {
+    __syncthreads();  // the previous ISM's use of smem is over
+    const int s = a.ism_size, L = a.levels;
+    float4* lvl_base = reinterpret_cast<float4*>(smem + kPullPushTableBytes);
+    auto lvl = [&](int l) {  // level l >= 2 in shared memory, row pitch s >> l
         size_t off = 0;
-        for (int k = 1; k < l; ++k) off += (size_t)(s >> k) * (s >> k);
+        for (int k = 2; k < l; ++k) off += (size_t)(s >> k) * (s >> k);
         return lvl_base + off;
     };
-
-    // ---- pull, levels 1..L (pull.comp) ----
-    const int poff[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};
-    for (int l = 1; l <= L; ++l) {
-        const int sl = s >> l, si = s >> (l - 1);
-        const int ox0 = bx >> l, oy0 = by >> l;
-        const float4* in = l == 1 ? nullptr : lvl(l - 1);
+    const int ix = ism % a.grid_x, iy = ism / a.grid_x;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    for (int l = 2; l <= L; ++l) {  // pull
+        const int sl = s >> l;
+        const int ox0 = ix * sl, oy0 = iy * sl;
         float4* out = lvl(l);
         const float scale = pow2neg(l);
         for (int i = tid; i < sl * sl; i += nt) {
-            const int lx = i % sl, ly = i / sl;
-            const int gox = ox0 + lx, goy = oy0 + ly;
-            float depthSamples[4], maxDepths[4], radiuses[4], dvx[4], dvy[4];
-            bool valid[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int lix = 2 * lx + poff[k][0], liy = 2 * ly + poff[k][1];
-                const int gix = 2 * gox + poff[k][0], giy = 2 * goy + poff[k][1];
-                float depthSample, radius, maxDepth, dx, dy;
-                if (l == 1) {
-                    const uint32_t key = __ldg(keys + (size_t)(by + liy) * a.atlas_w + bx + lix);
-                    depthSample = float(key >> 8) / 16777216.0f;
-                    dx = 0.f;
-                    dy = 0.f;
-                    maxDepth = depthSample + s_mdo[key & 0xFFu];
-                    const float distToCamera = depthSample * a.z_far;
-                    radius = s_rad[key & 0xFFu] / distToCamera / 3.14f * float(s);
-                    radius = radius * 1.3f;
-                    radius = gmin(radius, 15.0f);
-                } else {
-                    const float4 t = in[liy * si + lix];
-                    depthSample = t.x;
-                    maxDepth = t.y;
-                    radius = t.z;
-                    const float2 d = unpack_half2(__float_as_uint(t.w));
-                    dx = d.x;
-                    dy = d.y;
-                }
-                const float ndx = (float(gix) + 0.5f + dx) / 2.0f - (float(gox) + 0.5f);
-                const float ndy = (float(giy) + 0.5f + dy) / 2.0f - (float(goy) + 0.5f);
-                const float dist = sqrtf(ndx * ndx + ndy * ndy);
-                const bool pass = dist <= radius * scale;
-                depthSamples[k] = depthSample;
-                maxDepths[k] = maxDepth;
-                radiuses[k] = radius;
-                dvx[k] = ndx;
-                dvy[k] = ndy;
-                valid[k] = depthSample != 1.0f && pass;
-            }
-            float minimum = __int_as_float(0x7f800000);
-            float maxDepth = 0.f;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!valid[k]) continue;
-                minimum = gmin(depthSamples[k], minimum);
-                if (minimum == depthSamples[k]) maxDepth = maxDepths[k];
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (depthSamples[k] > maxDepth) valid[k] = false;
-            float depthAcc = 0.f, radiusAcc = 0.f, maxValid = 0.f, dax = 0.f, day = 0.f;
-            int numValid = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!valid[k]) continue;
-                depthAcc = depthAcc + depthSamples[k];
-                dax = dax + dvx[k];
-                day = day + dvy[k];
-                radiusAcc = radiusAcc + radiuses[k];
-                maxValid = gmax(maxValid, maxDepths[k]);
-                numValid++;
-            }
-            float4 r;
-            if (numValid > 0) {
-                r = make_float4(div_count(depthAcc, numValid), maxValid, div_count(radiusAcc, numValid),
-                                __uint_as_float(pack_half2(div_count(dax, numValid), div_count(day, numValid))));
-            } else {
-                r = make_float4(1.0f, 0.f, 0.f, 0.f);
-            }
-            out[i] = r;
+            const int gox = ox0 + i % sl, goy = oy0 + i / sl;
+            out[i] = l == 2 ? pull_texel(a.lv1, a.atlas_w >> 1, 0, 0, gox, goy, scale)
+                            : pull_texel(lvl(l - 1), 2 * sl, 2 * ox0, 2 * oy0, gox, goy, scale);
         }
         __syncthreads();
     }
-
-    // ---- push, levels L-1..0 (push.comp): one thread per 2x2 output quad sharing the same four
-    // coarse texels, as in the shader; outputs outside this ISM are skipped ----
-    const int qoff[4][2] = {{0, 0}, {0, 1}, {1, 1}, {1, 0}};
-    const int weightsX[4] = {9, 3, 1, 3};
-    for (int l = L - 1; l >= 0; --l) {
-        const int sl = s >> l, sc = s >> (l + 1), nq = sc + 1;
-        const int o0x = bx >> l, o0y = by >> l;              // this ISM's origin at level l
-        const int c0x = bx >> (l + 1), c0y = by >> (l + 1);  // and at level l+1
-        const float4* coarse = lvl(l + 1);
-        float4* same = l == 0 ? nullptr : lvl(l);
+    for (int l = L - 1; l >= 2; --l) {  // push in place: a texel reads only its own pull value
+        const int sl = s >> l;
+        const int ox0 = ix * sl, oy0 = iy * sl;
+        const float4* coarse_lvl = lvl(l + 1);
+        float4* same = lvl(l);
         const float scale = pow2neg(l);
-        for (int q = tid; q < nq * nq; q += nt) {
-            const int gidx = c0x + q % nq, gidy = c0y + q / nq;  // global gid of the quad
-            const int cllx = gidx - 1, clly = gidy - 1;
-            float depths[4], maxDepths[4], radiuses[4], dcx[4], dcy[4], rs[4];
-            bool usable[4];
+        const int sc = sl >> 1;
+        for (int i = tid; i < sl * sl; i += nt) {
+            const int px = ox0 + i % sl, py = oy0 + i / sl;
+            // the coarse texels, as push_gather but on the ISM-local level in shared memory
+            float4 coarse[4];
+            bool inside[4];
+            const int gidx = (px + 1) >> 1, gidy = (py + 1) >> 1;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const int cx = cllx + qoff[k][0] - c0x, cy = clly + qoff[k][1] - c0y;
-                if (cx >= 0 && cy >= 0 && cx < sc && cy < sc) {
-                    const float4 t = coarse[cy * sc + cx];
-                    depths[k] = t.x;
-                    maxDepths[k] = t.y;
-                    radiuses[k] = t.z;
-                    const float2 d = unpack_half2(__float_as_uint(t.w));
-                    dcx[k] = d.x;
-                    dcy[k] = d.y;
-                    // weight 0 for invalid depth (push.comp:88-93)
-                    usable[k] = depths[k] != 1.0f;
-                } else {  // across the ISM border: weight 0 (push.comp:77-86)
-                    depths[k] = maxDepths[k] = radiuses[k] = dcx[k] = dcy[k] = 0.f;
-                    usable[k] = false;
-                }
-                rs[k] = radiuses[k] * scale;
+                const int cx = gidx - 1 + kPushOff[k][0] - ix * sc, cy = gidy - 1 + kPushOff[k][1] - iy * sc;
+                inside[k] = cx >= 0 && cy >= 0 && cx < sc && cy < sc;
+                coarse[k] = inside[k] ? coarse_lvl[cy * sc + cx] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-#pragma unroll
-            for (int op = 0; op < 4; ++op) {
-                const int px = gidx * 2 - 1 + qoff[op][0], py = gidy * 2 - 1 + qoff[op][1];
-                const int lpx = px - o0x, lpy = py - o0y;
-                if (lpx < 0 || lpy < 0 || lpx >= sl || lpy >= sl) continue;
-                int w[4];
-                float dvx[4], dvy[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    w[k] = usable[k] ? weightsX[(k - op + 4) & 3] : 0;
-                    const float ctx = (float(cllx + qoff[k][0]) + 0.5f) * 2.0f;
-                    const float cty = (float(clly + qoff[k][1]) + 0.5f) * 2.0f;
-                    dvx[k] = ctx - (float(px) + 0.5f) + dcx[k] * 2.0f;
-                    dvy[k] = cty - (float(py) + 0.5f) + dcy[k] * 2.0f;
-                    if (w[k] != 0 && sqrtf(dvx[k] * dvx[k] + dvy[k] * dvy[k]) > rs[k]) w[k] = 0;
-                }
-                float minimum = 9001.0f, maxDepth = 0.f;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    if (w[k] == 0) continue;
-                    minimum = gmin(depths[k], minimum);
-                    if (minimum == depths[k]) maxDepth = maxDepths[k];
-                }
-                int weightAcc = 0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    if (depths[k] > maxDepth) w[k] = 0;
-                    weightAcc += w[k];
-                }
-                const int lp = lpy * sl + lpx;
-                float4 orig;
-                if (l == 0) {
-                    orig = make_float4(float(__ldg(keys + (size_t)py * a.atlas_w + px) >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
-                } else {
-                    orig = same[lp];
-                }
-                const bool invalid = orig.x == 1.0f;
-                bool occluded = false;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) occluded = occluded || (w[k] > 0 && orig.x > maxDepths[k]);
-                float4 r = orig;
-                // the weighted mean is only needed when it replaces the texel (push.comp:158-161);
-                // zero-weight terms add +0 and are skipped
-                if (!(weightAcc <= 0 || (!invalid && !occluded))) {
-                    float depthAcc = 0.f, maxDepthAcc = 0.f, radiusAcc = 0.f, dax = 0.f, day = 0.f;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        if (w[k] == 0) continue;
-                        const float wf = float(w[k]);
-                        depthAcc = depthAcc + depths[k] * wf;
-                        if (l > 0) {
-                            maxDepthAcc = maxDepthAcc + maxDepths[k] * wf;
-                            radiusAcc = radiusAcc + radiuses[k] * wf;
-                            dax = dax + dvx[k] * wf;
-                            day = day + dvy[k] * wf;
-                        }
-                    }
-                    r.x = div_count(depthAcc, weightAcc);
-                    if (l > 0) {  // level 0 writes only the depth channel (push.comp:33-37)
-                        r.y = div_count(maxDepthAcc, weightAcc);
-                        r.z = div_count(radiusAcc, weightAcc);
-                        r.w = __uint_as_float(pack_half2(div_count(dax, weightAcc), div_count(day, weightAcc)));
-                    }
-                }
-                if (l == 0) {
-                    const size_t o = (size_t)py * a.atlas_w + px;
-                    if (a.out_f16)
-                        reinterpret_cast<__half*>(a.out)[o] = __float2half_rn(r.x);
-                    else
-                        reinterpret_cast<float*>(a.out)[o] = r.x;
-                } else {
-                    same[lp] = r;
-                }
-            }
+            same[i] = push_texel<true>(coarse, inside, (px + 1) & 1, (py + 1) & 1, same[i], scale);
         }
         __syncthreads();
     }
+    const int s2 = s >> 2, w2 = a.atlas_w >> 2;
+    const float4* l2 = lvl(2);
+    for (int i = tid; i < s2 * s2; i += nt)
+        a.lv2[(size_t)(iy * s2 + i / s2) * w2 + ix * s2 + i % s2] = l2[i];
 }
 
-__global__ void __launch_bounds__(kPullPushThreads, 2) pullpush_kernel(PullPushArgs a) {
+__global__ void __launch_bounds__(kPpTileW * kPpTileH) pull1_kernel(PullPushArgs a) {
+    __shared__ float s_tab[512];
+    fill_key_tables(s_tab, s_tab + 256, a.z_far);
+    __syncthreads();
+    pull1_tile(a, blockIdx.x, blockIdx.y, s_tab, s_tab + 256);
+}
+
+__global__ void __launch_bounds__(kPullMidThreads) pullmid_kernel(PullPushArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    pullpush_ism(a, blockIdx.x, smem);
+    pullmid_ism(a, blockIdx.x, smem);
 }
 
-size_t pullpush_smem_bytes(int ism_size, int levels) {
+__global__ void __launch_bounds__(kPpTileW * kPpTileH) push1_kernel(PullPushArgs a) {
+    push1_tile(a, blockIdx.x, blockIdx.y);
+}
+
+__global__ void __launch_bounds__(kPpTileW * kPpTileH) push0_kernel(PullPushArgs a) {
+    push0_tile(a, blockIdx.x, blockIdx.y);
+}
+
+size_t pullmid_smem_bytes(int ism_size, int levels) {
     size_t b = kPullPushTableBytes;
-    for (int l = 1; l <= levels; ++l) b += (size_t)(ism_size >> l) * (ism_size >> l) * 16;
+    for (int l = 2; l <= levels; ++l) b += (size_t)(ism_size >> l) * (ism_size >> l) * 16;
     return b;
 }
 
+size_t pullpush_scratch_bytes(int atlas_w, int atlas_h, int levels, size_t* lv2_offset) {
+    const size_t lv1 = (size_t)(atlas_w >> 1) * (atlas_h >> 1) * 16;
+    const size_t lv2 = levels >= 2 ? (size_t)(atlas_w >> 2) * (atlas_h >> 2) * 16 : 0;
+    if (lv2_offset) *lv2_offset = (lv1 + 255) & ~(size_t)255;
+    return ((lv1 + 255) & ~(size_t)255) + lv2;
+}
+
+__host__ __device__ __forceinline__ int tiles_x(int w) { return (w + kPpTileW - 1) / kPpTileW; }
+__host__ __device__ __forceinline__ int tiles_y(int h) { return (h + kPpTileH - 1) / kPpTileH; }
+// Work items of the batched per-texel passes: runs of kPpBatchTiles tiles along a tile row.
+__host__ __device__ __forceinline__ int row_items(int w) { return (tiles_x(w) + kPpBatchTiles - 1) / kPpBatchTiles; }
+
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s) {
-    const size_t smem = pullpush_smem_bytes(a.ism_size, a.levels);
-    cudaError_t e = cudaFuncSetAttribute(pullpush_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    pullpush_kernel<<<a.grid_x * a.grid_y, kPullPushThreads, smem, s>>>(a);
+    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
+    const dim3 g1(tiles_x(w1), tiles_y(h1)), g0(tiles_x(a.atlas_w), tiles_y(a.atlas_h));
+    pull1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    if (a.levels >= 2) {
+        const size_t smem = pullmid_smem_bytes(a.ism_size, a.levels);
+        cudaError_t e = cudaFuncSetAttribute(pullmid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pullmid_kernel<<<a.grid_x * a.grid_y, kPullMidThreads, smem, s>>>(a);
+        push1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    }
+    push0_kernel<<<g0, kPpTileW * kPpTileH, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -522,16 +642,81 @@ __global__ void __launch_bounds__(kSplatThreads) batch_splat_kernel(BatchTable t
     }
 }
 
-__global__ void __launch_bounds__(kPullPushThreads, 2) batch_pullpush_kernel(BatchTable t) {
-    extern __shared__ __align__(16) unsigned char smem[];
+// Pull-push passes over the view table. An item is kPpBatchTiles texel tiles (or one ISM for the
+// middle pass); the view's arguments (and the key tables of pull level 1) are staged in shared
+// memory when a block moves to another view.
+__device__ __forceinline__ bool stage_pp_args(const BatchTable& t, const int v, int& cur, PullPushArgs& args) {
+    if (v == cur) return false;  // v is uniform over the block
+    __syncthreads();
+    if (threadIdx.x == 0) args = t.views[v].pp;
+    __syncthreads();
+    cur = v;
+    return true;
+}
+
+__global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_pull1_kernel(BatchTable t) {
+    __shared__ float s_tab[512];
     __shared__ PullPushArgs args;
-    const int* pre = t.prefix + kBpPullPush * (t.n_views + 1);
+    const int* pre = t.prefix + kBpPull1 * (t.n_views + 1);
+    int cur = -1;
     for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
         const int v = find_view(pre, t.n_views, item);
-        __syncthreads();
-        if (threadIdx.x == 0) args = t.views[v].pp;
-        __syncthreads();
-        pullpush_ism(args, item - __ldg(pre + v), smem);
+        if (stage_pp_args(t, v, cur, args)) {
+            fill_key_tables(s_tab, s_tab + 256, args.z_far);
+            __syncthreads();
+        }
+        const int w1 = args.atlas_w >> 1, per_row = row_items(w1), i = item - __ldg(pre + v);
+        const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
+        for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(w1); ++tx) pull1_tile(args, tx, ty, s_tab, s_tab + 256);
+    }
+}
+
+__global__ void __launch_bounds__(kPullMidThreads) batch_pullmid_kernel(BatchTable t) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ PullPushArgs args;
+    const int* pre = t.prefix + kBpPullMid * (t.n_views + 1);
+    int cur = -1;
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        const int v = find_view(pre, t.n_views, item);
+        stage_pp_args(t, v, cur, args);
+        pullmid_ism(args, item - __ldg(pre + v), smem);
+    }
+}
+
+__global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push1_kernel(BatchTable t) {
+    __shared__ PullPushArgs args;
+    const int* pre = t.prefix + kBpPush1 * (t.n_views + 1);
+    int cur = -1;
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        const int v = find_view(pre, t.n_views, item);
+        stage_pp_args(t, v, cur, args);
+        const int w1 = args.atlas_w >> 1, per_row = row_items(w1), i = item - __ldg(pre + v);
+        const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
+        for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(w1); ++tx) push1_tile(args, tx, ty);
+    }
+}
+
+__global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push0_kernel(BatchTable t) {
+    __shared__ PullPushArgs args;
+    const int* pre = t.prefix + kBpPush0 * (t.n_views + 1);
+    int cur = -1;
+    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
+        const int v = find_view(pre, t.n_views, item);
+        stage_pp_args(t, v, cur, args);
+        const int w = args.atlas_w, per_row = row_items(w), i = item - __ldg(pre + v);
+        const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
+        for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(w); ++tx) push0_tile(args, tx, ty);
+    }
+}
+
+int pullpush_batch_items(int pass, int atlas_w, int atlas_h, int ism_count, int levels) {
+    const int w1 = atlas_w >> 1, h1 = atlas_h >> 1;
+    switch (pass) {
+        case kBpPull1: return row_items(w1) * tiles_y(h1);
+        case kBpPullMid: return levels >= 2 ? ism_count : 0;
+        case kBpPush1: return levels >= 2 ? row_items(w1) * tiles_y(h1) : 0;
+        case kBpPush0: return row_items(atlas_w) * tiles_y(atlas_h);
+        default: return 0;
     }
 }
 
@@ -541,9 +726,12 @@ cudaError_t launch_batch_ism(const BatchTable& t, int pass, int grid, size_t sme
         case kBpClear: batch_clear_kernel<<<grid, 256, 0, s>>>(t); break;
         case kBpVpl: batch_vpl_kernel<<<grid, kBatchVplPerItem, 0, s>>>(t); break;
         case kBpSplat: batch_splat_kernel<<<grid, kSplatThreads, 0, s>>>(t); break;
-        case kBpPullPush:  // the dynamic shared-memory limit was raised by batch_blocks_per_sm()
-            batch_pullpush_kernel<<<grid, kPullPushThreads, smem, s>>>(t);
+        case kBpPull1: batch_pull1_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(t); break;
+        case kBpPullMid:  // the dynamic shared-memory limit was raised by batch_blocks_per_sm()
+            batch_pullmid_kernel<<<grid, kPullMidThreads, smem, s>>>(t);
             break;
+        case kBpPush1: batch_push1_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(t); break;
+        case kBpPush0: batch_push0_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(t); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -551,14 +739,18 @@ cudaError_t launch_batch_ism(const BatchTable& t, int pass, int grid, size_t sme
 
 int batch_blocks_per_sm(int pass, size_t smem) {
     int n = 1;
+    const int tt = kPpTileW * kPpTileH;
     switch (pass) {
         case kBpClear: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_clear_kernel, 256, 0); break;
         case kBpVpl: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_vpl_kernel, kBatchVplPerItem, 0); break;
         case kBpSplat: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_splat_kernel, kSplatThreads, 0); break;
-        case kBpPullPush:
-            cudaFuncSetAttribute(batch_pullpush_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pullpush_kernel, kPullPushThreads, smem);
+        case kBpPull1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pull1_kernel, tt, 0); break;
+        case kBpPullMid:
+            cudaFuncSetAttribute(batch_pullmid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pullmid_kernel, kPullMidThreads, smem);
             break;
+        case kBpPush1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_push1_kernel, tt, 0); break;
+        case kBpPush0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_push0_kernel, tt, 0); break;
         default: break;
     }
     return n > 0 ? n : 1;

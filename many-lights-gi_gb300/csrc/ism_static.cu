@@ -5,15 +5,16 @@
 // process whose device memory is fully reserved up front by another allocator, a plugin that is
 // only handed pre-allocated buffers, or a callback that runs while the CUDA allocator is locked.
 // Such callers still pass their own input (points, VPLs) and output (final depth atlas) buffers;
-// only the intermediate key atlas lives here.
+// only the intermediates -- the key atlas and pull-push pyramid levels 1 and 2 -- live here.
 //
 // Limits and behaviour:
 //   * The key atlas holds at most kStaticKeyTexels = 1,048,576 texels (a 1024 x 1024 atlas,
-//     4 MiB). Larger atlases are rejected with MLGI_EINVAL. Every GPU that loads this library
-//     keeps those 4 MiB reserved until the process exits.
-//   * The first call on a device resolves the array's device address (cudaGetSymbolAddress)
+//     4 MiB), the pyramid levels a quarter and a sixteenth of that as float4 (5 MiB). Larger
+//     atlases are rejected with MLGI_EINVAL. Every GPU that loads this library keeps those 9 MiB
+//     reserved until the process exits.
+//   * The first call on a device resolves the arrays' device addresses (cudaGetSymbolAddress)
 //     with that device current; make that first call before any stream capture.
-//   * All calls share the one array. Each call clears it to the empty key (0xFFFFFFFF) before
+//   * All calls share the one set of arrays. Each call clears it to the empty key (0xFFFFFFFF) before
 //     splatting, so nothing of a previous call leaks into the result, but calls whose work
 //     overlaps on the GPU (different streams, or different host threads) race on it.
 //   * No cudaMalloc, cudaFree or allocating library call is made.
@@ -28,14 +29,20 @@ namespace {
 
 constexpr size_t kStaticKeyTexels = size_t(1) << 20;
 
+// levels 1 and 2 of a kStaticKeyTexels atlas, laid out as pullpush_scratch_bytes() describes
+constexpr size_t kStaticPyramidFloat4 = (kStaticKeyTexels / 4) + 16 + kStaticKeyTexels / 16;
+
 __device__ __align__(256) uint32_t g_static_keys[kStaticKeyTexels];
+__device__ __align__(256) float4 g_static_pyramid[kStaticPyramidFloat4];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 uint32_t* g_static_keys_dev[kMaxDevices] = {};
+void* g_static_pyramid_dev[kMaxDevices] = {};
 
-// Device address of g_static_keys on the current device (resolved once per device).
-mlgi_status static_keys_address(uint32_t** out) {
+// Device addresses of g_static_keys and g_static_pyramid on the current device (resolved once
+// per device).
+mlgi_status static_addresses(uint32_t** keys, void** pyramid) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
@@ -44,15 +51,18 @@ mlgi_status static_keys_address(uint32_t** out) {
     if (dev < 0 || dev >= kMaxDevices) return MLGI_EINVAL;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_static_keys_dev[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_keys);
-        if (e != cudaSuccess || !p) {
+        void *p = nullptr, *q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_keys);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_static_pyramid);
+        if (e != cudaSuccess || !p || !q) {
             cudaGetLastError();
             return MLGI_ECUDA;
         }
+        g_static_pyramid_dev[dev] = q;
         g_static_keys_dev[dev] = static_cast<uint32_t*>(p);
     }
-    *out = g_static_keys_dev[dev];
+    *keys = g_static_keys_dev[dev];
+    *pyramid = g_static_pyramid_dev[dev];
     return MLGI_OK;
 }
 
@@ -78,10 +88,14 @@ extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi
     if (!vpls->packed || (reinterpret_cast<uintptr_t>(vpls->packed) & 15) ||
         (reinterpret_cast<uintptr_t>(pts->points) & 15))
         return MLGI_EINVAL;
-    if (mlgi::pullpush_smem_bytes(p->ism_size, p->levels) > 227 * 1024) return MLGI_EINVAL;
+    if (mlgi::pullmid_smem_bytes(p->ism_size, p->levels) > 227 * 1024) return MLGI_EINVAL;
+    size_t lv2_off = 0;
+    if (mlgi::pullpush_scratch_bytes((int)aw, (int)ah, p->levels, &lv2_off) > kStaticPyramidFloat4 * sizeof(float4))
+        return MLGI_EINVAL;
 
     uint32_t* keys = nullptr;
-    const mlgi_status st = static_keys_address(&keys);
+    void* pyramid = nullptr;
+    const mlgi_status st = static_addresses(&keys, &pyramid);
     if (st != MLGI_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
@@ -115,6 +129,10 @@ extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi
     q.grid_x = p->grid_x;
     q.grid_y = p->grid_y;
     q.z_far = p->z_far;
+    q.m_s0 = (uint32_t)((0x100000000ull + p->ism_size - 1) / p->ism_size);
+    q.m_s1 = p->ism_size >= 4 ? (uint32_t)((0x100000000ull + (p->ism_size >> 1) - 1) / (p->ism_size >> 1)) : 0;  // levels >= 2 only
+    q.lv1 = static_cast<float4*>(pyramid);
+    q.lv2 = p->levels >= 2 ? reinterpret_cast<float4*>(static_cast<char*>(pyramid) + lv2_off) : nullptr;
     if (mlgi::launch_pullpush(q, s) != cudaSuccess) return MLGI_ECUDA;
     return MLGI_OK;
 }

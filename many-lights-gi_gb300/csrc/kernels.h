@@ -43,6 +43,9 @@ struct PullPushArgs {
     int ism_size, levels;
     int grid_x, grid_y;
     float z_far;
+    float4* lv1;          // scratch: pyramid level 1, (atlas_w/2) x (atlas_h/2)
+    float4* lv2;          // scratch: pyramid level 2, (atlas_w/4) x (atlas_h/4), when levels >= 2
+    uint32_t m_s0, m_s1;  // ceil(2^32 / d) for d = ism_size and ism_size / 2 (exact small divisions)
 };
 
 struct FgArgs {
@@ -85,7 +88,7 @@ struct BatchView {
     int fg_mode;  // 0: FP32 records/atlas/normals, 1: reduced (24-byte records, FP16 atlas and normals)
 };
 
-enum BatchPass { kBpClear = 0, kBpVpl, kBpSplat, kBpPullPush, kBpFg, kBpCount };
+enum BatchPass { kBpClear = 0, kBpVpl, kBpSplat, kBpPull1, kBpPullMid, kBpPush1, kBpPush0, kBpFg, kBpCount };
 
 struct BatchTable {
     const BatchView* views;  // device
@@ -107,7 +110,11 @@ cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s);
 cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s);
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s);
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s);
-size_t pullpush_smem_bytes(int ism_size, int levels);
+// Shared memory of the per-ISM middle pass (levels 2..L), and the lv1 + lv2 scratch in bytes
+// (lv2 starts at *lv2_offset).
+size_t pullmid_smem_bytes(int ism_size, int levels);
+size_t pullpush_scratch_bytes(int atlas_w, int atlas_h, int levels, size_t* lv2_offset);
+int pullpush_batch_items(int pass, int atlas_w, int atlas_h, int ism_count, int levels);
 cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s);
 
 }  // namespace mlgi

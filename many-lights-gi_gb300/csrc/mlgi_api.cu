@@ -38,6 +38,7 @@ struct mlgi_ctx {
     uint32_t* status = nullptr;           // device error word
     // frame-level buffers
     DevBuf vpl, packed, reduced, keys, depth;
+    DevBuf pp;  // pull-push pyramid levels 1 and 2
     // host-frame input copies
     DevBuf h_rsm_depth, h_rsm_normal, h_rsm_diffuse, h_points, h_counts, h_gdepth, h_gnormal, h_rgb;
     bool timing = false;
@@ -185,7 +186,7 @@ void mlgi_destroy(mlgi_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->shuffle_dev) cudaFree(kv.second);
-    for (DevBuf* b : {&ctx->vpl, &ctx->packed, &ctx->reduced, &ctx->keys, &ctx->depth, &ctx->h_rsm_depth,
+    for (DevBuf* b : {&ctx->vpl, &ctx->packed, &ctx->reduced, &ctx->keys, &ctx->depth, &ctx->pp, &ctx->h_rsm_depth,
                       &ctx->h_rsm_normal, &ctx->h_rsm_diffuse, &ctx->h_points, &ctx->h_counts, &ctx->h_gdepth,
                       &ctx->h_gnormal, &ctx->h_rgb})
         if (b->p) cudaFree(b->p);
@@ -209,6 +210,7 @@ mlgi_status mlgi_ctx_reserve(mlgi_ctx* ctx, int max_vpl, size_t max_atlas_texels
     if (st == MLGI_OK) st = ensure(ctx, ctx->reduced, (size_t)max_vpl * 24);
     if (st == MLGI_OK) st = ensure(ctx, ctx->keys, max_atlas_texels * 4);
     if (st == MLGI_OK) st = ensure(ctx, ctx->depth, max_atlas_texels * 4);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->pp, max_atlas_texels * 5 + 512);  // levels 1 and 2
     const int32_t* shuffle = nullptr;
     for (int n = 64; st == MLGI_OK && n <= max_vpl; n *= 2) st = get_shuffle(ctx, n, &shuffle);
     return st;
@@ -293,16 +295,16 @@ mlgi_status build_splat_args(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_v
     return MLGI_OK;
 }
 
-mlgi_status build_pullpush_args(mlgi_ctx* ctx, const mlgi_atlas* atlas, const mlgi_ism_params* p,
+// `scratch` holds pullpush_scratch_bytes() bytes (device, 256-byte aligned).
+mlgi_status build_pullpush_args(mlgi_ctx* ctx, const mlgi_atlas* atlas, const mlgi_ism_params* p, void* scratch,
                                 mlgi::PullPushArgs& a) {
     mlgi_status st = check_ism(ctx, p);
     if (st != MLGI_OK) return st;
     if ((st = check_atlas(ctx, atlas, p)) != MLGI_OK) return st;
-    if (!atlas->keys || !atlas->depth) return fail(ctx, MLGI_EINVAL, "atlas buffers are NULL");
-    if (mlgi::pullpush_smem_bytes(p->ism_size, p->levels) > 227 * 1024)
+    if (!atlas->keys || !atlas->depth || !scratch) return fail(ctx, MLGI_EINVAL, "atlas buffers are NULL");
+    if (mlgi::pullmid_smem_bytes(p->ism_size, p->levels) > 227 * 1024)
         return fail(ctx, MLGI_EINVAL, "a %d-texel ISM pyramid exceeds shared memory", p->ism_size);
-    if ((p->ism_size & 3) == 0 && !aligned16(atlas->keys))
-        return fail(ctx, MLGI_EINVAL, "atlas keys must be 16-byte aligned");
+    if (!aligned16(atlas->keys)) return fail(ctx, MLGI_EINVAL, "atlas keys must be 16-byte aligned");
     a = mlgi::PullPushArgs{};
     a.keys = atlas->keys;
     a.out = atlas->depth;
@@ -314,6 +316,12 @@ mlgi_status build_pullpush_args(mlgi_ctx* ctx, const mlgi_atlas* atlas, const ml
     a.grid_x = p->grid_x;
     a.grid_y = p->grid_y;
     a.z_far = p->z_far;
+    size_t lv2_off = 0;
+    mlgi::pullpush_scratch_bytes(atlas->width, atlas->height, p->levels, &lv2_off);
+    a.m_s0 = (uint32_t)((0x100000000ull + p->ism_size - 1) / p->ism_size);
+    a.m_s1 = p->ism_size >= 4 ? (uint32_t)((0x100000000ull + (p->ism_size >> 1) - 1) / (p->ism_size >> 1)) : 0;  // levels >= 2 only
+    a.lv1 = static_cast<float4*>(scratch);
+    a.lv2 = p->levels >= 2 ? reinterpret_cast<float4*>(static_cast<char*>(scratch) + lv2_off) : nullptr;
     return MLGI_OK;
 }
 
@@ -405,9 +413,12 @@ mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl
 
 mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* p, mlgi_stream stream) {
     if (!ctx) return MLGI_EINVAL;
-    mlgi::PullPushArgs a;
-    const mlgi_status st = build_pullpush_args(ctx, atlas, p, a);
+    if (!atlas || !p) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    mlgi_status st =
+        ensure(ctx, ctx->pp, std::max<size_t>(16, mlgi::pullpush_scratch_bytes(atlas->width, atlas->height, p->levels, nullptr)));
     if (st != MLGI_OK) return st;
+    mlgi::PullPushArgs a;
+    if ((st = build_pullpush_args(ctx, atlas, p, ctx->pp.p, a)) != MLGI_OK) return st;
     MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream)));
     return MLGI_OK;
 }
@@ -580,8 +591,10 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 size_t view_arena_bytes(const mlgi_frame_desc& f) {
     const size_t n = (size_t)f.vpl.count, texels = (size_t)f.ism.grid_x * f.ism.ism_size * f.ism.grid_y * f.ism.ism_size;
+    const int aw = f.ism.grid_x * f.ism.ism_size, ah = f.ism.grid_y * f.ism.ism_size;
     return align256(n * 48) + align256(n * 16) + align256(n * 24) + align256(texels * 4) +
-           align256(texels * (f.atlas_format == MLGI_F16 ? 2 : 4));
+           align256(texels * (f.atlas_format == MLGI_F16 ? 2 : 4)) +
+           align256(mlgi::pullpush_scratch_bytes(aw, ah, f.ism.levels, nullptr));
 }
 
 // Fill one view-table entry; intermediates live at `base` in the batch arena.
@@ -595,7 +608,8 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     float* packed = reinterpret_cast<float*>(p); p += align256(n * 16);
     void* reduced = p; p += align256(n * 24);
     uint32_t* keys = reinterpret_cast<uint32_t*>(p); p += align256(texels * 4);
-    void* depth = p;
+    void* depth = p; p += align256(texels * (f.atlas_format == MLGI_F16 ? 2 : 4));
+    void* pp_scratch = p;
     const bool red = f.fg.vpl_format == MLGI_F16;
     if (red != (f.atlas_format == MLGI_F16) || red != (f.gbuffer.normal_format == MLGI_F16))
         return fail(ctx, MLGI_EINVAL, "a batched view must be all FP32 or all reduced precision");
@@ -604,12 +618,12 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     v = mlgi::BatchView{};
     mlgi_status st = build_vpl_args(ctx, &f.rsm, &f.vpl, &vb, v.vpl);
     if (st == MLGI_OK) st = build_splat_args(ctx, &f.points, &vb, (int)n, &f.ism, &atlas, v.splat);
-    if (st == MLGI_OK) st = build_pullpush_args(ctx, &atlas, &f.ism, v.pp);
+    if (st == MLGI_OK) st = build_pullpush_args(ctx, &atlas, &f.ism, pp_scratch, v.pp);
     mlgi_fg_params fp = f.fg;
     fp.tile = 16;
     if (st == MLGI_OK) st = build_fg_args(ctx, &f.gbuffer, &vb, &atlas, &fp, &out, v.fg);
     if (st != MLGI_OK) return st;
-    if (mlgi::pullpush_smem_bytes(f.ism.ism_size, f.ism.levels) > 200 * 1024)
+    if (mlgi::pullmid_smem_bytes(f.ism.ism_size, f.ism.levels) > 200 * 1024)
         return fail(ctx, MLGI_EINVAL, "ISM size %d too large for the batched pull-push", f.ism.ism_size);
     v.keys = keys;
     v.atlas_texels = texels;
@@ -620,7 +634,8 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     counts[mlgi::kBpClear] = (int)((texels + mlgi::kBatchClearTexels - 1) / mlgi::kBatchClearTexels);
     counts[mlgi::kBpVpl] = (int)((n + mlgi::kBatchVplPerItem - 1) / mlgi::kBatchVplPerItem);
     counts[mlgi::kBpSplat] = f.points.n_buckets;
-    counts[mlgi::kBpPullPush] = f.ism.grid_x * f.ism.grid_y;
+    for (int pass : {mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1, mlgi::kBpPush0})
+        counts[pass] = mlgi::pullpush_batch_items(pass, aw, ah, f.ism.grid_x * f.ism.grid_y, f.ism.levels);
     counts[mlgi::kBpFg] = v.fg_tiles_per_class * I * I;
     return MLGI_OK;
 }
@@ -677,13 +692,13 @@ mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc*
                                           b->h_views[i], counts);
         if (st != MLGI_OK) return bail(st);
         for (int p = 0; p < mlgi::kBpCount; ++p) prefix[p * (n_views + 1) + i + 1] = prefix[p * (n_views + 1) + i] + counts[p];
-        b->pp_smem = std::max(b->pp_smem, mlgi::pullpush_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
+        b->pp_smem = std::max(b->pp_smem, mlgi::pullmid_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     for (int p = 0; p < mlgi::kBpCount; ++p) {
         const int items = prefix[p * (n_views + 1) + n_views];
-        const int per_sm = p == mlgi::kBpFg ? 4 : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullPush ? b->pp_smem : 0);
+        const int per_sm = p == mlgi::kBpFg ? 4 : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
         b->grid[p] = std::min(items, std::max(1, sms) * per_sm);
     }
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -697,8 +712,9 @@ mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc*
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(mlgi::BatchView) * n_views, cudaMemcpyHostToDevice,
                             b->stream);
-    for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPullPush})
-        if (e == cudaSuccess) e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullPush ? b->pp_smem : 0, b->stream);
+    for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1,
+                  mlgi::kBpPush0})
+        if (e == cudaSuccess) e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullMid ? b->pp_smem : 0, b->stream);
     if (e == cudaSuccess) e = mlgi::launch_batch_fg(t, b->grid[mlgi::kBpFg], b->stream);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
