@@ -98,6 +98,7 @@ constexpr int kSplatThreads = 256;
 
 struct SplatSmem {
     float4 pos[16], n[16];  // xyz used; float4 for 16-byte shared loads
+    float4 tasks[kSplatThreads / 32][128];  // per warp: (point xyz, VPL slot << 8 | radius byte)
     v3 s[16], u[16];
     float tx[16], ty[16];   // the VPL's ISM tile offsets, float(x) and float(y) (ism_utils.glsl:35-37)
 };
@@ -140,33 +141,58 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, S
     const float4* bucket = a.points + (int64_t)wg * a.bucket_stride;
     const float fw = float(a.atlas_w), fh = float(a.atlas_h), fgx = float(a.gx), fgy = float(a.gy);
     const float rgx = pow2_recip(a.gx), rgy = pow2_recip(a.gy);
-    for (uint32_t j = threadIdx.x; j < cnt; j += kSplatThreads) {
-        const float4 pt = __ldg(bucket + j);
-        const v3 position = mk(pt.x, pt.y, pt.z);
-        const uint32_t nr = __float_as_uint(pt.w);
-        const v3 pn = mk(float(nr & 0xFFu) / 255.0f * 2.0f - 1.0f, float((nr >> 8) & 0xFFu) / 255.0f * 2.0f - 1.0f,
-                         float((nr >> 16) & 0xFFu) / 255.0f * 2.0f - 1.0f);
-        const float pointRadius = float(nr >> 24) / 255.0f * 25.0f;
-        const uint32_t rbyte = f2u(pointRadius * 10.0f / 2.0f);  // / sqrt(maxVplCollectCount)
-        // gather up to 4 VPLs that pass the two-sided cull (ism.comp:93-107), as 4-bit indices
-        uint32_t used = 0;
+    const int lane = threadIdx.x & 31;
+    float4* tasks = S.tasks[threadIdx.x >> 5];
+    // Each warp takes 32 points at a time; a point's projections into its <= 4 VPLs become tasks
+    // that the whole warp then runs, so lanes do not idle on points with fewer VPLs.
+    for (uint32_t base = threadIdx.x - lane; base < cnt; base += kSplatThreads) {
+        const uint32_t j = base + lane;
+        float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
         int found = 0;
+        uint32_t used = 0;
+        if (j < cnt) {
+            pt = __ldg(bucket + j);
+            const v3 position = mk(pt.x, pt.y, pt.z);
+            const uint32_t nr = __float_as_uint(pt.w);
+            const v3 pn = mk(float(nr & 0xFFu) / 255.0f * 2.0f - 1.0f, float((nr >> 8) & 0xFFu) / 255.0f * 2.0f - 1.0f,
+                             float((nr >> 16) & 0xFFu) / 255.0f * 2.0f - 1.0f);
+            // gather up to 4 VPLs that pass the two-sided cull (ism.comp:93-107), as 4-bit indices
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            if (found == 4) break;  // later VPLs are not used (ism.comp:103-106)
-            const float4 vp = S.pos[i], vn = S.n[i];
-            const v3 rel = position - mk(vp.x, vp.y, vp.z);
-            const bool cull = dot(mk(vn.x, vn.y, vn.z), rel) < 0.0f || dot(pn, -rel) < 0.0f;
-            if (!cull) {
-                used |= (uint32_t)i << (4 * found);
-                ++found;
+            for (int i = 0; i < 16; ++i) {
+                if (found == 4) break;  // later VPLs are not used (ism.comp:103-106)
+                const float4 vp = S.pos[i], vn = S.n[i];
+                const v3 rel = position - mk(vp.x, vp.y, vp.z);
+                const bool cull = dot(mk(vn.x, vn.y, vn.z), rel) < 0.0f || dot(pn, -rel) < 0.0f;
+                if (!cull) {
+                    used |= (uint32_t)i << (4 * found);
+                    ++found;
+                }
             }
         }
-        // for each found VPL, project and atomicMin (ism.comp:112-137)
-        for (int k = 0; k < found; ++k) {
-            const int i = (used >> (4 * k)) & 15;
+        // exclusive prefix of `found` over the warp
+        int pre = found;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, pre, o);
+            if (lane >= o) pre += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, pre, 31);
+        pre -= found;
+        if (found > 0) {
+            const float pointRadius = float(__float_as_uint(pt.w) >> 24) / 255.0f * 25.0f;
+            const uint32_t rbyte = f2u(pointRadius * 10.0f / 2.0f);  // / sqrt(maxVplCollectCount)
+            for (int k = 0; k < found; ++k)
+                tasks[pre + k] = make_float4(pt.x, pt.y, pt.z, __uint_as_float((((used >> (4 * k)) & 15u) << 8) | rbyte));
+        }
+        __syncwarp();
+        // for each task, project and atomicMin (ism.comp:112-137)
+        for (int t = lane; t < total; t += 32) {
+            const float4 task = tasks[t];
+            const uint32_t tw = __float_as_uint(task.w);
+            const int i = (int)(tw >> 8);
+            const uint32_t rbyte = tw & 0xFFu;
             const float4 vp = S.pos[i], vn = S.n[i];
-            const v3 rel = position - mk(vp.x, vp.y, vp.z);
+            const v3 rel = mk(task.x, task.y, task.z) - mk(vp.x, vp.y, vp.z);
             // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
             const float dist = length(rel);
             const v3 n = mk(vn.x, vn.y, vn.z);
@@ -196,6 +222,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, S
             if (px < 0 || py < 0 || px >= a.atlas_w || py >= a.atlas_h) continue;  // image op out of range: no-op
             atomicMin(a.keys + (size_t)py * a.atlas_w + px, key);
         }
+        __syncwarp();  // the warp's tasks are consumed before the next points overwrite them
     }
 }
 
