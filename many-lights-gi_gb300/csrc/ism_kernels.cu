@@ -461,21 +461,109 @@ __device__ __forceinline__ float4 push_texel(const float4 (&coarse)[4], const bo
     return r;
 }
 
-// The coarse texels of level-l texel (px, py): level l+1 is `c` (row pitch pc) and this ISM covers
-// [c0x, c0x + sc) x [c0y, c0y + sc) of it. Indices fit 32 bits: atlas sides are below 65536.
-__device__ __forceinline__ void push_gather(const float4* c, const uint32_t pc, const int px, const int py,
-                                            const int c0x, const int c0y, const int sc, float4 (&coarse)[4],
-                                            bool (&inside)[4]) {
-    const int gidx = (px + 1) >> 1, gidy = (py + 1) >> 1;
+// Push levels 1 and 0 by 2x2 quads: the thread of quad gid = (gx, gy) of level l loads the four
+// coarse texels gid - 1 + kPushOff[k] of level l+1 once and derives their per-texel terms once,
+// then produces the quad's outputs (2 gx - 1 + qx, 2 gy - 1 + qy) -- those inside the atlas --
+// with the shader's per-output arithmetic. A quad straddles two ISMs in x exactly when gx is a
+// multiple of the ISM edge sc at level l+1 (then its left output is the last column of one ISM
+// and its right output the first of the next); coarse column gx - 1 + kx belongs to the ISM of
+// output qx unless the quad straddles and kx != qx. The same holds in y.
+struct PushCoarse {
+    float depth[4], maxDepth[4], radius[4], ax[4], ay[4], rs[4], hi[4], lo[4];
+    bool usable[4];
+};
+
+__device__ __forceinline__ void push_coarse(const float4* c, const int pc, const int cw, const int ch, const int gx,
+                                            const int gy, const float scale, PushCoarse& C) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int cx = gidx - 1 + kPushOff[k][0], cy = gidy - 1 + kPushOff[k][1];
-        inside[k] = cx >= c0x && cy >= c0y && cx < c0x + sc && cy < c0y + sc;
-        coarse[k] = inside[k] ? c[(uint32_t)cy * pc + (uint32_t)cx] : make_float4(0.f, 0.f, 0.f, 0.f);
+        // coordinates off the level are clamped: such texels are never inside an output's ISM
+        const int cx = min(max(gx - 1 + kPushOff[k][0], 0), cw - 1);
+        const int cy = min(max(gy - 1 + kPushOff[k][1], 0), ch - 1);
+        const float4 t = c[(uint32_t)cy * (uint32_t)pc + (uint32_t)cx];
+        const float2 d = unpack_half2(__float_as_uint(t.w));
+        C.depth[k] = t.x;
+        C.maxDepth[k] = t.y;
+        C.radius[k] = t.z;
+        C.usable[k] = t.x != 1.0f;  // weight 0 for invalid depth (push.comp:88-93)
+        C.ax[k] = d.x * 2.0f;
+        C.ay[k] = d.y * 2.0f;
+        const float r = t.z * scale;
+        const float p = r * r;
+        const bool fast = r > 0.f && p >= 1e-30f;  // the thresholds of sqrt_gt; NaN sends to sqrtf
+        C.rs[k] = r;
+        C.hi[k] = fast ? p * 1.00000095367431640625f : __int_as_float(0x7fc00000);
+        C.lo[k] = fast ? p * 0.99999904632568359375f : __int_as_float(0x7fc00000);
     }
 }
 
-// Per-texel passes on a kPpTileW x kPpTileH tile (tx, ty) of their level.
+// Output (qx, qy) of the quad (push.comp:95-161); `orig` is its pull value.
+template <bool kFull, int qx, int qy>
+__device__ __forceinline__ float4 push_output(const PushCoarse& C, const bool bx, const bool by, const float4 orig) {
+    float dvx[4], dvy[4];
+    int w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int kx = kPushOff[k][0], ky = kPushOff[k][1];
+        const bool inside = (kx == qx || !bx) && (ky == qy || !by);  // weight 0 across the border (push.comp:77-86)
+        w[k] = inside && C.usable[k] ? (kx == qx ? 3 : 1) * (ky == qy ? 3 : 1) : 0;
+        // (ctx - (px + 0.5)) is exactly 2 kx - qx - 0.5 (see push_texel)
+        dvx[k] = (float(2 * kx - qx) - 0.5f) + C.ax[k];
+        dvy[k] = (float(2 * ky - qy) - 0.5f) + C.ay[k];
+        if (w[k] != 0) {
+            const float d2 = dvx[k] * dvx[k] + dvy[k] * dvy[k];
+            const bool gt = d2 > C.hi[k] || (!(d2 < C.lo[k]) && sqrt_gt_band(d2, C.rs[k]));
+            if (gt) w[k] = 0;
+        }
+    }
+    float minimum = 9001.0f, maxDepth = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (w[k] == 0) continue;
+        minimum = gmin(C.depth[k], minimum);
+        if (minimum == C.depth[k]) maxDepth = C.maxDepth[k];
+    }
+    int weightAcc = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (C.depth[k] > maxDepth) w[k] = 0;
+        weightAcc += w[k];
+    }
+    const bool invalid = orig.x == 1.0f;
+    bool occluded = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) occluded = occluded || (w[k] > 0 && orig.x > C.maxDepth[k]);
+    float4 r = orig;
+    if (!(weightAcc <= 0 || (!invalid && !occluded))) {
+        float depthAcc = 0.f, maxDepthAcc = 0.f, radiusAcc = 0.f, dax = 0.f, day = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (w[k] == 0) continue;
+            const float wf = float(w[k]);
+            depthAcc = depthAcc + C.depth[k] * wf;
+            if (kFull) {
+                maxDepthAcc = maxDepthAcc + C.maxDepth[k] * wf;
+                radiusAcc = radiusAcc + C.radius[k] * wf;
+                dax = dax + dvx[k] * wf;
+                day = day + dvy[k] * wf;
+            }
+        }
+        r.x = div_count(depthAcc, weightAcc);
+        if (kFull) {
+            r.y = div_count(maxDepthAcc, weightAcc);
+            r.z = div_count(radiusAcc, weightAcc);
+            r.w = __uint_as_float(pack_half2(div_count(dax, weightAcc), div_count(day, weightAcc)));
+        }
+    }
+    return r;
+}
+
+// x is a multiple of d (d >= 1, x < 2^16; m = ceil(2^32 / d) when d >= 2)
+__device__ __forceinline__ bool multiple_of(const int x, const int d, const uint32_t m) {
+    return d == 1 || x == div_small(x, m) * d;
+}
+
+// Per-texel pass on a kPpTileW x kPpTileH tile (tx, ty) of level 1.
 __device__ __forceinline__ void pull1_tile(const PullPushArgs& a, const int tx, const int ty, const float* s_rad,
                                            const float* s_mdo) {
     const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = ty * kPpTileH + (threadIdx.x / kPpTileW);
@@ -483,32 +571,59 @@ __device__ __forceinline__ void pull1_tile(const PullPushArgs& a, const int tx, 
     if (x < w1 && y < h1) a.lv1[(uint32_t)y * w1 + x] = pull1_texel(a, s_rad, s_mdo, x, y);
 }
 
-__device__ __forceinline__ void push1_tile(const PullPushArgs& a, const int tx, const int ty) {
-    const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = ty * kPpTileH + (threadIdx.x / kPpTileW);
-    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
-    if (x >= w1 || y >= h1) return;
+// Quad passes on a kPpTileW x kPpTileH tile (tx, ty) of quads: level l has (w_l / 2 + 1) x
+// (h_l / 2 + 1) quads.
+__device__ __forceinline__ void push1_quads(const PullPushArgs& a, const int tx, const int ty) {
+    const int gx = tx * kPpTileW + (threadIdx.x % kPpTileW), gy = ty * kPpTileH + (threadIdx.x / kPpTileW);
+    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1, w2 = a.atlas_w >> 2, h2 = a.atlas_h >> 2;
+    if (gx > w2 || gy > h2) return;
     const int sc = a.ism_size >> 2;  // ISM edge at level 2
-    float4 coarse[4];
-    bool inside[4];
-    push_gather(a.lv2, a.atlas_w >> 2, x, y, div_small(x, a.m_s1) * sc, div_small(y, a.m_s1) * sc, sc, coarse, inside);
-    float4* t = a.lv1 + (uint32_t)y * w1 + x;
-    *t = push_texel<true>(coarse, inside, (x + 1) & 1, (y + 1) & 1, *t, 0.5f);
+    PushCoarse C;
+    push_coarse(a.lv2, w2, w2, h2, gx, gy, 0.5f, C);
+    const bool bx = multiple_of(gx, sc, a.m_c1), by = multiple_of(gy, sc, a.m_c1);
+    const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
+    const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w1, oky0 = y0 >= 0, oky1 = y0 + 1 < h1;
+    float4* row0 = a.lv1 + (uint32_t)max(y0, 0) * w1;  // only used when oky0
+    float4* row1 = a.lv1 + (uint32_t)min(y0 + 1, h1 - 1) * w1;  // only used when oky1
+    if (oky0 && okx0) row0[x0] = push_output<true, 0, 0>(C, bx, by, row0[x0]);
+    if (oky0 && okx1) row0[x0 + 1] = push_output<true, 1, 0>(C, bx, by, row0[x0 + 1]);
+    if (oky1 && okx0) row1[x0] = push_output<true, 0, 1>(C, bx, by, row1[x0]);
+    if (oky1 && okx1) row1[x0 + 1] = push_output<true, 1, 1>(C, bx, by, row1[x0 + 1]);
 }
 
-__device__ __forceinline__ void push0_tile(const PullPushArgs& a, const int tx, const int ty) {
-    const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = ty * kPpTileH + (threadIdx.x / kPpTileW);
-    if (x >= a.atlas_w || y >= a.atlas_h) return;
-    const int sc = a.ism_size >> 1;  // ISM edge at level 1
-    float4 coarse[4];
-    bool inside[4];
-    push_gather(a.lv1, a.atlas_w >> 1, x, y, div_small(x, a.m_s0) * sc, div_small(y, a.m_s0) * sc, sc, coarse, inside);
-    const uint32_t o = (uint32_t)y * a.atlas_w + x;
-    const float4 orig = make_float4(float(__ldg(a.keys + o) >> 8) / 16777216.0f, 0.f, 0.f, 0.f);
-    const float d = push_texel<false>(coarse, inside, (x + 1) & 1, (y + 1) & 1, orig, 1.0f).x;
+__device__ __forceinline__ void store_depth(const PullPushArgs& a, const uint32_t o, const float d) {
     if (a.out_f16)
         reinterpret_cast<__half*>(a.out)[o] = __float2half_rn(d);
     else
         reinterpret_cast<float*>(a.out)[o] = d;
+}
+
+__device__ __forceinline__ float key_depth(const PullPushArgs& a, const uint32_t o) {
+    return float(__ldg(a.keys + o) >> 8) / 16777216.0f;
+}
+
+__device__ __forceinline__ void push0_quads(const PullPushArgs& a, const int tx, const int ty) {
+    const int gx = tx * kPpTileW + (threadIdx.x % kPpTileW), gy = ty * kPpTileH + (threadIdx.x / kPpTileW);
+    const int w = a.atlas_w, h = a.atlas_h, w1 = w >> 1, h1 = h >> 1;
+    if (gx > w1 || gy > h1) return;
+    const int sc = a.ism_size >> 1;  // ISM edge at level 1
+    PushCoarse C;
+    push_coarse(a.lv1, w1, w1, h1, gx, gy, 1.0f, C);
+    const bool bx = multiple_of(gx, sc, a.m_c0), by = multiple_of(gy, sc, a.m_c0);
+    const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
+    const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w, oky0 = y0 >= 0, oky1 = y0 + 1 < h;
+    const uint32_t r0 = (uint32_t)y0 * w, r1 = (uint32_t)(y0 + 1) * w;
+    // level 0 writes only the depth channel (push.comp:33-37)
+    if (oky0 && okx0)
+        store_depth(a, r0 + x0, push_output<false, 0, 0>(C, bx, by, make_float4(key_depth(a, r0 + x0), 0.f, 0.f, 0.f)).x);
+    if (oky0 && okx1)
+        store_depth(a, r0 + x0 + 1,
+                    push_output<false, 1, 0>(C, bx, by, make_float4(key_depth(a, r0 + x0 + 1), 0.f, 0.f, 0.f)).x);
+    if (oky1 && okx0)
+        store_depth(a, r1 + x0, push_output<false, 0, 1>(C, bx, by, make_float4(key_depth(a, r1 + x0), 0.f, 0.f, 0.f)).x);
+    if (oky1 && okx1)
+        store_depth(a, r1 + x0 + 1,
+                    push_output<false, 1, 1>(C, bx, by, make_float4(key_depth(a, r1 + x0 + 1), 0.f, 0.f, 0.f)).x);
 }
 
 // Levels 2..L of one ISM in shared memory (tables first, then level 2, 3, ...): pull from lv1,
@@ -545,7 +660,7 @@ __device__ __forceinline__ void pullmid_ism(const PullPushArgs& a, const int ism
         const int sc = sl >> 1;
         for (int i = tid; i < sl * sl; i += nt) {
             const int px = ox0 + i % sl, py = oy0 + i / sl;
-            // the coarse texels, as push_gather but on the ISM-local level in shared memory
+            // the coarse texels of the texel's quad, on the ISM-local level in shared memory
             float4 coarse[4];
             bool inside[4];
             const int gidx = (px + 1) >> 1, gidy = (py + 1) >> 1;
@@ -578,11 +693,11 @@ __global__ void __launch_bounds__(kPullMidThreads) pullmid_kernel(PullPushArgs a
 }
 
 __global__ void __launch_bounds__(kPpTileW * kPpTileH) push1_kernel(PullPushArgs a) {
-    push1_tile(a, blockIdx.x, blockIdx.y);
+    push1_quads(a, blockIdx.x, blockIdx.y);
 }
 
 __global__ void __launch_bounds__(kPpTileW * kPpTileH) push0_kernel(PullPushArgs a) {
-    push0_tile(a, blockIdx.x, blockIdx.y);
+    push0_quads(a, blockIdx.x, blockIdx.y);
 }
 
 size_t pullmid_smem_bytes(int ism_size, int levels) {
@@ -605,16 +720,17 @@ __host__ __device__ __forceinline__ int row_items(int w) { return (tiles_x(w) + 
 
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s) {
     const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
-    const dim3 g1(tiles_x(w1), tiles_y(h1)), g0(tiles_x(a.atlas_w), tiles_y(a.atlas_h));
+    const dim3 g1(tiles_x(w1), tiles_y(h1));
+    const dim3 q1(tiles_x(w1 / 2 + 1), tiles_y(h1 / 2 + 1)), q0(tiles_x(w1 + 1), tiles_y(h1 + 1));
     pull1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
     if (a.levels >= 2) {
         const size_t smem = pullmid_smem_bytes(a.ism_size, a.levels);
         cudaError_t e = cudaFuncSetAttribute(pullmid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         pullmid_kernel<<<a.grid_x * a.grid_y, kPullMidThreads, smem, s>>>(a);
-        push1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
+        push1_kernel<<<q1, kPpTileW * kPpTileH, 0, s>>>(a);
     }
-    push0_kernel<<<g0, kPpTileW * kPpTileH, 0, s>>>(a);
+    push0_kernel<<<q0, kPpTileW * kPpTileH, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -717,9 +833,9 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push1_kernel(BatchT
     for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
         const int v = find_view(pre, t.n_views, item);
         stage_pp_args(t, v, cur, args);
-        const int w1 = args.atlas_w >> 1, per_row = row_items(w1), i = item - __ldg(pre + v);
+        const int qw = (args.atlas_w >> 2) + 1, per_row = row_items(qw), i = item - __ldg(pre + v);
         const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
-        for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(w1); ++tx) push1_tile(args, tx, ty);
+        for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(qw); ++tx) push1_quads(args, tx, ty);
     }
 }
 
@@ -730,9 +846,9 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push0_kernel(BatchT
     for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
         const int v = find_view(pre, t.n_views, item);
         stage_pp_args(t, v, cur, args);
-        const int w = args.atlas_w, per_row = row_items(w), i = item - __ldg(pre + v);
+        const int qw = (args.atlas_w >> 1) + 1, per_row = row_items(qw), i = item - __ldg(pre + v);
         const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
-        for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(w); ++tx) push0_tile(args, tx, ty);
+        for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(qw); ++tx) push0_quads(args, tx, ty);
     }
 }
 
@@ -741,8 +857,8 @@ int pullpush_batch_items(int pass, int atlas_w, int atlas_h, int ism_count, int 
     switch (pass) {
         case kBpPull1: return row_items(w1) * tiles_y(h1);
         case kBpPullMid: return levels >= 2 ? ism_count : 0;
-        case kBpPush1: return levels >= 2 ? row_items(w1) * tiles_y(h1) : 0;
-        case kBpPush0: return row_items(atlas_w) * tiles_y(atlas_h);
+        case kBpPush1: return levels >= 2 ? row_items(w1 / 2 + 1) * tiles_y(h1 / 2 + 1) : 0;
+        case kBpPush0: return row_items(w1 + 1) * tiles_y(h1 + 1);
         default: return 0;
     }
 }

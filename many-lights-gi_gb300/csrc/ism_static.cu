@@ -129,8 +129,8 @@ extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi
     q.grid_x = p->grid_x;
     q.grid_y = p->grid_y;
     q.z_far = p->z_far;
-    q.m_s0 = (uint32_t)((0x100000000ull + p->ism_size - 1) / p->ism_size);
-    q.m_s1 = p->ism_size >= 4 ? (uint32_t)((0x100000000ull + (p->ism_size >> 1) - 1) / (p->ism_size >> 1)) : 0;  // levels >= 2 only
+    q.m_c0 = mlgi::small_div_magic(p->ism_size >> 1);
+    q.m_c1 = mlgi::small_div_magic(p->ism_size >> 2);
     q.lv1 = static_cast<float4*>(pyramid);
     q.lv2 = p->levels >= 2 ? reinterpret_cast<float4*>(static_cast<char*>(pyramid) + lv2_off) : nullptr;
     if (mlgi::launch_pullpush(q, s) != cudaSuccess) return MLGI_ECUDA;

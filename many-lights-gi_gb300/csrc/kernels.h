@@ -35,6 +35,9 @@ struct SplatArgs {
     uint32_t* keys;
 };
 
+// ceil(2^32 / d) for 2 <= d < 2^16 (exact floor(n / d) for n < 2^16 by a high multiply), else 0.
+inline uint32_t small_div_magic(int d) { return d >= 2 ? (uint32_t)((0x100000000ull + d - 1) / d) : 0u; }
+
 struct PullPushArgs {
     const uint32_t* keys;
     void* out;            // final depth (FP32 or FP16)
@@ -45,7 +48,7 @@ struct PullPushArgs {
     float z_far;
     float4* lv1;          // scratch: pyramid level 1, (atlas_w/2) x (atlas_h/2)
     float4* lv2;          // scratch: pyramid level 2, (atlas_w/4) x (atlas_h/4), when levels >= 2
-    uint32_t m_s0, m_s1;  // ceil(2^32 / d) for d = ism_size and ism_size / 2 (exact small divisions)
+    uint32_t m_c0, m_c1;  // ceil(2^32 / d) for d = ism_size / 2 and ism_size / 4 when d >= 2, else 0
 };
 
 struct FgArgs {

@@ -318,8 +318,8 @@ mlgi_status build_pullpush_args(mlgi_ctx* ctx, const mlgi_atlas* atlas, const ml
     a.z_far = p->z_far;
     size_t lv2_off = 0;
     mlgi::pullpush_scratch_bytes(atlas->width, atlas->height, p->levels, &lv2_off);
-    a.m_s0 = (uint32_t)((0x100000000ull + p->ism_size - 1) / p->ism_size);
-    a.m_s1 = p->ism_size >= 4 ? (uint32_t)((0x100000000ull + (p->ism_size >> 1) - 1) / (p->ism_size >> 1)) : 0;  // levels >= 2 only
+    a.m_c0 = mlgi::small_div_magic(p->ism_size >> 1);
+    a.m_c1 = mlgi::small_div_magic(p->ism_size >> 2);
     a.lv1 = static_cast<float4*>(scratch);
     a.lv2 = p->levels >= 2 ? reinterpret_cast<float4*>(static_cast<char*>(scratch) + lv2_off) : nullptr;
     return MLGI_OK;
