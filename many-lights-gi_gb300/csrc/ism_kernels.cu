@@ -250,7 +250,7 @@ cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s) {
 // RGBA32F pyramid. Coordinates entering the displacement arithmetic are global coordinates of the
 // level, as in the level-by-level shaders.
 constexpr int kPpTileW = 32, kPpTileH = 8;  // texel tile of the per-texel kernels (256 threads)
-constexpr int kPullMidThreads = 256;
+constexpr int kPullMidThreads = 128;  // one wave of ISM blocks at the usual atlas sizes
 constexpr int kPpBatchTiles = 4;  // texel tiles per work item of the batched per-texel passes
 constexpr size_t kPullPushTableBytes = 2 * 256 * sizeof(float);  // key-byte tables, see below
 
