@@ -364,7 +364,8 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* frame, floa
 
 /* Per-pass device times (ms) of the last mlgi_gi_frame / mlgi_gi_frame_host call when timing is
  * enabled, named after the reference's PerfCounter passes:
- * [0] VPLP, [1] ISM clear, [2] ISM CS (splat), [3] pull-push, [4] FG, [5] H2D, [6] D2H.
+ * [0] VPLP, [1] ISM clear, [2] ISM CS (splat), [3] pull-push, [4] FG, [5] H2D, [6] D2H, then the
+ * pull-push pass's launches: [7] pull level 1, [8] middle levels, [9] push level 1, [10] push level 0.
  * Reading them synchronises the context's stream. */
 mlgi_status mlgi_set_timing(mlgi_ctx* ctx, int enabled);
 mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n);

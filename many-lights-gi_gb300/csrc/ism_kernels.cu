@@ -718,18 +718,23 @@ __host__ __device__ __forceinline__ int tiles_y(int h) { return (h + kPpTileH - 
 // Work items of the batched per-texel passes: runs of kPpBatchTiles tiles along a tile row.
 __host__ __device__ __forceinline__ int row_items(int w) { return (tiles_x(w) + kPpBatchTiles - 1) / kPpBatchTiles; }
 
-cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s) {
+cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks) {
     const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
     const dim3 g1(tiles_x(w1), tiles_y(h1));
     const dim3 q1(tiles_x(w1 / 2 + 1), tiles_y(h1 / 2 + 1)), q0(tiles_x(w1 + 1), tiles_y(h1 + 1));
     pull1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    if (marks) cudaEventRecord(marks[0], s);
     if (a.levels >= 2) {
         const size_t smem = pullmid_smem_bytes(a.ism_size, a.levels);
         cudaError_t e = cudaFuncSetAttribute(pullmid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         pullmid_kernel<<<a.grid_x * a.grid_y, kPullMidThreads, smem, s>>>(a);
+        if (marks) cudaEventRecord(marks[1], s);
         push1_kernel<<<q1, kPpTileW * kPpTileH, 0, s>>>(a);
+    } else if (marks) {
+        cudaEventRecord(marks[1], s);
     }
+    if (marks) cudaEventRecord(marks[2], s);
     push0_kernel<<<q0, kPpTileW * kPpTileH, 0, s>>>(a);
     return cudaGetLastError();
 }

@@ -112,7 +112,8 @@ constexpr uint32_t kStatusTmaTimeout = 1u;
 cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s);
 cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s);
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s);
-cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s);
+// marks (optional): three events recorded after level 1, the middle levels and push level 1.
+cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks = nullptr);
 // Shared memory of the per-ISM middle pass (levels 2..L), and the lv1 + lv2 scratch in bytes
 // (lv2 starts at *lv2_offset).
 size_t pullmid_smem_bytes(int ism_size, int levels);

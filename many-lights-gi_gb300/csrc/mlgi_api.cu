@@ -24,6 +24,8 @@ struct DevBuf {
 };
 
 enum Pass { kVplp = 0, kIsmClear, kIsmCs, kPullPush, kFg, kH2D, kD2H, kNumPasses };
+// the pull-push pass's launches, reported after the passes
+enum SubPass { kPull1 = kNumPasses, kPullMid, kPush1, kPush0, kNumTimings };
 // Event slots: ev[k]..ev[k+1] bracket device pass k (k <= kFg); two extra slots bracket the
 // host-frame copies.
 constexpr int kEvH2DStart = kNumPasses + 1, kEvD2HEnd = kNumPasses + 2, kNumEvents = kNumPasses + 3;
@@ -45,7 +47,8 @@ struct mlgi_ctx {
     bool timed_host_frame = false;  // the last timed call was mlgi_gi_frame_host
     bool timed_frame = false;
     cudaEvent_t ev[kNumEvents] = {};
-    float last_ms[kNumPasses] = {};
+    cudaEvent_t ev_pp[3] = {};  // inside the pull-push pass
+    float last_ms[kNumTimings] = {};
 };
 
 namespace {
@@ -172,6 +175,7 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->status, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(ctx->status, 0, sizeof(uint32_t));
     for (int i = 0; e == cudaSuccess && i < kNumEvents; ++i) e = cudaEventCreate(&ctx->ev[i]);
+    for (int i = 0; e == cudaSuccess && i < 3; ++i) e = cudaEventCreate(&ctx->ev_pp[i]);
     if (e != cudaSuccess) {
         cudaGetLastError();
         mlgi_destroy(ctx);
@@ -191,6 +195,8 @@ void mlgi_destroy(mlgi_ctx* ctx) {
                       &ctx->h_gnormal, &ctx->h_rgb})
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->ev_pp)
         if (e) cudaEventDestroy(e);
     if (ctx->status) cudaFree(ctx->status);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -419,7 +425,7 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
     if (st != MLGI_OK) return st;
     mlgi::PullPushArgs a;
     if ((st = build_pullpush_args(ctx, atlas, p, ctx->pp.p, a)) != MLGI_OK) return st;
-    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream)));
+    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream), ctx->timing ? ctx->ev_pp : nullptr));
     return MLGI_OK;
 }
 
@@ -457,17 +463,19 @@ mlgi_status mlgi_set_timing(mlgi_ctx* ctx, int enabled) {
 
 mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n) {
     if (!ctx || !ms) return MLGI_EINVAL;
-    for (int k = 0; k < kNumPasses; ++k) ctx->last_ms[k] = 0.f;
+    for (int k = 0; k < kNumTimings; ++k) ctx->last_ms[k] = 0.f;
     if (ctx->timed_frame) {
         MLGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[kFg + 1]));
         for (int k = kVplp; k <= kFg; ++k) cudaEventElapsedTime(&ctx->last_ms[k], ctx->ev[k], ctx->ev[k + 1]);
+        const cudaEvent_t pp[5] = {ctx->ev[kPullPush], ctx->ev_pp[0], ctx->ev_pp[1], ctx->ev_pp[2], ctx->ev[kPullPush + 1]};
+        for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&ctx->last_ms[kPull1 + k], pp[k], pp[k + 1]);
         if (ctx->timed_host_frame) {
             MLGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[kEvD2HEnd]));
             cudaEventElapsedTime(&ctx->last_ms[kH2D], ctx->ev[kEvH2DStart], ctx->ev[kVplp]);
             cudaEventElapsedTime(&ctx->last_ms[kD2H], ctx->ev[kFg + 1], ctx->ev[kEvD2HEnd]);
         }
     }
-    for (int i = 0; i < n && i < kNumPasses; ++i) ms[i] = ctx->last_ms[i];
+    for (int i = 0; i < n && i < kNumTimings; ++i) ms[i] = ctx->last_ms[i];
     return MLGI_OK;
 }
 

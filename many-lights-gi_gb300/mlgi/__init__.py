@@ -277,8 +277,10 @@ class Context:
         return self._chk(lib().mlgi_set_timing(self.h, int(on)))
 
     def last_timings(self) -> np.ndarray:
-        ms = np.zeros(7, np.float32)
-        self._chk(lib().mlgi_last_timings(self.h, ms.ctypes.data, 7))
+        """Per-pass ms of the last timed frame: VPLP, ISM clear, splat, pull-push, FG, H2D, D2H, then
+        pull level 1, middle levels, push level 1, push level 0."""
+        ms = np.zeros(11, np.float32)
+        self._chk(lib().mlgi_last_timings(self.h, ms.ctypes.data, 11))
         return ms
 
     def check_device_status(self, stream: int = 0):

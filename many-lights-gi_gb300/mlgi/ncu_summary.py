@@ -1,7 +1,10 @@
-"""Summarise an ncu report (or a launch-list CSV) into the short text kept in profiles/.
+"""Summarise an ncu report (or a launch-list CSV) into the short text kept beside the benchmark.
 
-    python profiles/summarize_ncu.py report.ncu-rep  > profiles/<kernel>_<workload>.md
-    python profiles/summarize_ncu.py launches.csv    > profiles/launches_<workload>.md
+    python -m mlgi.ncu_summary report.ncu-rep  > <kernel>_<workload>.md
+    python -m mlgi.ncu_summary launches.csv    > launches_<workload>.md
+
+A report summary ends each kernel with a `traffic[<kernel>] = <bytes>` line (DRAM read + write of
+one launch), which bench.py reads for the roofline's `traffic`.
 """
 import collections
 import csv
@@ -52,7 +55,8 @@ def report(path):
         wr *= scale.get(units[hdr.index("dram__bytes_write.sum")], 1)
         short = name.split("(")[0].split("::")[-1].split("<")[0].replace("void ", "").strip()
         passes = {"vpl_process_kernel": "vpl_process", "ism_clear_kernel": "ism_clear", "ism_splat_kernel": "ism_splat",
-                  "pullpush_kernel": "pullpush", "fg_kernel": "final_gather"}
+                  "pull1_kernel": "pull1", "pullmid_kernel": "pullmid", "push1_kernel": "push1",
+                  "push0_kernel": "push0", "fg_kernel": "final_gather"}
         print(f"traffic[{passes.get(short, short)}] = {rd + wr:.4e}  (DRAM read + write bytes of this launch)\n")
 
 
@@ -70,7 +74,7 @@ def launches(path):
         if d.get("Metric Name") != "gpu__time_duration.sum":
             continue
         v = float(d["Metric Value"].replace(",", ""))
-        v *= {"nsecond": 1e-3, "usecond": 1.0, "msecond": 1e3}.get(d["Metric Unit"], 1.0)
+        v *= {"nsecond": 1e-3, "ns": 1e-3, "usecond": 1.0, "us": 1.0, "msecond": 1e3, "ms": 1e3}[d["Metric Unit"]]
         a = agg.setdefault(d["Kernel Name"].split("(")[0], [0, 0.0])
         a[0] += 1
         a[1] += v
