@@ -408,6 +408,13 @@ def run_batch(args, rank, world, local_rank):
         torch.cuda.synchronize()
         plain_ms = ev[0].elapsed_time(ev[1]) / args.steps
     clocks = sampler.stop()
+    # per-kernel device time of the plain form, summed over the views (one untimed extra pass)
+    ctx.set_timing(True)
+    plain_kernels = np.zeros(11)
+    for f in frames:
+        ctx.gi_frame(f.frame_desc(), f.radiance(), ctx.stream())
+        plain_kernels += ctx.last_timings()
+    ctx.set_timing(False)
     ctx.check_device_status()
     if rank == 0:
         n = len(frames)
@@ -422,7 +429,8 @@ def run_batch(args, rank, world, local_rank):
                        "l2": "inputs larger than L2"},
             "frames_per_s": n / (batched_ms * 1e-3), "plain_ms_per_batch": plain_ms,
             "plain_frames_per_s": n / (plain_ms * 1e-3), "speedup_vs_plain": plain_ms / batched_ms,
-            "gpu_launches": 8 * args.steps, "autotune_s": t_tune, "clocks": clocks}), flush=True)
+            "plain_kernels_ms": {n: float(plain_kernels[i]) for n, i in KERNELS},
+            "gpu_launches": 9 * args.steps, "autotune_s": t_tune, "clocks": clocks}), flush=True)
     batch.close()
     ctx.close()
 

@@ -14,6 +14,7 @@
 // Accumulation order is ascending VPL index for every pixel, so results are deterministic.
 #include <cuda_runtime.h>
 
+#include "batch_items.cuh"
 #include "gi_device.cuh"
 #include "kernels.h"
 
@@ -308,6 +309,10 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
             // Two pairs per iteration so that both ISM texel loads are in flight together.
             const float* atlas32 = reinterpret_cast<const float*>(a.atlas);
             const __half* atlas16 = reinterpret_cast<const __half*>(a.atlas);
+            // per-pair parameters in registers (a may live in shared memory in the batched form)
+            const float clampv = a.clamp_value;
+            const bool shadow = a.shadowing != 0;
+            const int aw = a.atlas_w, ah = a.atlas_h;
             auto prepare = [&](int k, float& G, float& vz, size_t& t, float3& flux) -> bool {
                 const float4 A = S.a[k], B = S.b[k];
                 const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
@@ -319,10 +324,10 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
                 const float angle = fmaxf(0.f, a1) * fmaxf(0.f, a2);
                 if (!(angle > 0.f)) return false;
                 const float att = (inv * inv) * (inv * inv);
-                G = fminf(angle * att, a.clamp_value);
+                G = fminf(angle * att, clampv);
                 const float4 C = S.c[k];
                 flux = make_float3(A.w, B.w, C.w);
-                if (a.shadowing) {
+                if (shadow) {
                     const float4 D = S.d[k];
                     const float2 org = S.org[k];
                     // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false):
@@ -332,11 +337,11 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
                     const float py = (D.x * ndx + D.y * ndy + D.z * ndz) * rz;
                     int ix = __float2int_rd(fmaf(px, hs, org.x));
                     int iy = __float2int_rd(fmaf(py, hs, org.y));
-                    if (ix >= a.atlas_w) ix -= a.atlas_w;  // GL_REPEAT
-                    if (ix < 0) ix += a.atlas_w;
-                    if (iy >= a.atlas_h) iy -= a.atlas_h;
-                    if (iy < 0) iy += a.atlas_h;
-                    t = (size_t)iy * a.atlas_w + ix;
+                    if (ix >= aw) ix -= aw;  // GL_REPEAT
+                    if (ix < 0) ix += aw;
+                    if (iy >= ah) iy -= ah;
+                    if (iy < 0) iy += ah;
+                    t = (size_t)iy * aw + ix;
                     vz = (d2 * inv) * inv_zfar;
                 }
                 return true;
@@ -345,7 +350,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
                 return kAtlasF16 ? __half2float(__ldg(atlas16 + t)) : __ldg(atlas32 + t);
             };
             auto shade = [&](float G, float vz, float occ) -> float {
-                if (!a.shadowing) return G;
+                if (!shadow) return G;
                 const float sv0 = 1.0f - (vz - occ);
                 const float tt = __saturatef((sv0 - 0.98f) * 50.0f);  // smoothstep(0.98, 1, sv0)
                 return G * (tt * tt * (3.0f - 2.0f * tt));
@@ -358,8 +363,8 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
                 float3 f0, f1;
                 const bool ok0 = prepare(k0, G0, vz0, t0, f0);
                 const bool ok1 = prepare(k1, G1, vz1, t1, f1);
-                const float o0 = (ok0 && a.shadowing) ? occluder(t0) : 0.f;
-                const float o1 = (ok1 && a.shadowing) ? occluder(t1) : 0.f;
+                const float o0 = (ok0 && shadow) ? occluder(t0) : 0.f;
+                const float o1 = (ok1 && shadow) ? occluder(t1) : 0.f;
                 if (ok0) {
                     const float g = shade(G0, vz0, o0);
                     accx = fmaf(f0.x, g, accx);
@@ -432,37 +437,43 @@ cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s) {
 }
 
 // Persistent final gathering over a view table (16 x 16 tiles). Views are FP32 or fully reduced.
+// One pass per precision (FP32 views in pass kBpFg, reduced views in kBpFg16), so that each
+// kernel holds one variant of the tile body, as the single-view kernels do.
+template <bool kReduced>
 __global__ void __launch_bounds__(256, 4) batch_fg_kernel(BatchTable t) {
     __shared__ FgSmem<256> S;
-    __shared__ FgArgs args;  // the item's view arguments, staged once per item
-    __shared__ int mode, tpc;
+    __shared__ FgArgs args;  // the item's view arguments, staged when the block changes views
+    __shared__ int tpc;
     if (threadIdx.x == 0) mbar_init(&S.bar, 1);
     uint32_t parity = 0;
-    const int* pre = t.prefix + kBpFg * (t.n_views + 1);
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        int lo = 0, hi = t.n_views - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(pre + mid) <= item) lo = mid; else hi = mid - 1;
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + (kReduced ? kBpFg16 : kBpFg) * (t.n_views + 1), t.n_views, s_pre);
+    int cur = -1;
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int lo = w.view(item);
+        if (lo != cur) {  // lo is uniform over the block
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                args = t.views[lo].fg;
+                tpc = t.views[lo].fg_tiles_per_class;
+            }
+            __syncthreads();
+            cur = lo;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            args = t.views[lo].fg;
-            mode = t.views[lo].fg_mode;
-            tpc = t.views[lo].fg_tiles_per_class;
-        }
-        __syncthreads();
-        const int local = item - __ldg(pre + lo);
+        const int local = w.local(item);
         const int tile = local % tpc, cls = local / tpc;
-        const bool ok = mode ? fg_tile<16, true, true, true>(args, tile, cls, S, parity)
-                             : fg_tile<16, false, false, false>(args, tile, cls, S, parity);
-        if (!ok) return;  // block-uniform: the staging wait timed out (status word already set)
+        if (!fg_tile<16, kReduced, kReduced, kReduced>(args, tile, cls, S, parity))
+            return;  // block-uniform: the staging wait timed out (status word already set)
     }
 }
 
-cudaError_t launch_batch_fg(const BatchTable& t, int grid, cudaStream_t s) {
+cudaError_t launch_batch_fg(const BatchTable& t, int pass, int grid, cudaStream_t s) {
     if (grid <= 0) return cudaSuccess;
-    batch_fg_kernel<<<grid, 256, 0, s>>>(t);
+    if (pass == kBpFg16)
+        batch_fg_kernel<true><<<grid, 256, 0, s>>>(t);
+    else
+        batch_fg_kernel<false><<<grid, 256, 0, s>>>(t);
     return cudaGetLastError();
 }
 

@@ -8,6 +8,7 @@
 //                          ImperfectShadowmap::pullpush (ImperfectShadowmap.cpp:121-182)
 #include <cuda_runtime.h>
 
+#include "batch_items.cuh"
 #include "gi_device.cuh"
 #include "kernels.h"
 
@@ -111,7 +112,11 @@ __device__ __forceinline__ float pow2_recip(int x) {
 }
 
 // Bucket wg (one block of kSplatThreads threads).
-__device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, SplatSmem& S) {
+// Work item `item` of a splat: chunk item % chunks of bucket item / chunks, i.e. the bucket's
+// points [chunk * kSplatChunk, (chunk + 1) * kSplatChunk), the last chunk up to the bucket's count
+// (one block each).
+__device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item, SplatSmem& S) {
+    const int wg = item / a.chunks, chunk = item - wg * a.chunks;
     __syncthreads();  // the previous bucket's use of S is over
     const int vplCount = a.vpl_end - a.vpl_start;
     if (a.points_only_scaled && wg > vplCount) return;
@@ -137,7 +142,9 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, S
     }
     __syncthreads();
 
-    const uint32_t cnt = __ldg(a.counts + wg);
+    const uint32_t first = (uint32_t)chunk * kSplatChunk;
+    const uint32_t count = __ldg(a.counts + wg);  // the last chunk takes any points beyond the stride
+    const uint32_t cnt = chunk == a.chunks - 1 ? count : min(count, first + kSplatChunk);
     const float4* bucket = a.points + (int64_t)wg * a.bucket_stride;
     const float fw = float(a.atlas_w), fh = float(a.atlas_h), fgx = float(a.gx), fgy = float(a.gy);
     const float rgx = pow2_recip(a.gx), rgy = pow2_recip(a.gy);
@@ -145,7 +152,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int wg, S
     float4* tasks = S.tasks[threadIdx.x >> 5];
     // Each warp takes 32 points at a time; a point's projections into its <= 4 VPLs become tasks
     // that the whole warp then runs, so lanes do not idle on points with fewer VPLs.
-    for (uint32_t base = threadIdx.x - lane; base < cnt; base += kSplatThreads) {
+    for (uint32_t base = first + threadIdx.x - lane; base < cnt; base += kSplatThreads) {
         const uint32_t j = base + lane;
         float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
         int found = 0;
@@ -233,7 +240,7 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
 
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s) {
     if (a.n_groups <= 0) return cudaSuccess;
-    ism_splat_kernel<<<a.n_groups, kSplatThreads, 0, s>>>(a);
+    ism_splat_kernel<<<a.n_groups * a.chunks, kSplatThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -743,21 +750,14 @@ cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* 
 // Persistent forms over a view table: block b takes work items b, b + gridDim.x, ... of the pass;
 // an item is (view, index inside the view) found from the pass's running item counts. Each item
 // runs exactly the single-view body, so batched results equal single-frame results bit for bit.
-__device__ __forceinline__ int find_view(const int* prefix, int n_views, int item) {
-    int lo = 0, hi = n_views - 1;  // last view whose first item <= item
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(prefix + mid) <= item) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
 
 __global__ void __launch_bounds__(256) batch_clear_kernel(BatchTable t) {
-    const int* pre = t.prefix + kBpClear * (t.n_views + 1);
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        const int v = find_view(pre, t.n_views, item);
-        const BatchView& V = t.views[v];
-        const size_t first = (size_t)(item - __ldg(pre + v)) * kBatchClearTexels;
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + kBpClear * (t.n_views + 1), t.n_views, s_pre);
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const BatchView& V = t.views[w.view(item)];
+        const size_t first = (size_t)w.local(item) * kBatchClearTexels;
         uint32_t* keys = V.keys;
         const size_t n = V.atlas_texels;
         for (size_t i = first + threadIdx.x * 4; i < first + kBatchClearTexels && i < n; i += 256 * 4) {
@@ -770,23 +770,31 @@ __global__ void __launch_bounds__(256) batch_clear_kernel(BatchTable t) {
 }
 
 __global__ void __launch_bounds__(kBatchVplPerItem) batch_vpl_kernel(BatchTable t) {
-    const int* pre = t.prefix + kBpVpl * (t.n_views + 1);
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        const int v = find_view(pre, t.n_views, item);
-        vpl_one(t.views[v].vpl, (uint32_t)(item - __ldg(pre + v)) * kBatchVplPerItem + threadIdx.x);
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + kBpVpl * (t.n_views + 1), t.n_views, s_pre);
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int v = w.view(item);
+        vpl_one(t.views[v].vpl, (uint32_t)w.local(item) * kBatchVplPerItem + threadIdx.x);
     }
 }
 
 __global__ void __launch_bounds__(kSplatThreads) batch_splat_kernel(BatchTable t) {
     __shared__ SplatSmem S;
     __shared__ SplatArgs args;  // the item's view arguments, staged once per item
-    const int* pre = t.prefix + kBpSplat * (t.n_views + 1);
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        const int v = find_view(pre, t.n_views, item);
-        __syncthreads();
-        if (threadIdx.x == 0) args = t.views[v].splat;
-        __syncthreads();
-        splat_bucket(args, item - __ldg(pre + v), S);
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + kBpSplat * (t.n_views + 1), t.n_views, s_pre);
+    int cur = -1;
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int v = w.view(item);
+        if (v != cur) {  // v is uniform over the block
+            __syncthreads();
+            if (threadIdx.x == 0) args = t.views[v].splat;
+            __syncthreads();
+            cur = v;
+        }
+        splat_bucket(args, w.local(item), S);
     }
 }
 
@@ -805,15 +813,17 @@ __device__ __forceinline__ bool stage_pp_args(const BatchTable& t, const int v, 
 __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_pull1_kernel(BatchTable t) {
     __shared__ float s_tab[512];
     __shared__ PullPushArgs args;
-    const int* pre = t.prefix + kBpPull1 * (t.n_views + 1);
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + kBpPull1 * (t.n_views + 1), t.n_views, s_pre);
     int cur = -1;
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        const int v = find_view(pre, t.n_views, item);
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int v = w.view(item);
         if (stage_pp_args(t, v, cur, args)) {
             fill_key_tables(s_tab, s_tab + 256, args.z_far);
             __syncthreads();
         }
-        const int w1 = args.atlas_w >> 1, per_row = row_items(w1), i = item - __ldg(pre + v);
+        const int w1 = args.atlas_w >> 1, per_row = row_items(w1), i = w.local(item);
         const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
         for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(w1); ++tx) pull1_tile(args, tx, ty, s_tab, s_tab + 256);
     }
@@ -822,23 +832,27 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_pull1_kernel(BatchT
 __global__ void __launch_bounds__(kPullMidThreads) batch_pullmid_kernel(BatchTable t) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ PullPushArgs args;
-    const int* pre = t.prefix + kBpPullMid * (t.n_views + 1);
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + kBpPullMid * (t.n_views + 1), t.n_views, s_pre);
     int cur = -1;
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        const int v = find_view(pre, t.n_views, item);
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int v = w.view(item);
         stage_pp_args(t, v, cur, args);
-        pullmid_ism(args, item - __ldg(pre + v), smem);
+        pullmid_ism(args, w.local(item), smem);
     }
 }
 
 __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push1_kernel(BatchTable t) {
     __shared__ PullPushArgs args;
-    const int* pre = t.prefix + kBpPush1 * (t.n_views + 1);
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + kBpPush1 * (t.n_views + 1), t.n_views, s_pre);
     int cur = -1;
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        const int v = find_view(pre, t.n_views, item);
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int v = w.view(item);
         stage_pp_args(t, v, cur, args);
-        const int qw = (args.atlas_w >> 2) + 1, per_row = row_items(qw), i = item - __ldg(pre + v);
+        const int qw = (args.atlas_w >> 2) + 1, per_row = row_items(qw), i = w.local(item);
         const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
         for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(qw); ++tx) push1_quads(args, tx, ty);
     }
@@ -846,12 +860,14 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push1_kernel(BatchT
 
 __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push0_kernel(BatchTable t) {
     __shared__ PullPushArgs args;
-    const int* pre = t.prefix + kBpPush0 * (t.n_views + 1);
+    __shared__ int s_pre[kBatchPrefixCache + 1];
+    ItemWalk w;
+    w.init(t.prefix + kBpPush0 * (t.n_views + 1), t.n_views, s_pre);
     int cur = -1;
-    for (int item = blockIdx.x; item < __ldg(pre + t.n_views); item += gridDim.x) {
-        const int v = find_view(pre, t.n_views, item);
+    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int v = w.view(item);
         stage_pp_args(t, v, cur, args);
-        const int qw = (args.atlas_w >> 1) + 1, per_row = row_items(qw), i = item - __ldg(pre + v);
+        const int qw = (args.atlas_w >> 1) + 1, per_row = row_items(qw), i = w.local(item);
         const int ty = i / per_row, tx0 = (i - ty * per_row) * kPpBatchTiles;
         for (int tx = tx0; tx < tx0 + kPpBatchTiles && tx < tiles_x(qw); ++tx) push0_quads(args, tx, ty);
     }

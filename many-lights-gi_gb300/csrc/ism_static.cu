@@ -20,6 +20,7 @@
 //   * No cudaMalloc, cudaFree or allocating library call is made.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "kernels.h"
@@ -105,6 +106,7 @@ extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi
     a.counts = pts->counts;
     a.bucket_stride = pts->bucket_stride;
     a.n_groups = pts->n_buckets;
+    a.chunks = (int)std::max<int64_t>(1, (pts->bucket_stride + mlgi::kSplatChunk - 1) / mlgi::kSplatChunk);
     a.packed = reinterpret_cast<const float4*>(vpls->packed);
     a.n_vpl = n_vpl;
     a.vpl_start = p->vpl_start;

@@ -21,11 +21,14 @@ struct VplArgs {
     uint8_t* reduced;      // 24 bytes per VPL, or nullptr
 };
 
+constexpr int kSplatChunk = 1024;  // points of a bucket per splat work item
+
 struct SplatArgs {
     const float4* points;
     const uint32_t* counts;
     int64_t bucket_stride;
-    int n_groups;
+    int n_groups;          // buckets
+    int chunks;            // work items per bucket: ceil(bucket_stride / kSplatChunk), at least 1
     const float4* packed;  // packedVplBuffer
     int n_vpl;
     int vpl_start, vpl_end;
@@ -91,7 +94,7 @@ struct BatchView {
     int fg_mode;  // 0: FP32 records/atlas/normals, 1: reduced (24-byte records, FP16 atlas and normals)
 };
 
-enum BatchPass { kBpClear = 0, kBpVpl, kBpSplat, kBpPull1, kBpPullMid, kBpPush1, kBpPush0, kBpFg, kBpCount };
+enum BatchPass { kBpClear = 0, kBpVpl, kBpSplat, kBpPull1, kBpPullMid, kBpPush1, kBpPush0, kBpFg, kBpFg16, kBpCount };
 
 struct BatchTable {
     const BatchView* views;  // device
@@ -103,7 +106,7 @@ constexpr int kBatchClearTexels = 4096;  // atlas texels cleared per work item
 constexpr int kBatchVplPerItem = 256;
 
 cudaError_t launch_batch_ism(const BatchTable& t, int pass, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_batch_fg(const BatchTable& t, int grid, cudaStream_t s);
+cudaError_t launch_batch_fg(const BatchTable& t, int pass, int grid, cudaStream_t s);  // pass kBpFg or kBpFg16
 int batch_blocks_per_sm(int pass, size_t smem);
 
 // Error bits written to the device status word.

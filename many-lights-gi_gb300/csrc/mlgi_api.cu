@@ -286,6 +286,7 @@ mlgi_status build_splat_args(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_v
     a.counts = pts->counts;
     a.bucket_stride = pts->bucket_stride;
     a.n_groups = pts->n_buckets;
+    a.chunks = (int)std::max<int64_t>(1, (pts->bucket_stride + mlgi::kSplatChunk - 1) / mlgi::kSplatChunk);
     a.packed = reinterpret_cast<const float4*>(vpls->packed);
     a.n_vpl = n_vpl;
     a.vpl_start = p->vpl_start;
@@ -641,10 +642,11 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     v.fg_mode = red ? 1 : 0;
     counts[mlgi::kBpClear] = (int)((texels + mlgi::kBatchClearTexels - 1) / mlgi::kBatchClearTexels);
     counts[mlgi::kBpVpl] = (int)((n + mlgi::kBatchVplPerItem - 1) / mlgi::kBatchVplPerItem);
-    counts[mlgi::kBpSplat] = f.points.n_buckets;
+    counts[mlgi::kBpSplat] = f.points.n_buckets * v.splat.chunks;
     for (int pass : {mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1, mlgi::kBpPush0})
         counts[pass] = mlgi::pullpush_batch_items(pass, aw, ah, f.ism.grid_x * f.ism.grid_y, f.ism.levels);
-    counts[mlgi::kBpFg] = v.fg_tiles_per_class * I * I;
+    counts[mlgi::kBpFg] = red ? 0 : v.fg_tiles_per_class * I * I;
+    counts[mlgi::kBpFg16] = red ? v.fg_tiles_per_class * I * I : 0;
     return MLGI_OK;
 }
 
@@ -706,7 +708,9 @@ mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     for (int p = 0; p < mlgi::kBpCount; ++p) {
         const int items = prefix[p * (n_views + 1) + n_views];
-        const int per_sm = p == mlgi::kBpFg ? 4 : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
+        const int per_sm = p == mlgi::kBpFg || p == mlgi::kBpFg16
+                               ? 4
+                               : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
         b->grid[p] = std::min(items, std::max(1, sms) * per_sm);
     }
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -723,7 +727,8 @@ mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc*
     for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1,
                   mlgi::kBpPush0})
         if (e == cudaSuccess) e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullMid ? b->pp_smem : 0, b->stream);
-    if (e == cudaSuccess) e = mlgi::launch_batch_fg(t, b->grid[mlgi::kBpFg], b->stream);
+    for (int p : {mlgi::kBpFg, mlgi::kBpFg16})
+        if (e == cudaSuccess) e = mlgi::launch_batch_fg(t, p, b->grid[p], b->stream);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
     if (e == cudaSuccess) e = e2;
