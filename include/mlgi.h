@@ -224,6 +224,22 @@ mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_des
 mlgi_status mlgi_batch_launch(mlgi_batch* b, mlgi_stream stream);
 void mlgi_batch_destroy(mlgi_batch* b);
 
+/* Batch forms. PERSISTENT (mlgi_batch_create): one persistent launch per pass over all views.
+ * CONCURRENT: each view's own single-frame kernels, the views spread over `streams` CUDA streams
+ * (balanced by estimated cost) and joined in one graph, so that the kernels of different views
+ * overlap (filling each other's tail waves and launch gaps). Both give results bit-identical to
+ * mlgi_gi_frame on each view. */
+#define MLGI_BATCH_PERSISTENT 0
+#define MLGI_BATCH_CONCURRENT 1
+typedef struct {
+    int form;     /* MLGI_BATCH_PERSISTENT or MLGI_BATCH_CONCURRENT */
+    int streams;  /* CONCURRENT: streams the views are spread over (0 selects 4) */
+} mlgi_batch_opts;
+mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc* views,
+                                 const mlgi_radiance* outputs, const mlgi_batch_opts* opts, mlgi_batch** out);
+/* Kernels one mlgi_batch_launch runs. */
+int mlgi_batch_kernel_launches(const mlgi_batch* b);
+
 /* ---- autotuner ------------------------------------------------------------------------------ */
 
 /* Picks the interleave factor, ISM edge (with its pull-push levels and a power-of-two-wide ISM

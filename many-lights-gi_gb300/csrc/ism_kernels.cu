@@ -148,6 +148,10 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
     const float4* bucket = a.points + (int64_t)wg * a.bucket_stride;
     const float fw = float(a.atlas_w), fh = float(a.atlas_h), fgx = float(a.gx), fgy = float(a.gy);
     const float rgx = pow2_recip(a.gx), rgy = pow2_recip(a.gy);
+    // per-task parameters in registers (a may live in shared memory in the batched form)
+    const float z_far = a.z_far;
+    const int atlas_w = a.atlas_w, atlas_h = a.atlas_h;
+    uint32_t* const keys = a.keys;
     const int lane = threadIdx.x & 31;
     float4* tasks = S.tasks[threadIdx.x >> 5];
     // Each warp takes 32 points at a time; a point's projections into its <= 4 VPLs become tasks
@@ -213,7 +217,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             vz = 1.0f - vz;
             vx = vx / vz;
             vy = vy / vz;
-            vz = dist / a.z_far;
+            vz = dist / z_far;
             vz = vz * -signOfV;
             vx = (vx + 1.0f) / 2.0f;
             vy = (vy + 1.0f) / 2.0f;
@@ -226,8 +230,8 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             vz = vz * 16777216.0f;
             const uint32_t key = (f2u(vz) << 8) | rbyte;
             const int px = f2i(vx), py = f2i(vy);
-            if (px < 0 || py < 0 || px >= a.atlas_w || py >= a.atlas_h) continue;  // image op out of range: no-op
-            atomicMin(a.keys + (size_t)py * a.atlas_w + px, key);
+            if (px < 0 || py < 0 || px >= atlas_w || py >= atlas_h) continue;  // image op out of range: no-op
+            atomicMin(keys + (size_t)py * atlas_w + px, key);
         }
         __syncwarp();  // the warp's tasks are consumed before the next points overwrite them
     }
@@ -725,6 +729,23 @@ __host__ __device__ __forceinline__ int tiles_y(int h) { return (h + kPpTileH - 
 // Work items of the batched per-texel passes: runs of kPpBatchTiles tiles along a tile row.
 __host__ __device__ __forceinline__ int row_items(int w) { return (tiles_x(w) + kPpBatchTiles - 1) / kPpBatchTiles; }
 
+cudaError_t pullpush_prepare(size_t smem) {
+    return cudaFuncSetAttribute(pullmid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
+    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
+    const dim3 g1(tiles_x(w1), tiles_y(h1));
+    const dim3 q1(tiles_x(w1 / 2 + 1), tiles_y(h1 / 2 + 1)), q0(tiles_x(w1 + 1), tiles_y(h1 + 1));
+    pull1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    if (a.levels >= 2) {
+        pullmid_kernel<<<a.grid_x * a.grid_y, kPullMidThreads, pullmid_smem_bytes(a.ism_size, a.levels), s>>>(a);
+        push1_kernel<<<q1, kPpTileW * kPpTileH, 0, s>>>(a);
+    }
+    push0_kernel<<<q0, kPpTileW * kPpTileH, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks) {
     const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
     const dim3 g1(tiles_x(w1), tiles_y(h1));
@@ -748,6 +769,8 @@ cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* 
 
 // ---------------------------------------------------------------------------------------------
 // Persistent forms over a view table: block b takes work items b, b + gridDim.x, ... of the pass;
+// their register budgets (launch bounds) keep the occupancy of the single-view kernels, which the
+// loop state would otherwise lower;
 // an item is (view, index inside the view) found from the pass's running item counts. Each item
 // runs exactly the single-view body, so batched results equal single-frame results bit for bit.
 
@@ -779,7 +802,7 @@ __global__ void __launch_bounds__(kBatchVplPerItem) batch_vpl_kernel(BatchTable 
     }
 }
 
-__global__ void __launch_bounds__(kSplatThreads) batch_splat_kernel(BatchTable t) {
+__global__ void __launch_bounds__(kSplatThreads, 6) batch_splat_kernel(BatchTable t) {
     __shared__ SplatSmem S;
     __shared__ SplatArgs args;  // the item's view arguments, staged once per item
     __shared__ int s_pre[kBatchPrefixCache + 1];
@@ -810,7 +833,7 @@ __device__ __forceinline__ bool stage_pp_args(const BatchTable& t, const int v, 
     return true;
 }
 
-__global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_pull1_kernel(BatchTable t) {
+__global__ void __launch_bounds__(kPpTileW * kPpTileH, 6) batch_pull1_kernel(BatchTable t) {
     __shared__ float s_tab[512];
     __shared__ PullPushArgs args;
     __shared__ int s_pre[kBatchPrefixCache + 1];
@@ -829,7 +852,7 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_pull1_kernel(BatchT
     }
 }
 
-__global__ void __launch_bounds__(kPullMidThreads) batch_pullmid_kernel(BatchTable t) {
+__global__ void __launch_bounds__(kPullMidThreads, 8) batch_pullmid_kernel(BatchTable t) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ PullPushArgs args;
     __shared__ int s_pre[kBatchPrefixCache + 1];
@@ -843,7 +866,7 @@ __global__ void __launch_bounds__(kPullMidThreads) batch_pullmid_kernel(BatchTab
     }
 }
 
-__global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push1_kernel(BatchTable t) {
+__global__ void __launch_bounds__(kPpTileW * kPpTileH, 4) batch_push1_kernel(BatchTable t) {
     __shared__ PullPushArgs args;
     __shared__ int s_pre[kBatchPrefixCache + 1];
     ItemWalk w;
@@ -858,7 +881,7 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push1_kernel(BatchT
     }
 }
 
-__global__ void __launch_bounds__(kPpTileW * kPpTileH) batch_push0_kernel(BatchTable t) {
+__global__ void __launch_bounds__(kPpTileW * kPpTileH, 5) batch_push0_kernel(BatchTable t) {
     __shared__ PullPushArgs args;
     __shared__ int s_pre[kBatchPrefixCache + 1];
     ItemWalk w;

@@ -117,6 +117,10 @@ cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s);
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s);
 // marks (optional): three events recorded after level 1, the middle levels and push level 1.
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks = nullptr);
+// Raise the middle pass's dynamic shared-memory limit to `smem` outside any stream capture; then
+// launch_pullpush_captured issues the same launches as launch_pullpush without that attribute call.
+cudaError_t pullpush_prepare(size_t smem);
+cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s);
 // Shared memory of the per-ISM middle pass (levels 2..L), and the lv1 + lv2 scratch in bytes
 // (lv2 starts at *lv2_offset).
 size_t pullmid_smem_bytes(int ism_size, int levels);

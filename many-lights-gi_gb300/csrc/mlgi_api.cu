@@ -589,6 +589,10 @@ struct mlgi_batch {
     int* d_prefix = nullptr;
     int grid[mlgi::kBpCount] = {};
     size_t pp_smem = 0;
+    int form = MLGI_BATCH_PERSISTENT;
+    int launches = 0;                  // kernels per mlgi_batch_launch
+    std::vector<cudaStream_t> side;    // concurrent form: the views' streams (used during capture)
+    std::vector<cudaEvent_t> events;   // concurrent form: fork and join events of the capture
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -650,6 +654,75 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     return MLGI_OK;
 }
 
+// Capture the batch's graph from its view table: the table upload and one persistent launch per
+// pass, or (concurrent form) each view's kernels on its stream between a fork and a join.
+mlgi_status capture_batch(mlgi_batch* b) {
+    const int n_views = b->n, form = b->form;
+    const mlgi_frame_desc* views = b->frames.data();
+    const mlgi::BatchTable t{b->d_views, b->d_prefix, n_views};
+    b->launches = 0;
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (form == MLGI_BATCH_PERSISTENT) {
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(mlgi::BatchView) * n_views, cudaMemcpyHostToDevice,
+                                b->stream);
+        for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1,
+                      mlgi::kBpPush0})
+            if (e == cudaSuccess)
+                e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullMid ? b->pp_smem : 0, b->stream);
+        for (int p : {mlgi::kBpFg, mlgi::kBpFg16})
+            if (e == cudaSuccess) e = mlgi::launch_batch_fg(t, p, b->grid[p], b->stream);
+        b->launches = 9;
+    } else {
+        // views to streams, costliest first onto the least-loaded stream (estimated from the work
+        // measured per unit at 1080p: gathered pairs, splatted points, atlas texels)
+        const int k = (int)b->side.size();
+        std::vector<std::pair<double, int>> cost;
+        for (int i = 0; i < n_views; ++i) {
+            const mlgi_frame_desc& f = views[i];
+            const double pairs = (double)f.gbuffer.width * f.gbuffer.height * f.vpl.count /
+                                 ((double)f.fg.interleave * f.fg.interleave);
+            const double texels = (double)f.ism.grid_x * f.ism.ism_size * f.ism.grid_y * f.ism.ism_size;
+            const double points = (double)f.points.n_buckets * f.points.bucket_stride;
+            cost.push_back({pairs * 4.3e-9 + points * 4.1e-8 + texels * 1.9e-8, i});
+        }
+        std::sort(cost.begin(), cost.end(), std::greater<std::pair<double, int>>());
+        std::vector<double> load(k, 0.0);
+        std::vector<std::vector<int>> lane(k);
+        for (const auto& c : cost) {
+            const int j = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[j] += c.first;
+            lane[j].push_back(c.second);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(b->events[k], b->stream);  // fork
+        for (int j = 0; j < k && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(b->side[j], b->events[k], 0);
+        for (int j = 0; j < k; ++j) {
+            for (int i : lane[j]) {
+                const mlgi::BatchView& v = b->h_views[i];
+                cudaStream_t s = b->side[j];
+                if (e == cudaSuccess) e = mlgi::launch_vpl_process(v.vpl, s);
+                if (e == cudaSuccess) e = mlgi::launch_ism_clear(v.keys, v.atlas_texels, s);
+                if (e == cudaSuccess) e = mlgi::launch_ism_splat(v.splat, s);
+                if (e == cudaSuccess) e = mlgi::launch_pullpush_captured(v.pp, s);
+                if (e == cudaSuccess) e = mlgi::launch_final_gather(v.fg, s);
+                b->launches += 3 + (v.pp.levels >= 2 ? 4 : 2) + 1;
+            }
+            if (e == cudaSuccess) e = cudaEventRecord(b->events[j], b->side[j]);  // join
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->events[j], 0);
+        }
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    b->graph = g;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(b->ctx, e, "batch graph capture");
+    }
+    return MLGI_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -663,16 +736,27 @@ void mlgi_batch_destroy(mlgi_batch* b) {
     if (b->d_views) cudaFree(b->d_views);
     if (b->d_prefix) cudaFree(b->d_prefix);
     if (b->h_views) cudaFreeHost(b->h_views);
+    for (cudaEvent_t e : b->events) cudaEventDestroy(e);
+    for (cudaStream_t st : b->side) cudaStreamDestroy(st);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
 
 mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc* views, const mlgi_radiance* outputs,
                               mlgi_batch** out) {
+    return mlgi_batch_create_ex(ctx, n_views, views, outputs, nullptr, out);
+}
+
+mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc* views,
+                                 const mlgi_radiance* outputs, const mlgi_batch_opts* opts, mlgi_batch** out) {
     if (!ctx) return MLGI_EINVAL;
     if (!out || !views || !outputs || n_views <= 0) return fail(ctx, MLGI_EINVAL, "bad batch arguments");
+    const int form = opts ? opts->form : MLGI_BATCH_PERSISTENT;
+    if (form != MLGI_BATCH_PERSISTENT && form != MLGI_BATCH_CONCURRENT) return fail(ctx, MLGI_EINVAL, "bad batch form");
+    if (opts && (opts->streams < 0 || opts->streams > 64)) return fail(ctx, MLGI_EINVAL, "streams must be 0..64");
     *out = nullptr;
     mlgi_batch* b = new mlgi_batch();
+    b->form = form;
     b->ctx = ctx;
     b->n = n_views;
     b->frames.assign(views, views + n_views);
@@ -718,26 +802,20 @@ mlgi_status mlgi_batch_create(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc*
         cudaGetLastError();
         return bail(fail(ctx, MLGI_ECUDA, "batch set-up"));
     }
-    // capture: table upload, then one persistent launch per pass
-    const mlgi::BatchTable t{b->d_views, b->d_prefix, n_views};
-    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(mlgi::BatchView) * n_views, cudaMemcpyHostToDevice,
-                            b->stream);
-    for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1,
-                  mlgi::kBpPush0})
-        if (e == cudaSuccess) e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullMid ? b->pp_smem : 0, b->stream);
-    for (int p : {mlgi::kBpFg, mlgi::kBpFg16})
-        if (e == cudaSuccess) e = mlgi::launch_batch_fg(t, p, b->grid[p], b->stream);
-    cudaGraph_t g = nullptr;
-    const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
-    if (e == cudaSuccess) e = e2;
-    b->graph = g;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return bail(cuda_fail(ctx, e, "batch graph capture"));
+    cudaError_t e = cudaSuccess;
+    if (form == MLGI_BATCH_CONCURRENT) {
+        const int k = std::min(n_views, opts && opts->streams > 0 ? opts->streams : 4);
+        b->side.assign(k, nullptr);
+        b->events.assign(k + 1, nullptr);
+        for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking);
+        for (int i = 0; i <= k && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->events[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = mlgi::pullpush_prepare(b->pp_smem);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return bail(cuda_fail(ctx, e, "batch streams"));
+        }
     }
+    if (const mlgi_status st = capture_batch(b); st != MLGI_OK) return bail(st);
     *out = b;
     return MLGI_OK;
 }
@@ -758,8 +836,17 @@ mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_des
     if (st != MLGI_OK) return st;
     b->h_views[view] = v;
     b->frames[view] = *desc;
+    if (b->form == MLGI_BATCH_CONCURRENT) {  // its graph holds the kernel arguments: capture it again
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+        return capture_batch(b);
+    }
     return MLGI_OK;
 }
+
+int mlgi_batch_kernel_launches(const mlgi_batch* b) { return b ? b->launches : 0; }
 
 mlgi_status mlgi_batch_launch(mlgi_batch* b, mlgi_stream stream) {
     if (!b) return MLGI_EINVAL;

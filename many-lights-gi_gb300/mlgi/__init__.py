@@ -107,6 +107,13 @@ class SceneInfo(C.Structure):
                 ("bucket_stride", C.c_int64)]
 
 
+BATCH_PERSISTENT, BATCH_CONCURRENT = 0, 1
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("form", C.c_int), ("streams", C.c_int)]
+
+
 class ServerDesc(C.Structure):
     _fields_ = [("device", C.c_int), ("slots", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int),
                 ("rsm_size", C.c_int), ("hbm_budget", C.c_size_t)]
@@ -159,6 +166,8 @@ _SIGS = {
     "mlgi_batch_update_view": (C.c_int32, [_p, C.c_int, C.POINTER(FrameDesc), C.POINTER(Radiance)]),
     "mlgi_batch_launch": (C.c_int32, [_p, _p]),
     "mlgi_batch_destroy": (None, [_p]),
+    "mlgi_batch_create_ex": (C.c_int32, [_p, C.c_int, _p, _p, C.POINTER(BatchOpts), C.POINTER(C.c_void_p)]),
+    "mlgi_batch_kernel_launches": (C.c_int, [_p]),
     "mlgi_autotune": (C.c_int32, [_p, C.POINTER(AutotuneQuery), C.POINTER(AutotuneResult)]),
     "mlgi_ctx_reserve": (C.c_int32, [_p, C.c_int, C.c_size_t]),
     "mlgi_server_create": (C.c_int32, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),

@@ -157,19 +157,21 @@ def pinned_inputs(scene: Scene) -> dict:
 
 
 class Batch:
-    """mlgi_batch over DeviceFrames: one persistent launch per pass, replayed from a CUDA graph."""
+    """mlgi_batch over DeviceFrames, replayed from a CUDA graph: one persistent launch per pass
+    (form BATCH_PERSISTENT) or each view's kernels spread over `streams` streams (BATCH_CONCURRENT)."""
 
-    def __init__(self, ctx, frames):
+    def __init__(self, ctx, frames, form: int = 0, streams: int = 0):
         import ctypes as C
 
-        from . import FrameDesc, Radiance, lib
+        from . import BatchOpts, FrameDesc, Radiance, lib
 
         self.ctx, self.frames = ctx, list(frames)
         self.descs = (FrameDesc * len(self.frames))(*[f.frame_desc() for f in self.frames])
         self.outs = (Radiance * len(self.frames))(*[f.radiance() for f in self.frames])
         self.h = C.c_void_p()
-        ctx._chk(lib().mlgi_batch_create(ctx.h, len(self.frames), C.cast(self.descs, C.c_void_p),
-                                         C.cast(self.outs, C.c_void_p), C.byref(self.h)))
+        opts = BatchOpts(form, streams)
+        ctx._chk(lib().mlgi_batch_create_ex(ctx.h, len(self.frames), C.cast(self.descs, C.c_void_p),
+                                            C.cast(self.outs, C.c_void_p), C.byref(opts), C.byref(self.h)))
 
     def launch(self, stream: int = 0):
         from . import lib
@@ -184,6 +186,11 @@ class Batch:
 
         self.descs[i] = self.frames[i].frame_desc()
         return self.ctx._chk(lib().mlgi_batch_update_view(self.h, i, C.byref(self.descs[i]), C.byref(self.outs[i])))
+
+    def kernel_launches(self) -> int:
+        from . import lib
+
+        return lib().mlgi_batch_kernel_launches(self.h)
 
     def close(self):
         from . import lib

@@ -1,5 +1,6 @@
-"""Batched views (mlgi_batch_*): one persistent launch per pass over mixed views, replayed from a
-CUDA graph, must give each view exactly its single-frame (mlgi_gi_frame) result."""
+"""Batched views (mlgi_batch_*): one persistent launch per pass over mixed views, or each view's
+kernels on several streams, replayed from a CUDA graph, must give each view exactly its
+single-frame (mlgi_gi_frame) result."""
 import numpy as np
 import pytest
 
@@ -28,7 +29,9 @@ def single(ctx, df):
     return df.rgb_np().copy()
 
 
-def test_batch_equals_single_frames_and_replays(ctx):
+@pytest.mark.parametrize("form,streams", [(mlgi.BATCH_PERSISTENT, 0), (mlgi.BATCH_CONCURRENT, 3)],
+                         ids=["persistent", "concurrent"])
+def test_batch_equals_single_frames_and_replays(ctx, form, streams):
     import torch
 
     frames = [DeviceFrame(mlgi.make_scene(c)) for c in VIEWS]
@@ -36,7 +39,9 @@ def test_batch_equals_single_frames_and_replays(ctx):
     for f in frames:
         f.rgb.zero_()
     torch.cuda.synchronize()  # the batch runs on its own stream
-    b = Batch(ctx, frames)
+    b = Batch(ctx, frames, form, streams)
+    assert b.kernel_launches() == (9 if form == mlgi.BATCH_PERSISTENT
+                                   else sum(3 + (4 if f.cfg.levels >= 2 else 2) + 1 for f in frames))
     for _ in range(2):  # the graph replays
         b.launch()
         torch.cuda.synchronize()
