@@ -48,6 +48,8 @@ typedef void* mlgi_stream; /* a cudaStream_t; NULL selects the context's stream 
 #define MLGI_F32 0
 #define MLGI_F16 1
 #define MLGI_BF16 2
+#define MLGI_R11G11B10F 3  /* one 32-bit word per pixel, as GL_R11F_G11F_B10F */
+#define MLGI_RGBA8 4       /* one 32-bit word per pixel, UNORM, r in bits 0-7 */
 
 typedef struct {
     int device;          /* CUDA device ordinal */
@@ -204,6 +206,45 @@ typedef struct {
 /* VPL processing -> ISM splat -> pull-push -> final gathering on device buffers; the VPL
  * buffers and the atlas are context-owned. */
 mlgi_status mlgi_gi_frame(mlgi_ctx* ctx, const mlgi_frame_desc* frame, mlgi_radiance* out, mlgi_stream stream);
+
+/* ---- after the gathering: GI buffer format, bilateral blur, composite ------------------------ */
+
+/* GIStage's GI buffers are GL_R11F_G11F_B10F (GIStage.cpp:470). Packing of n RGB triples (device)
+ * into words with R in bits 0-10, G in 11-21, B in 22-31: unsigned floats with a 5-bit exponent
+ * (bias 15) and 6/6/5 mantissa bits, rounded to nearest even; negatives and -0 give 0, finite
+ * values beyond the largest (65024 / 65024 / 64512) give the largest, +Inf gives Inf, NaN gives
+ * NaN; denormals are kept. Unpacking is exact. */
+mlgi_status mlgi_pack_r11g11b10f(mlgi_ctx* ctx, const float* rgb, uint32_t* words, int64_t n, mlgi_stream stream);
+mlgi_status mlgi_unpack_r11g11b10f(mlgi_ctx* ctx, const uint32_t* words, float* rgb, int64_t n, mlgi_stream stream);
+
+/* GIStage::blur (GIStage.cpp:308-344) with gi_blur.frag:24-72: a separable 7-tap bilateral filter,
+ * the X pass then the Y pass, weights max(0, (4 - i)/4 - dz^2 - (5 (1 - max(0, N.n)))^2) from the
+ * linear depth difference dz (reprojection.glsl linearDepth) and the G-buffer normals. Both passes
+ * run in one kernel (the X pass of a tile and its 3-pixel halo rows is kept on chip). With
+ * format MLGI_R11G11B10F, input, intermediate and output are R11G11B10F words, as the reference's
+ * buffers are; with MLGI_F32 they are RGB floats. Samples outside the image are skipped (the
+ * reference's texelFetch there is undefined). */
+typedef struct {
+    float proj_a, proj_b;  /* projectionMatrix[2][2] and [3][2] (column-major [col][row]) */
+    int format;            /* MLGI_F32 or MLGI_R11G11B10F */
+} mlgi_blur_params;
+mlgi_status mlgi_gi_blur(mlgi_ctx* ctx, const mlgi_gbuffer_view* gbuffer, const void* gi_in, void* gi_out,
+                         const mlgi_blur_params* params, mlgi_stream stream);
+
+/* The GI part of the deferred composite (deferredshading.frag:47-81): ambient = GI * toLinear(albedo)
+ * * occlusion, plus the caller's direct term (diffuse + specular, which need the light's shadow
+ * map and are not part of this path), Reinhard tone mapping with exposure, then toSRGB (gamma
+ * 2.2, srgb_utils.glsl). albedo: RGBA8 UNORM words; occlusion and direct may be NULL (1 and 0).
+ * Output: RGB floats (out_format MLGI_F32) or RGBA8 UNORM words with alpha 255 (MLGI_RGBA8). */
+typedef struct {
+    int width, height;
+    float exposure;
+    int gi_format;   /* MLGI_F32 or MLGI_R11G11B10F */
+    int out_format;  /* MLGI_F32 or MLGI_RGBA8 */
+} mlgi_composite_params;
+mlgi_status mlgi_composite(mlgi_ctx* ctx, const void* gi, const uint32_t* albedo, const float* occlusion,
+                           const float* direct_rgb, void* out, const mlgi_composite_params* params,
+                           mlgi_stream stream);
 
 /* ---- batched views ------------------------------------------------------------------------- */
 

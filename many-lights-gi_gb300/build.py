@@ -27,6 +27,7 @@ CUDA_UNITS = [
     ("csrc/mlgi_api.cu", []),
     ("csrc/ism_static.cu", []),
     ("csrc/scene_kernels.cu", []),
+    ("csrc/post_kernels.cu", []),
     ("host/serve.cpp", []),
     ("host/autotune.cpp", []),
 ]

@@ -82,6 +82,35 @@ struct FgArgs {
     uint32_t* status;         // device error word (bit 0: VPL staging wait timed out)
 };
 
+// ---- after the gathering -------------------------------------------------------------------
+struct BlurArgs {
+    int width, height;
+    const float* depth;
+    const void* normal;  // octahedral, 2 x f32 or 2 x f16 per pixel
+    int normal_f16;
+    const void* gi_in;   // RGB floats or R11G11B10F words
+    void* gi_out;
+    int packed;          // 1: R11G11B10F input, intermediate and output
+    float proj_a, proj_b;
+};
+
+struct CompositeArgs {
+    int width, height;
+    const void* gi;
+    int gi_packed;
+    const uint32_t* albedo;    // RGBA8 UNORM
+    const float* occlusion;    // or nullptr
+    const float* direct;       // RGB floats, or nullptr
+    void* out;
+    int out_rgba8;
+    float exposure;
+};
+
+cudaError_t launch_pack_r11(const float* rgb, uint32_t* words, int64_t n, cudaStream_t s);
+cudaError_t launch_unpack_r11(const uint32_t* words, float* rgb, int64_t n, cudaStream_t s);
+cudaError_t launch_gi_blur(const BlurArgs& a, cudaStream_t s);
+cudaError_t launch_composite(const CompositeArgs& a, cudaStream_t s);
+
 // ---- batched frames: one persistent launch per pass over a device-resident view table -------
 struct BatchView {
     VplArgs vpl;

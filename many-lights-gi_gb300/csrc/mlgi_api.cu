@@ -456,6 +456,70 @@ mlgi_status mlgi_check_device_status(mlgi_ctx* ctx, mlgi_stream stream) {
     return MLGI_OK;
 }
 
+mlgi_status mlgi_pack_r11g11b10f(mlgi_ctx* ctx, const float* rgb, uint32_t* words, int64_t n, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (n < 0 || (n > 0 && (!rgb || !words))) return fail(ctx, MLGI_EINVAL, "bad packing arguments");
+    MLGI_CUDA(ctx, mlgi::launch_pack_r11(rgb, words, n, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_unpack_r11g11b10f(mlgi_ctx* ctx, const uint32_t* words, float* rgb, int64_t n, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (n < 0 || (n > 0 && (!rgb || !words))) return fail(ctx, MLGI_EINVAL, "bad unpacking arguments");
+    MLGI_CUDA(ctx, mlgi::launch_unpack_r11(words, rgb, n, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_gi_blur(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const void* gi_in, void* gi_out,
+                         const mlgi_blur_params* p, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!g || !p || !gi_in || !gi_out || !g->depth || !g->normal) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    if (g->width <= 0 || g->height <= 0 || g->width > 65535 || g->height > 65535)
+        return fail(ctx, MLGI_EINVAL, "bad image size %dx%d", g->width, g->height);
+    if (g->normal_format != MLGI_F32 && g->normal_format != MLGI_F16)
+        return fail(ctx, MLGI_EINVAL, "G-buffer normals must be F32 or F16");
+    if (p->format != MLGI_F32 && p->format != MLGI_R11G11B10F)
+        return fail(ctx, MLGI_EINVAL, "blur format must be F32 or R11G11B10F");
+    if (gi_in == gi_out) return fail(ctx, MLGI_EINVAL, "the blur does not run in place");
+    mlgi::BlurArgs a{};
+    a.width = g->width;
+    a.height = g->height;
+    a.depth = g->depth;
+    a.normal = g->normal;
+    a.normal_f16 = g->normal_format == MLGI_F16;
+    a.gi_in = gi_in;
+    a.gi_out = gi_out;
+    a.packed = p->format == MLGI_R11G11B10F;
+    a.proj_a = p->proj_a;
+    a.proj_b = p->proj_b;
+    MLGI_CUDA(ctx, mlgi::launch_gi_blur(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_composite(mlgi_ctx* ctx, const void* gi, const uint32_t* albedo, const float* occlusion,
+                           const float* direct_rgb, void* out, const mlgi_composite_params* p, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!gi || !albedo || !out || !p) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    if (p->width <= 0 || p->height <= 0) return fail(ctx, MLGI_EINVAL, "bad image size %dx%d", p->width, p->height);
+    if (p->gi_format != MLGI_F32 && p->gi_format != MLGI_R11G11B10F)
+        return fail(ctx, MLGI_EINVAL, "GI format must be F32 or R11G11B10F");
+    if (p->out_format != MLGI_F32 && p->out_format != MLGI_RGBA8)
+        return fail(ctx, MLGI_EINVAL, "output format must be F32 or RGBA8");
+    mlgi::CompositeArgs a{};
+    a.width = p->width;
+    a.height = p->height;
+    a.gi = gi;
+    a.gi_packed = p->gi_format == MLGI_R11G11B10F;
+    a.albedo = albedo;
+    a.occlusion = occlusion;
+    a.direct = direct_rgb;
+    a.out = out;
+    a.out_rgba8 = p->out_format == MLGI_RGBA8;
+    a.exposure = p->exposure;
+    MLGI_CUDA(ctx, mlgi::launch_composite(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
 mlgi_status mlgi_set_timing(mlgi_ctx* ctx, int enabled) {
     if (!ctx) return MLGI_EINVAL;
     ctx->timing = enabled != 0;

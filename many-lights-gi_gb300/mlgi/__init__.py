@@ -17,7 +17,7 @@ PKG = os.path.dirname(_HERE)
 LIB_PATH = os.path.join(PKG, "_build", "libmlgi.so")
 
 OK, EINVAL, ENOMEM, ETIMEDOUT, ECUDA, ECANCELED = 0, 1, 2, 3, 4, 5
-F32, F16, BF16 = 0, 1, 2
+F32, F16, BF16, R11G11B10F, RGBA8 = 0, 1, 2, 3, 4
 
 _p = C.c_void_p
 _f16 = C.c_float * 16
@@ -107,6 +107,15 @@ class SceneInfo(C.Structure):
                 ("bucket_stride", C.c_int64)]
 
 
+class BlurParams(C.Structure):
+    _fields_ = [("proj_a", C.c_float), ("proj_b", C.c_float), ("format", C.c_int)]
+
+
+class CompositeParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("exposure", C.c_float), ("gi_format", C.c_int),
+                ("out_format", C.c_int)]
+
+
 BATCH_PERSISTENT, BATCH_CONCURRENT = 0, 1
 
 
@@ -182,6 +191,10 @@ _SIGS = {
                                             C.POINTER(C.c_double)]),
     "mlgi_frame_host_sizes_get": (C.c_int32, [C.POINTER(FrameDesc), C.POINTER(FrameHostSizes)]),
     "mlgi_gi_frame_host": (C.c_int32, [_p, C.POINTER(FrameDesc), _p]),
+    "mlgi_pack_r11g11b10f": (C.c_int32, [_p, _p, _p, C.c_int64, _p]),
+    "mlgi_unpack_r11g11b10f": (C.c_int32, [_p, _p, _p, C.c_int64, _p]),
+    "mlgi_gi_blur": (C.c_int32, [_p, C.POINTER(GBufferView), _p, _p, C.POINTER(BlurParams), _p]),
+    "mlgi_composite": (C.c_int32, [_p, _p, _p, _p, _p, _p, C.POINTER(CompositeParams), _p]),
     "mlgi_set_timing": (C.c_int32, [_p, C.c_int]),
     "mlgi_last_timings": (C.c_int32, [_p, _p, C.c_int]),
     "mlgi_check_device_status": (C.c_int32, [_p, _p]),
@@ -291,6 +304,22 @@ class Context:
         ms = np.zeros(11, np.float32)
         self._chk(lib().mlgi_last_timings(self.h, ms.ctypes.data, 11))
         return ms
+
+    def pack_r11g11b10f(self, rgb, words, n: int, stream: int = 0):
+        return self._chk(lib().mlgi_pack_r11g11b10f(self.h, ptr(rgb), ptr(words), n, stream))
+
+    def unpack_r11g11b10f(self, words, rgb, n: int, stream: int = 0):
+        return self._chk(lib().mlgi_unpack_r11g11b10f(self.h, ptr(words), ptr(rgb), n, stream))
+
+    def gi_blur(self, g: GBufferView, gi_in, gi_out, proj_a: float, proj_b: float, fmt: int = F32, stream: int = 0):
+        p = BlurParams(proj_a, proj_b, fmt)
+        return self._chk(lib().mlgi_gi_blur(self.h, C.byref(g), ptr(gi_in), ptr(gi_out), C.byref(p), stream))
+
+    def composite(self, gi, albedo, out, width: int, height: int, exposure: float, gi_format: int = F32,
+                  out_format: int = F32, occlusion=None, direct=None, stream: int = 0):
+        p = CompositeParams(width, height, exposure, gi_format, out_format)
+        return self._chk(lib().mlgi_composite(self.h, ptr(gi), ptr(albedo), ptr(occlusion), ptr(direct), ptr(out),
+                                              C.byref(p), stream))
 
     def check_device_status(self, stream: int = 0):
         return self._chk(lib().mlgi_check_device_status(self.h, stream))
@@ -422,6 +451,12 @@ def make_scene(cfg: Config, points: bool = True) -> Scene:
     if st != OK:
         raise MlgiError(st, "mlgi_scene_generate")
     return Scene(cfg, info, gd, gn, ga, rd, rn, rf, pts, cnt, int(info.bucket_stride))
+
+
+def depth_terms(scene: "Scene") -> tuple[float, float]:
+    """projectionMatrix[2][2] and [3][2] of the camera (reprojection.glsl's linearDepth A and B)."""
+    p = scene.mat("proj")
+    return float(p[10]), float(p[14])
 
 
 def ism_params(cfg: Config) -> IsmParams:

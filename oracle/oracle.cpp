@@ -37,6 +37,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #ifdef _OPENMP
@@ -574,6 +575,144 @@ void final_gather(const FgParams& p, const float* depth, const float* nrm_oct, c
 }  // namespace
 
 // ---- C entry points (ctypes) ----------------------------------------------------------------
+namespace {
+
+// ---- after the gathering -------------------------------------------------------------------
+// R11G11B10F (GL_R11F_G11F_B10F, GIStage.cpp:470): one unsigned float channel with a 5-bit
+// exponent (bias 15) and `mb` mantissa bits, restated in double arithmetic: round to nearest even
+// (nearbyint in the default rounding mode), negatives and -0 to 0, finite overflow to the largest
+// finite value, +Inf to Inf, NaN to NaN, denormals kept.
+uint32_t uf_pack_ref(float x, int mb) {
+    const uint32_t emax = 31u << mb, maxfin = (30u << mb) | ((1u << mb) - 1u);
+    if (std::isnan(x)) return emax | (1u << (mb - 1));
+    if (std::signbit(x) || x == 0.0f) return 0u;
+    if (std::isinf(x)) return emax;
+    const double v = x;
+    if (v >= (2.0 - std::ldexp(1.0, -mb)) * 32768.0) return maxfin;
+    int e2 = 0;
+    std::frexp(v, &e2);  // v in [2^(e2-1), 2^e2)
+    int E = e2 - 1;
+    if (E < -14) return (uint32_t)std::nearbyint(v / std::ldexp(1.0, -14 - mb));  // denormal (or smallest normal)
+    double q = std::nearbyint(v / std::ldexp(1.0, E - mb));                          // in [2^mb, 2^(mb+1)]
+    if (q >= std::ldexp(1.0, mb + 1)) {
+        q = q / 2.0;
+        ++E;
+    }
+    if (E + 15 >= 31) return maxfin;
+    return ((uint32_t)(E + 15) << mb) | ((uint32_t)q - (1u << mb));
+}
+
+float uf_unpack_ref(uint32_t v, int mb) {
+    const uint32_t e = (v >> mb) & 31u, m = v & ((1u << mb) - 1u);
+    if (e == 31u) return m ? std::numeric_limits<float>::quiet_NaN() : std::numeric_limits<float>::infinity();
+    if (e == 0u) return (float)std::ldexp((double)m, -14 - mb);
+    return (float)std::ldexp(1.0 + std::ldexp((double)m, -mb), (int)e - 15);
+}
+
+uint32_t pack_r11_ref(float r, float g, float b) {
+    return uf_pack_ref(r, 6) | (uf_pack_ref(g, 6) << 11) | (uf_pack_ref(b, 5) << 22);
+}
+V3<float> unpack_r11_ref(uint32_t w) {
+    return V3<float>(uf_unpack_ref(w & 0x7FFu, 6), uf_unpack_ref((w >> 11) & 0x7FFu, 6), uf_unpack_ref(w >> 22, 5));
+}
+
+// gi_blur.frag:24-72 as GIStage::blur runs it (GIStage.cpp:308-344): the X pass over the whole
+// image into a temporary buffer, then the Y pass; with `packed`, every buffer is R11G11B10F.
+// Samples outside the image are skipped.
+void gi_blur_ref(int w, int h, const float* depth, const float* nrm_oct, const void* gi_in, int packed, float A,
+                 float B, void* gi_out, int threads) {
+    const size_t n = (size_t)w * h;
+    std::vector<float> lin(n);
+    std::vector<V3<float>> nrm(n), src(n), tmp(n);
+    for (size_t p = 0; p < n; ++p) {
+        const float z_b = depth[p];
+        const float z_n = 2.0f * z_b - 1.0f;
+        lin[p] = -B / (A + z_n);  // reprojection.glsl:6-14
+        nrm[p] = oct_decode<float>(nrm_oct[2 * p], nrm_oct[2 * p + 1]);
+        src[p] = packed ? unpack_r11_ref(static_cast<const uint32_t*>(gi_in)[p])
+                        : V3<float>(static_cast<const float*>(gi_in)[3 * p], static_cast<const float*>(gi_in)[3 * p + 1],
+                                    static_cast<const float*>(gi_in)[3 * p + 2]);
+    }
+    auto weight = [](float r, float depthDiff, float normalDiff) {
+        const float factor = (3.0f - r + 1.0f) / 4.0f;  // (KERNEL_RADIUS - r + 1) / 4
+        float wgt = factor - depthDiff * depthDiff - normalDiff * normalDiff;
+        return glsl::gmax(0.0f, wgt);
+    };
+    auto pass = [&](const std::vector<V3<float>>& in, std::vector<V3<float>>& out, int dx, int dy) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : omp_get_max_threads())
+#endif
+        for (int y = 0; y < h; ++y)
+            for (int x = 0; x < w; ++x) {
+                const size_t c = (size_t)y * w + x;
+                const float d = lin[c];
+                const V3<float> N = nrm[c];
+                V3<float> acc(0.0f, 0.0f, 0.0f);
+                float factorAcc = 0.0f;
+                acc = acc + in[c];
+                factorAcc = factorAcc + 1.0f;
+                for (int side = -1; side <= 1; side += 2)
+                    for (int i = 1; i <= 3; ++i) {
+                        const int sx = x + side * dx * i, sy = y + side * dy * i;
+                        if (sx < 0 || sy < 0 || sx >= w || sy >= h) continue;
+                        const size_t sp = (size_t)sy * w + sx;
+                        const float normalFactor = 1.0f - glsl::gmax(0.0f, dot(N, nrm[sp]));
+                        const float depthDiff = (lin[sp] - d) / 1.0f;
+                        const float factor = weight(float(i), depthDiff, normalFactor * 5.0f);
+                        factorAcc = factorAcc + factor;
+                        acc = acc + in[sp] * factor;
+                    }
+                V3<float> o = acc / factorAcc;
+                if (packed) o = unpack_r11_ref(pack_r11_ref(o.x, o.y, o.z));
+                out[c] = o;
+            }
+    };
+    pass(src, tmp, 1, 0);
+    pass(tmp, src, 0, 1);
+    for (size_t p = 0; p < n; ++p) {
+        if (packed) {
+            static_cast<uint32_t*>(gi_out)[p] = pack_r11_ref(src[p].x, src[p].y, src[p].z);
+        } else {
+            float* o = static_cast<float*>(gi_out);
+            o[3 * p] = src[p].x;
+            o[3 * p + 1] = src[p].y;
+            o[3 * p + 2] = src[p].z;
+        }
+    }
+}
+
+// deferredshading.frag:39-44, 69-80 (GI ambient + the caller's direct term, Reinhard, toSRGB with
+// srgb_utils.glsl's gamma 2.2); albedo is RGBA8 UNORM.
+void composite_ref(int w, int h, const void* gi, int packed, const uint32_t* albedo, const float* occ,
+                   const float* direct, float exposure, float* out_rgb, uint32_t* out_rgba8) {
+    const float gamma = 2.2f, inv_gamma = 1.0f / gamma;
+    for (size_t p = 0; p < (size_t)w * h; ++p) {
+        const V3<float> g = packed ? unpack_r11_ref(static_cast<const uint32_t*>(gi)[p])
+                                   : V3<float>(static_cast<const float*>(gi)[3 * p], static_cast<const float*>(gi)[3 * p + 1],
+                                               static_cast<const float*>(gi)[3 * p + 2]);
+        const uint32_t al = albedo[p];
+        const V3<float> diffuse(std::pow(float(al & 0xFFu) / 255.0f, gamma), std::pow(float((al >> 8) & 0xFFu) / 255.0f, gamma),
+                                std::pow(float((al >> 16) & 0xFFu) / 255.0f, gamma));
+        const float occlusion = occ ? occ[p] : 1.0f;
+        V3<float> c = g * diffuse * occlusion;
+        if (direct) c = c + V3<float>(direct[3 * p], direct[3 * p + 1], direct[3 * p + 2]);
+        c = c * exposure;
+        c = V3<float>(c.x / (1.0f + c.x), c.y / (1.0f + c.y), c.z / (1.0f + c.z));
+        c = V3<float>(std::pow(c.x, inv_gamma), std::pow(c.y, inv_gamma), std::pow(c.z, inv_gamma));
+        if (out_rgb) {
+            out_rgb[3 * p] = c.x;
+            out_rgb[3 * p + 1] = c.y;
+            out_rgb[3 * p + 2] = c.z;
+        }
+        if (out_rgba8) {
+            auto unorm = [](float v) { return to_uint(glsl::gmin(glsl::gmax(v, 0.0f), 1.0f) * 255.0f + 0.5f); };
+            out_rgba8[p] = unorm(c.x) | (unorm(c.y) << 8) | (unorm(c.z) << 16) | 0xFF000000u;
+        }
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 int oracle_max_threads() {
@@ -678,6 +817,26 @@ void oracle_final_gather_f64(int w, int h, const float* depth, const float* nrm_
 }
 
 // Exposed for unit tests of the shared math.
+void oracle_pack_r11g11b10f(const float* rgb, uint32_t* words, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) words[i] = pack_r11_ref(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+}
+void oracle_unpack_r11g11b10f(const uint32_t* words, float* rgb, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        const V3<float> c = unpack_r11_ref(words[i]);
+        rgb[3 * i] = c.x;
+        rgb[3 * i + 1] = c.y;
+        rgb[3 * i + 2] = c.z;
+    }
+}
+void oracle_gi_blur(int w, int h, const float* depth, const float* nrm_oct, const void* gi_in, int packed, float A,
+                    float B, void* gi_out, int threads) {
+    gi_blur_ref(w, h, depth, nrm_oct, gi_in, packed, A, B, gi_out, threads);
+}
+void oracle_composite(int w, int h, const void* gi, int packed, const uint32_t* albedo, const float* occ,
+                      const float* direct, float exposure, float* out_rgb, uint32_t* out_rgba8) {
+    composite_ref(w, h, gi, packed, albedo, occ, direct, exposure, out_rgb, out_rgba8);
+}
+
 uint32_t oracle_pack3sn_f32(float x, float y, float z) { return pack3SN<float>(V3<float>(x, y, z)); }
 void oracle_unpack3sn_f32(uint32_t u, float* out) {
     V3<float> v = unpack3SN<float>(u);

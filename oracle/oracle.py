@@ -147,3 +147,46 @@ def paraboloid_project(rel, dist, n, z_far, ism_index, gx, gy, preserve_sign):
     lib().oracle_paraboloid_project_f32(_p(np.asarray(rel, np.float32)), C.c_float(dist), _p(np.asarray(n, np.float32)),
                                         C.c_float(z_far), C.c_float(ism_index), gx, gy, int(preserve_sign), _p(out))
     return out
+
+
+def pack_r11g11b10f(rgb) -> np.ndarray:
+    """GL_R11F_G11F_B10F words of RGB triples (rgb: [..., 3] float32)."""
+    a = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+    out = np.zeros(len(a), np.uint32)
+    lib().oracle_pack_r11g11b10f(_p(a), _p(out), C.c_int64(len(a)))
+    return out
+
+
+def unpack_r11g11b10f(words) -> np.ndarray:
+    w = np.ascontiguousarray(words, np.uint32).reshape(-1)
+    out = np.zeros((len(w), 3), np.float32)
+    lib().oracle_unpack_r11g11b10f(_p(w), _p(out), C.c_int64(len(w)))
+    return out
+
+
+def gi_blur(depth, normal_oct, gi, proj_a, proj_b, packed=False, threads=0):
+    """gi_blur.frag's X then Y pass (GIStage.cpp:308-344). gi: [H, W, 3] float32, or [H, W] uint32
+    R11G11B10F words with packed=True; returns the same layout."""
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    n = np.ascontiguousarray(normal_oct, np.float32)
+    g = np.ascontiguousarray(gi, np.uint32 if packed else np.float32)
+    out = np.zeros_like(g)
+    lib().oracle_gi_blur(w, h, _p(depth), _p(n), _p(g), int(packed), C.c_float(proj_a), C.c_float(proj_b), _p(out),
+                         threads)
+    return out
+
+
+def composite(gi, albedo, exposure, occlusion=None, direct=None, packed=False):
+    """deferredshading.frag's GI ambient term, Reinhard and toSRGB. Returns (rgb float32 [H, W, 3],
+    rgba8 uint32 [H, W])."""
+    albedo = np.ascontiguousarray(albedo, np.uint32)
+    h, w = albedo.shape
+    g = np.ascontiguousarray(gi, np.uint32 if packed else np.float32)
+    occ = None if occlusion is None else np.ascontiguousarray(occlusion, np.float32)
+    d = None if direct is None else np.ascontiguousarray(direct, np.float32)
+    rgb = np.zeros((h, w, 3), np.float32)
+    words = np.zeros((h, w), np.uint32)
+    lib().oracle_composite(w, h, _p(g), int(packed), _p(albedo), _p(occ), _p(d), C.c_float(exposure), _p(rgb),
+                           _p(words))
+    return rgb, words
