@@ -177,10 +177,32 @@ typedef struct {
     int interleave;          /* interleaved-sampling factor I (N must be a multiple of I*I) */
     int shadowing;           /* GIShadowing */
     int tile;                /* work tile edge in same-class pixels: 8 or 16 (0 selects 16) */
-    int cull;                /* per-tile VPL culling against the tile's world-space bounds */
-    float influence_cutoff;  /* with cull: flux/d^4 contribution below which a VPL is dropped; 0 = off */
+    int cull;                /* 0: none; 1: per-tile culling against the tile's world-space bounds;
+                                2: reference-style clustered culling (mlgi_cluster_lights), which
+                                needs proj_a, proj_b and camera_z_far below */
+    float influence_cutoff;  /* with cull 1: flux/d^4 contribution below which a VPL is dropped; 0 = off */
     int vpl_format;          /* MLGI_F32: 48-byte records; MLGI_F16: 24-byte reduced records */
+    float proj_a, proj_b;    /* cull 2: projectionMatrix[2][2] and [3][2] of the camera */
+    float camera_z_far;      /* cull 2: the camera's far plane */
 } mlgi_fg_params;
+
+/* ClusteredShading::process (ClusteredShading.cpp:70-112) with clustering.comp and light_lists.comp:
+ * clusters of 128 x 128 pixels times 16 logarithmic depth slices; a used cluster keeps the VPLs
+ * for which any of its corners lies in front of the VPL's plane. Outputs (device): `used`, one
+ * word per tile (bit s = slice s is used; tiles_x = ceil(width / 128) per row), `masks`, per
+ * cluster (tile * 16 + slice) ceil(n_vpl / 32) words of keep bits (rows of unused clusters are
+ * left as they are), and `pixel_slice`, the slice of each pixel. Kept from the reference: slice 0
+ * starting at view z = +0.05 and its corner list, which has (left, top) twice in place of
+ * (right, top). The slice index is clamped to 15 (the reference's formula reaches 16 at the far
+ * plane). With cull == 2, mlgi_final_gather runs this itself with context scratch. */
+typedef struct {
+    float inv_view_proj[16];  /* inverse(projection * view), column-major */
+    float proj_a, proj_b;     /* projectionMatrix[2][2], [3][2] */
+    float z_far;              /* the camera's far plane */
+} mlgi_cluster_params;
+mlgi_status mlgi_cluster_lights(mlgi_ctx* ctx, const mlgi_gbuffer_view* gbuffer, const mlgi_vpl_buf* vpls, int n_vpl,
+                                const mlgi_cluster_params* params, uint32_t* used, uint32_t* masks,
+                                uint8_t* pixel_slice, mlgi_stream stream);
 
 typedef struct {
     int width, height;

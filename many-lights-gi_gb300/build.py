@@ -28,6 +28,7 @@ CUDA_UNITS = [
     ("csrc/ism_static.cu", []),
     ("csrc/scene_kernels.cu", []),
     ("csrc/post_kernels.cu", []),
+    ("csrc/cluster_kernels.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     ("host/serve.cpp", []),
     ("host/autotune.cpp", []),
 ]

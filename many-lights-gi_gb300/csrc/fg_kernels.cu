@@ -165,7 +165,8 @@ struct FgSmem {
 
 // One T x T tile of interleave class c. The caller initialises S.bar once and keeps `parity`
 // across calls. Returns false (block-uniform) when the VPL staging wait timed out.
-template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16>
+// kClusters: compile the clustered-culling path (cull == 2), which batched views do not use
+template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16, bool kClusters = true>
 __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const int c, FgSmem<T * T>& S,
                                         uint32_t& parity) {
     constexpr int NT = T * T;
@@ -183,6 +184,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     // ---- pixel setup: world position from depth (final_gathering.comp:70-76, evaluated with
     // compensated arithmetic) and the octahedral normal ----
     v3 fw = mk(0.f, 0.f, 0.f), fn = mk(0.f, 0.f, 1.f);
+    const uint32_t* cl_row = nullptr;  // cull == 2: the keep bits of the pixel's cluster
     if (valid) {
         const size_t pix = (size_t)y * a.width + x;
         const float d = __ldg(a.depth + pix);
@@ -198,11 +200,15 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
             ey = e.y;
         }
         fn = oct_decode(ex, ey);
+        if (kClusters && a.cull == 2) {
+            const int cluster = ((y / kClusterPixels) * a.cl_tiles_x + x / kClusterPixels) * kClusterSlices + a.cl_slice[pix];
+            cl_row = a.cl_masks + (size_t)cluster * a.cl_words;
+        }
     }
 
     // ---- per-tile bounds for culling ----
     v3 bmin = mk(0.f, 0.f, 0.f), bmax = mk(0.f, 0.f, 0.f);
-    if (a.cull) {
+    if (a.cull == 1) {
         const float inf = __int_as_float(0x7f800000);
         float b[6] = {valid ? fw.x : inf,  valid ? fw.y : inf,  valid ? fw.z : inf,
                       valid ? -fw.x : inf, valid ? -fw.y : inf, valid ? -fw.z : inf};
@@ -273,7 +279,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
             S.d[k] = make_float4(u.x, u.y, u.z, 0.f);
             S.org[k] = make_float2(float(tx * a.ism_size) + hs, float(ty * a.ism_size) + hs);
             bool keep = true;
-            if (a.cull) {
+            if (a.cull == 1) {
                 // front half-space of the VPL against the box corner farthest along its normal
                 const v3 sup = mk(n.x > 0.f ? bmax.x : bmin.x, n.y > 0.f ? bmax.y : bmin.y, n.z > 0.f ? bmax.z : bmin.z);
                 if (dot(n, sup - p) < -1e-3f) keep = false;
@@ -314,6 +320,10 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
             const bool shadow = a.shadowing != 0;
             const int aw = a.atlas_w, ah = a.atlas_h;
             auto prepare = [&](int k, float& G, float& vz, size_t& t, float3& flux) -> bool {
+                if (kClusters && cl_row) {  // outside the pixel's cluster list
+                    const int vid = vbase + base + k;
+                    if (!((__ldg(cl_row + (vid >> 5)) >> (vid & 31)) & 1u)) return false;
+                }
                 const float4 A = S.a[k], B = S.b[k];
                 const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
                 const float d2 = dx * dx + dy * dy + dz * dz;
@@ -463,7 +473,7 @@ __global__ void __launch_bounds__(256, 4) batch_fg_kernel(BatchTable t) {
         }
         const int local = w.local(item);
         const int tile = local % tpc, cls = local / tpc;
-        if (!fg_tile<16, kReduced, kReduced, kReduced>(args, tile, cls, S, parity))
+        if (!fg_tile<16, kReduced, kReduced, kReduced, false>(args, tile, cls, S, parity))
             return;  // block-uniform: the staging wait timed out (status word already set)
     }
 }

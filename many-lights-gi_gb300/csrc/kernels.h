@@ -80,7 +80,29 @@ struct FgArgs {
     float influence_cutoff;   // 0: off
     float* out;               // width*height*3
     uint32_t* status;         // device error word (bit 0: VPL staging wait timed out)
+    // cull == 2: clustered culling; a pixel keeps the VPLs of its cluster's mask
+    const uint32_t* cl_masks;     // (tiles_x * tiles_y * 16) x cl_words
+    const uint8_t* cl_slice;      // per pixel
+    int cl_tiles_x, cl_words;
 };
+
+// ---- clustered culling (reference style) ---------------------------------------------------
+constexpr int kClusterPixels = 128, kClusterSlices = 16, kClusterSlicesIntoFirst = 3;
+
+struct ClusterArgs {
+    int width, height, tiles_x, tiles_y;
+    const float* depth;
+    float inv_vp[16];
+    float proj_a, proj_b;
+    float scale;              // (16 + 3) / log2(zFar)
+    const float4* packed;     // packed VPL records
+    int n_vpl, mask_words;
+    uint32_t* used;           // per tile: bit s set when slice s is used
+    uint32_t* masks;          // per cluster (tile * 16 + slice): mask_words words
+    uint8_t* pixel_slice;     // per pixel
+};
+
+cudaError_t launch_cluster_lights(const ClusterArgs& a, cudaStream_t s);
 
 // ---- after the gathering -------------------------------------------------------------------
 struct BlurArgs {

@@ -41,6 +41,7 @@ struct mlgi_ctx {
     // frame-level buffers
     DevBuf vpl, packed, reduced, keys, depth;
     DevBuf pp;  // pull-push pyramid levels 1 and 2
+    DevBuf cl;  // clustered culling: used slices, cluster masks, pixel slices
     // host-frame input copies
     DevBuf h_rsm_depth, h_rsm_normal, h_rsm_diffuse, h_points, h_counts, h_gdepth, h_gnormal, h_rgb;
     bool timing = false;
@@ -124,6 +125,7 @@ void mark(mlgi_ctx* ctx, int pass, cudaStream_t s) {
 }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 mlgi_status check_ism(mlgi_ctx* ctx, const mlgi_ism_params* p) {
     if (!p) return fail(ctx, MLGI_EINVAL, "ism params are NULL");
@@ -190,7 +192,7 @@ void mlgi_destroy(mlgi_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->shuffle_dev) cudaFree(kv.second);
-    for (DevBuf* b : {&ctx->vpl, &ctx->packed, &ctx->reduced, &ctx->keys, &ctx->depth, &ctx->pp, &ctx->h_rsm_depth,
+    for (DevBuf* b : {&ctx->vpl, &ctx->packed, &ctx->reduced, &ctx->keys, &ctx->depth, &ctx->pp, &ctx->cl, &ctx->h_rsm_depth,
                       &ctx->h_rsm_normal, &ctx->h_rsm_diffuse, &ctx->h_points, &ctx->h_counts, &ctx->h_gdepth,
                       &ctx->h_gnormal, &ctx->h_rgb})
         if (b->p) cudaFree(b->p);
@@ -344,6 +346,9 @@ mlgi_status build_fg_args(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_
         return fail(ctx, MLGI_EINVAL, "VPL count %d is not a multiple of I^2 = %d", p->vpl_count, I * I);
     if (p->vpl_count > vpls->capacity) return fail(ctx, MLGI_EINVAL, "VPL count exceeds capacity");
     if (p->tile != 0 && p->tile != 8 && p->tile != 16) return fail(ctx, MLGI_EINVAL, "tile must be 0, 8 or 16");
+    if (p->cull < 0 || p->cull > 2) return fail(ctx, MLGI_EINVAL, "cull must be 0, 1 or 2");
+    if (p->cull == 2 && (!vpls->packed || !aligned16(vpls->packed) || !(p->camera_z_far > 1.f)))
+        return fail(ctx, MLGI_EINVAL, "clustered culling needs the packed VPL records and a camera far plane > 1");
     if (p->vpl_end <= p->vpl_start) return fail(ctx, MLGI_EINVAL, "empty VPL range");
     if (p->vpl_format != MLGI_F32 && p->vpl_format != MLGI_F16) return fail(ctx, MLGI_EINVAL, "bad VPL format");
     if (p->vpl_format == MLGI_F16 && !vpls->reduced) return fail(ctx, MLGI_EINVAL, "reduced VPL records missing");
@@ -430,13 +435,66 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
     return MLGI_OK;
 }
 
+mlgi_status mlgi_cluster_lights(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls, int n_vpl,
+                                const mlgi_cluster_params* p, uint32_t* used, uint32_t* masks, uint8_t* pixel_slice,
+                                mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!g || !vpls || !p || !used || !masks || !pixel_slice || !g->depth || !vpls->packed)
+        return fail(ctx, MLGI_EINVAL, "NULL argument");
+    if (g->width <= 0 || g->height <= 0 || g->width > 65535 || g->height > 65535)
+        return fail(ctx, MLGI_EINVAL, "bad image size %dx%d", g->width, g->height);
+    if (n_vpl <= 0 || n_vpl > vpls->capacity || !aligned16(vpls->packed))
+        return fail(ctx, MLGI_EINVAL, "bad VPL buffer (count %d, capacity %d)", n_vpl, vpls->capacity);
+    if (!(p->z_far > 1.f)) return fail(ctx, MLGI_EINVAL, "the camera far plane must be > 1");
+    mlgi::ClusterArgs a{};
+    a.width = g->width;
+    a.height = g->height;
+    a.tiles_x = (g->width + mlgi::kClusterPixels - 1) / mlgi::kClusterPixels;
+    a.tiles_y = (g->height + mlgi::kClusterPixels - 1) / mlgi::kClusterPixels;
+    a.depth = g->depth;
+    std::memcpy(a.inv_vp, p->inv_view_proj, sizeof(a.inv_vp));
+    a.proj_a = p->proj_a;
+    a.proj_b = p->proj_b;
+    a.scale = float(mlgi::kClusterSlices + mlgi::kClusterSlicesIntoFirst) / std::log2(p->z_far);
+    a.packed = reinterpret_cast<const float4*>(vpls->packed);
+    a.n_vpl = n_vpl;
+    a.mask_words = (n_vpl + 31) / 32;
+    a.used = used;
+    a.masks = masks;
+    a.pixel_slice = pixel_slice;
+    MLGI_CUDA(ctx, mlgi::launch_cluster_lights(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
 mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls,
                               const mlgi_atlas* atlas, const mlgi_fg_params* p, mlgi_radiance* out,
                               mlgi_stream stream) {
     if (!ctx) return MLGI_EINVAL;
     mlgi::FgArgs a;
-    const mlgi_status st = build_fg_args(ctx, g, vpls, atlas, p, out, a);
+    mlgi_status st = build_fg_args(ctx, g, vpls, atlas, p, out, a);
     if (st != MLGI_OK) return st;
+    if (p->cull == 2) {  // the clusters' VPL masks first, in context scratch
+        const int tx = (g->width + mlgi::kClusterPixels - 1) / mlgi::kClusterPixels;
+        const int ty = (g->height + mlgi::kClusterPixels - 1) / mlgi::kClusterPixels;
+        const int words = (p->vpl_count + 31) / 32;
+        const size_t used_b = align256((size_t)tx * ty * 4);
+        const size_t masks_b = align256((size_t)tx * ty * mlgi::kClusterSlices * words * 4);
+        if ((st = ensure(ctx, ctx->cl, used_b + masks_b + (size_t)g->width * g->height)) != MLGI_OK) return st;
+        char* base = static_cast<char*>(ctx->cl.p);
+        mlgi_cluster_params cp{};
+        std::memcpy(cp.inv_view_proj, p->inv_view_proj, sizeof(cp.inv_view_proj));
+        cp.proj_a = p->proj_a;
+        cp.proj_b = p->proj_b;
+        cp.z_far = p->camera_z_far;
+        if ((st = mlgi_cluster_lights(ctx, g, vpls, p->vpl_count, &cp, reinterpret_cast<uint32_t*>(base),
+                                      reinterpret_cast<uint32_t*>(base + used_b),
+                                      reinterpret_cast<uint8_t*>(base + used_b + masks_b), stream)) != MLGI_OK)
+            return st;
+        a.cl_masks = reinterpret_cast<const uint32_t*>(base + used_b);
+        a.cl_slice = reinterpret_cast<const uint8_t*>(base + used_b + masks_b);
+        a.cl_tiles_x = tx;
+        a.cl_words = words;
+    }
     MLGI_CUDA(ctx, mlgi::launch_final_gather(a, pick(ctx, stream)));
     return MLGI_OK;
 }
@@ -664,7 +722,6 @@ struct mlgi_batch {
 
 namespace {
 
-size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 size_t view_arena_bytes(const mlgi_frame_desc& f) {
     const size_t n = (size_t)f.vpl.count, texels = (size_t)f.ism.grid_x * f.ism.ism_size * f.ism.grid_y * f.ism.ism_size;
@@ -696,6 +753,7 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     mlgi_status st = build_vpl_args(ctx, &f.rsm, &f.vpl, &vb, v.vpl);
     if (st == MLGI_OK) st = build_splat_args(ctx, &f.points, &vb, (int)n, &f.ism, &atlas, v.splat);
     if (st == MLGI_OK) st = build_pullpush_args(ctx, &atlas, &f.ism, pp_scratch, v.pp);
+    if (f.fg.cull == 2) return fail(ctx, MLGI_EINVAL, "clustered culling is a single-frame mode");
     mlgi_fg_params fp = f.fg;
     fp.tile = 16;
     if (st == MLGI_OK) st = build_fg_args(ctx, &f.gbuffer, &vb, &atlas, &fp, &out, v.fg);

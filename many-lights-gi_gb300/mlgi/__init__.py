@@ -59,7 +59,8 @@ class FgParams(C.Structure):
                 ("clamp_value", C.c_float), ("vpl_count", C.c_int), ("vpl_start", C.c_int), ("vpl_end", C.c_int),
                 ("scale_isms", C.c_int), ("ism_size", C.c_int), ("grid_x", C.c_int), ("grid_y", C.c_int),
                 ("interleave", C.c_int), ("shadowing", C.c_int), ("tile", C.c_int), ("cull", C.c_int),
-                ("influence_cutoff", C.c_float), ("vpl_format", C.c_int)]
+                ("influence_cutoff", C.c_float), ("vpl_format", C.c_int), ("proj_a", C.c_float),
+                ("proj_b", C.c_float), ("camera_z_far", C.c_float)]
 
 
 class Radiance(C.Structure):
@@ -105,6 +106,10 @@ class SceneInfo(C.Structure):
                 ("light_pos", C.c_float * 3), ("light_dir", C.c_float * 3), ("z_near", C.c_float),
                 ("z_far", C.c_float), ("total_area", C.c_float), ("point_radius", C.c_float),
                 ("bucket_stride", C.c_int64)]
+
+
+class ClusterParams(C.Structure):
+    _fields_ = [("inv_view_proj", _f16), ("proj_a", C.c_float), ("proj_b", C.c_float), ("z_far", C.c_float)]
 
 
 class BlurParams(C.Structure):
@@ -191,6 +196,8 @@ _SIGS = {
                                             C.POINTER(C.c_double)]),
     "mlgi_frame_host_sizes_get": (C.c_int32, [C.POINTER(FrameDesc), C.POINTER(FrameHostSizes)]),
     "mlgi_gi_frame_host": (C.c_int32, [_p, C.POINTER(FrameDesc), _p]),
+    "mlgi_cluster_lights": (C.c_int32, [_p, C.POINTER(GBufferView), C.POINTER(VplBuf), C.c_int,
+                                        C.POINTER(ClusterParams), _p, _p, _p, _p]),
     "mlgi_pack_r11g11b10f": (C.c_int32, [_p, _p, _p, C.c_int64, _p]),
     "mlgi_unpack_r11g11b10f": (C.c_int32, [_p, _p, _p, C.c_int64, _p]),
     "mlgi_gi_blur": (C.c_int32, [_p, C.POINTER(GBufferView), _p, _p, C.POINTER(BlurParams), _p]),
@@ -304,6 +311,11 @@ class Context:
         ms = np.zeros(11, np.float32)
         self._chk(lib().mlgi_last_timings(self.h, ms.ctypes.data, 11))
         return ms
+
+    def cluster_lights(self, g: GBufferView, vpls: VplBuf, n_vpl: int, params: ClusterParams, used, masks,
+                       pixel_slice, stream: int = 0):
+        return self._chk(lib().mlgi_cluster_lights(self.h, C.byref(g), C.byref(vpls), n_vpl, C.byref(params),
+                                                   ptr(used), ptr(masks), ptr(pixel_slice), stream))
 
     def pack_r11g11b10f(self, rgb, words, n: int, stream: int = 0):
         return self._chk(lib().mlgi_pack_r11g11b10f(self.h, ptr(rgb), ptr(words), n, stream))
@@ -468,6 +480,7 @@ def vpl_params(cfg: Config, scene: Scene) -> VplParams:
 
 
 def fg_params(cfg: Config, scene: Scene) -> FgParams:
+    a, b = depth_terms(scene) if scene.info is not None else (0.0, 0.0)
     return FgParams(mat16(scene.mat("inv_view_proj")), cfg.z_far, cfg.gi_intensity, cfg.clamp_value, cfg.n_vpl, 0,
                     cfg.n_vpl, 0, cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.interleave, 1, cfg.tile, cfg.cull,
-                    cfg.influence_cutoff, F16 if cfg.reduced else F32)
+                    cfg.influence_cutoff, F16 if cfg.reduced else F32, a, b, cfg.z_far)

@@ -442,6 +442,10 @@ struct FgParams {
     int tile;             // 0: no culling; else tile edge in de-interleaved pixels
     double influence_cutoff;  // 0: no influence-radius culling
     int accurate_world;       // reconstruct world positions exactly rounded (see frag_world_rounded)
+    // clustered culling: a pixel keeps the VPLs whose bit is set in its cluster's mask
+    const uint32_t* cl_masks = nullptr;
+    const uint8_t* cl_slice = nullptr;
+    int cl_tiles_x = 0, cl_words = 0;
 };
 
 template <class T> V3<T> oct_decode(T ex, T ey) {
@@ -539,7 +543,11 @@ void final_gather(const FgParams& p, const float* depth, const float* nrm_oct, c
             const size_t pix = (size_t)y * p.width + x;
             const V3<T> fn = oct_decode<T>(T(nrm_oct[2 * pix]), T(nrm_oct[2 * pix + 1]));
             V3<T> acc(T(0));
+            const uint32_t* cl_row =
+                p.cl_masks ? p.cl_masks + ((size_t)((y / 128) * p.cl_tiles_x + x / 128) * 16 + p.cl_slice[pix]) * p.cl_words
+                           : nullptr;
             for (int vi : list) {
+                if (cl_row && !((cl_row[vi >> 5] >> (vi & 31)) & 1u)) continue;
                 V3<T> vp(vpos[3 * vi], vpos[3 * vi + 1], vpos[3 * vi + 2]);
                 V3<T> vn(vnrm[3 * vi], vnrm[3 * vi + 1], vnrm[3 * vi + 2]);
                 V3<T> vc(vcol[3 * vi], vcol[3 * vi + 1], vcol[3 * vi + 2]);
@@ -679,6 +687,55 @@ void gi_blur_ref(int w, int h, const float* depth, const float* nrm_oct, const v
             o[3 * p + 2] = src[p].z;
         }
     }
+}
+
+// clustering.comp:30-86 and light_lists.comp:42-126 (ClusteredShading::process), in FP32 with the
+// shaders' operation order: used depth slices per 128-pixel tile, each pixel's slice, and per used
+// cluster the VPLs for which any of the 8 corners (the reference's list, (left, top) twice) lies
+// in front of the VPL's plane. Slice index clamped to 15.
+void cluster_lights_ref(int w, int h, const float* depth, const float* inv_vp16, float A, float B, float zfar,
+                        const float* vpos, const uint32_t* vpn_bits, int n_vpl, uint32_t* used, uint32_t* masks,
+                        uint8_t* pixel_slice) {
+    const int tx = (w + 127) / 128, ty = (h + 127) / 128, words = (n_vpl + 31) / 32;
+    const float scale = float(16 + 3) / std::log2(zfar);
+    auto lin_depth = [&](float z_b) { const float z_n = 2.0f * z_b - 1.0f; return -B / (A + z_n); };
+    auto log_depth = [&](float z_e) { const float z_n = (1.0f / z_e * -B) - A; return (z_n + 1.0f) / 2.0f; };
+    std::fill(used, used + (size_t)tx * ty, 0u);
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const float s = glsl::gmax(std::log2(-lin_depth(depth[(size_t)y * w + x])) * scale - 3.0f, 0.0f);
+            const int slice = std::min(to_int(s), 15);
+            pixel_slice[(size_t)y * w + x] = (uint8_t)slice;
+            used[(y / 128) * tx + x / 128] |= 1u << slice;
+        }
+    const tmat4<float> m = tmat4<float>::from(inv_vp16);
+    auto slice_to_z = [&](int sl) { return sl == 0 ? 0.05f : -std::pow(2.0f, float(sl + 3) / scale); };
+    for (int t = 0; t < tx * ty; ++t)
+        for (int sl = 0; sl < 16; ++sl) {
+            if (!((used[t] >> sl) & 1u)) continue;
+            const int cx = t % tx, cy = t / tx;
+            const float zF = slice_to_z(sl), zB = slice_to_z(sl + 1);
+            const float L = float(cx) * 128.0f / float(w), R = float(cx + 1) * 128.0f / float(w);
+            const float Bo = float(cy) * 128.0f / float(h), To = float(cy + 1) * 128.0f / float(h);
+            const float F = log_depth(zF), K = log_depth(zB);
+            const float cs[8][3] = {{L, Bo, F}, {L, Bo, K}, {R, Bo, F}, {R, Bo, K}, {L, To, F}, {L, To, K}, {L, To, F}, {L, To, K}};
+            V3<float> corner[8];
+            for (int i = 0; i < 8; ++i) {
+                V4<float> v(cs[i][0], cs[i][1], cs[i][2], 1.0f);
+                v = v * 2.0f - V4<float>(1.0f, 1.0f, 1.0f, 1.0f);
+                v = m * v;
+                corner[i] = V3<float>(v.x, v.y, v.z) / v.w;
+            }
+            uint32_t* row = masks + ((size_t)t * 16 + sl) * words;
+            std::fill(row, row + words, 0u);
+            for (int vi = 0; vi < n_vpl; ++vi) {
+                const V3<float> p(vpos[3 * vi], vpos[3 * vi + 1], vpos[3 * vi + 2]);
+                const V3<float> n = unpack3SN<float>(vpn_bits[vi]);
+                bool found = false;
+                for (int j = 0; j < 8; ++j) found = found || (dot(corner[j] - p, n) >= 0.0f);
+                if (found) row[vi >> 5] |= 1u << (vi & 31);
+            }
+        }
 }
 
 // deferredshading.frag:39-44, 69-80 (GI ambient + the caller's direct term, Reinhard, toSRGB with
@@ -831,6 +888,23 @@ void oracle_unpack_r11g11b10f(const uint32_t* words, float* rgb, int64_t n) {
 void oracle_gi_blur(int w, int h, const float* depth, const float* nrm_oct, const void* gi_in, int packed, float A,
                     float B, void* gi_out, int threads) {
     gi_blur_ref(w, h, depth, nrm_oct, gi_in, packed, A, B, gi_out, threads);
+}
+void oracle_cluster_lights(int w, int h, const float* depth, const float* inv_vp, float A, float B, float zfar,
+                           const float* vpos, const uint32_t* vpn_bits, int n_vpl, uint32_t* used, uint32_t* masks,
+                           uint8_t* pixel_slice) {
+    cluster_lights_ref(w, h, depth, inv_vp, A, B, zfar, vpos, vpn_bits, n_vpl, used, masks, pixel_slice);
+}
+void oracle_final_gather_f64_clustered(int w, int h, const float* depth, const float* nrm_oct, const double* inv_vp,
+                                       int n_vpl, int vpl_count, int ism_off, const double* vpos, const double* vnrm,
+                                       const double* vcol, const float* atlas, int aw, int ah, int gx, int gy,
+                                       double zfar, double gi, double clampv, int interleave, int shadowing,
+                                       const uint32_t* cl_masks, const uint8_t* cl_slice, double* out, int threads) {
+    FgParams p = make_fg(w, h, n_vpl, vpl_count, ism_off, interleave, shadowing, gx, gy, aw, ah, 0, 0.0);
+    p.cl_masks = cl_masks;
+    p.cl_slice = cl_slice;
+    p.cl_tiles_x = (w + 127) / 128;
+    p.cl_words = (n_vpl + 31) / 32;
+    final_gather<double>(p, depth, nrm_oct, inv_vp, vpos, vnrm, vcol, atlas, zfar, gi, clampv, out, threads);
 }
 void oracle_composite(int w, int h, const void* gi, int packed, const uint32_t* albedo, const float* occ,
                       const float* direct, float exposure, float* out_rgb, uint32_t* out_rgba8) {

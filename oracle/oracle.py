@@ -29,8 +29,17 @@ def lib() -> C.CDLL:
     return _lib
 
 
+class _Arg:
+    """A pointer argument that holds its array: ctypes passes `_as_parameter_`, and the array lives
+    as long as the call's argument list, also when it is a temporary conversion."""
+
+    def __init__(self, a):
+        self.a = a
+        self._as_parameter_ = C.c_void_p(0 if a is None else a.ctypes.data)
+
+
 def _p(a):
-    return C.c_void_p(0 if a is None else a.ctypes.data)
+    return _Arg(a)
 
 
 def _f(t):
@@ -118,9 +127,10 @@ def final_gather(depth, normal_oct, inv_vp, vpl_pos, vpl_nrm, vpl_col, atlas, is
     fn = lib().oracle_final_gather_f32 if dtype == np.float32 else lib().oracle_final_gather_f64
     if accurate_world and dtype == np.float32:
         fn = lib().oracle_final_gather_f32_accurate_world
-    fn(w, h, _p(np.ascontiguousarray(depth, np.float32)), _p(np.ascontiguousarray(normal_oct, np.float32)), _p(m), n,
-       vpl_count, ism_offset, _p(np.ascontiguousarray(vpl_pos, dtype)), _p(np.ascontiguousarray(vpl_nrm, dtype)),
-       _p(np.ascontiguousarray(vpl_col, dtype)), _p(np.ascontiguousarray(atlas, np.float32)), aw, ah, grid_x, grid_y,
+    d, nm = np.ascontiguousarray(depth, np.float32), np.ascontiguousarray(normal_oct, np.float32)
+    vp, vn = np.ascontiguousarray(vpl_pos, dtype), np.ascontiguousarray(vpl_nrm, dtype)
+    vc, at = np.ascontiguousarray(vpl_col, dtype), np.ascontiguousarray(atlas, np.float32)
+    fn(w, h, _p(d), _p(nm), _p(m), n, vpl_count, ism_offset, _p(vp), _p(vn), _p(vc), _p(at), aw, ah, grid_x, grid_y,
        _f(dtype)(z_far), _f(dtype)(gi_intensity), _f(dtype)(clamp_value), interleave, shadowing, tile,
        C.c_double(cutoff), _p(out), threads)
     return out
@@ -190,3 +200,42 @@ def composite(gi, albedo, exposure, occlusion=None, direct=None, packed=False):
     lib().oracle_composite(w, h, _p(g), int(packed), _p(albedo), _p(occ), _p(d), C.c_float(exposure), _p(rgb),
                            _p(words))
     return rgb, words
+
+
+def cluster_lights(depth, inv_vp, proj_a, proj_b, z_far, vpl_pos, vpl_pn, n_vpl):
+    """clustering.comp + light_lists.comp: (used [tiles] uint32, masks [tiles*16, words] uint32,
+    pixel_slice [H, W] uint8)."""
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    tiles = ((w + 127) // 128) * ((h + 127) // 128)
+    words = (n_vpl + 31) // 32
+    used = np.zeros(tiles, np.uint32)
+    masks = np.zeros((tiles * 16, words), np.uint32)
+    sl = np.zeros((h, w), np.uint8)
+    m = np.ascontiguousarray(np.asarray(inv_vp, np.float32).reshape(16))
+    vp = np.ascontiguousarray(vpl_pos, np.float32)
+    vn = np.ascontiguousarray(vpl_pn, np.uint32)
+    lib().oracle_cluster_lights(w, h, _p(depth), _p(m), C.c_float(proj_a), C.c_float(proj_b), C.c_float(z_far),
+                                _p(vp), _p(vn), n_vpl, _p(used), _p(masks), _p(sl))
+    return used, masks, sl
+
+
+def final_gather_clustered(depth, normal_oct, inv_vp, vpl_pos, vpl_nrm, vpl_col, atlas, ism_size, grid_x, grid_y,
+                           z_far, gi_intensity, clamp_value, interleave, masks, pixel_slice, shadowing=True,
+                           threads=0):
+    """final_gathering.comp in FP64 with each pixel restricted to its cluster's VPL mask."""
+    h, w = depth.shape
+    n = len(vpl_pos)
+    out = np.zeros((h, w, 3), np.float64)
+    # every converted array is bound to a name, so that it outlives the call
+    keep = [np.ascontiguousarray(depth, np.float32), np.ascontiguousarray(normal_oct, np.float32),
+            np.ascontiguousarray(np.asarray(inv_vp, np.float64).reshape(16)), np.ascontiguousarray(vpl_pos, np.float64),
+            np.ascontiguousarray(vpl_nrm, np.float64), np.ascontiguousarray(vpl_col, np.float64),
+            np.ascontiguousarray(atlas, np.float32), np.ascontiguousarray(masks, np.uint32),
+            np.ascontiguousarray(pixel_slice, np.uint8)]
+    d, nm, m, vp, vn, vc, at, mk, sl = keep
+    lib().oracle_final_gather_f64_clustered(
+        w, h, _p(d), _p(nm), _p(m), n, n, 0, _p(vp), _p(vn), _p(vc), _p(at), at.shape[1], at.shape[0], grid_x, grid_y,
+        C.c_double(z_far), C.c_double(gi_intensity), C.c_double(clamp_value), interleave, int(shadowing), _p(mk), _p(sl),
+        _p(out), threads)
+    return out

@@ -35,7 +35,7 @@ STRUCTS = {"mlgi_ctx_desc": "CtxDesc", "mlgi_rsm_view": "RsmView", "mlgi_vpl_par
            "mlgi_scene_desc": "SceneDesc", "mlgi_scene_info": "SceneInfo", "mlgi_server_desc": "ServerDesc",
            "mlgi_request": "Request", "mlgi_completion": "Completion", "mlgi_server_stats": "ServerStats",
            "mlgi_poisson_desc": "PoissonDesc", "mlgi_batch_opts": "BatchOpts", "mlgi_blur_params": "BlurParams",
-           "mlgi_composite_params": "CompositeParams"}
+           "mlgi_composite_params": "CompositeParams", "mlgi_cluster_params": "ClusterParams"}
 
 
 def test_struct_layouts_match_the_header(tmp_path):
