@@ -116,7 +116,8 @@ __device__ __forceinline__ float pow2_recip(int x) {
 // points [chunk * kSplatChunk, (chunk + 1) * kSplatChunk), the last chunk up to the bucket's count
 // (one block each).
 __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item, SplatSmem& S) {
-    const int wg = item / a.chunks, chunk = item - wg * a.chunks;
+    const int local = item / a.chunks, chunk = item - local * a.chunks;
+    const int wg = a.bucket0 + local;
     __syncthreads();  // the previous bucket's use of S is over
     const int vplCount = a.vpl_end - a.vpl_start;
     if (a.points_only_scaled && wg > vplCount) return;

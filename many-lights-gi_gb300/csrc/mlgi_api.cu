@@ -28,7 +28,11 @@ enum Pass { kVplp = 0, kIsmClear, kIsmCs, kPullPush, kFg, kH2D, kD2H, kNumPasses
 enum SubPass { kPull1 = kNumPasses, kPullMid, kPush1, kPush0, kNumTimings };
 // Event slots: ev[k]..ev[k+1] bracket device pass k (k <= kFg); two extra slots bracket the
 // host-frame copies.
-constexpr int kEvH2DStart = kNumPasses + 1, kEvD2HEnd = kNumPasses + 2, kNumEvents = kNumPasses + 3;
+constexpr int kEvH2DStart = kNumPasses + 1, kEvD2HEnd = kNumPasses + 2, kEvH2DEnd = kNumPasses + 3,
+              kNumEvents = kNumPasses + 4;
+// The host-buffer frame uploads the points in up to this many bucket ranges, each splatted as soon
+// as it has arrived.
+constexpr int kHostPointChunks = 4;
 
 }  // namespace
 
@@ -49,6 +53,9 @@ struct mlgi_ctx {
     bool timed_frame = false;
     cudaEvent_t ev[kNumEvents] = {};
     cudaEvent_t ev_pp[3] = {};  // inside the pull-push pass
+    // host-buffer frames: the upload stream and its events (RSM, point ranges, G-buffer)
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_rsm = nullptr, ev_gbuf = nullptr, ev_pts[kHostPointChunks] = {};
     float last_ms[kNumTimings] = {};
 };
 
@@ -178,6 +185,11 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
     if (e == cudaSuccess) e = cudaMemset(ctx->status, 0, sizeof(uint32_t));
     for (int i = 0; e == cudaSuccess && i < kNumEvents; ++i) e = cudaEventCreate(&ctx->ev[i]);
     for (int i = 0; e == cudaSuccess && i < 3; ++i) e = cudaEventCreate(&ctx->ev_pp[i]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_rsm, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_gbuf, cudaEventDisableTiming);
+    for (int i = 0; e == cudaSuccess && i < kHostPointChunks; ++i)
+        e = cudaEventCreateWithFlags(&ctx->ev_pts[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         mlgi_destroy(ctx);
@@ -200,6 +212,14 @@ void mlgi_destroy(mlgi_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->ev_pp)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ctx->ev_rsm, ctx->ev_gbuf})
+        if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->ev_pts)
+        if (e) cudaEventDestroy(e);
+    if (ctx->copy) {
+        cudaStreamSynchronize(ctx->copy);
+        cudaStreamDestroy(ctx->copy);
+    }
     if (ctx->status) cudaFree(ctx->status);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -594,7 +614,7 @@ mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n) {
         for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&ctx->last_ms[kPull1 + k], pp[k], pp[k + 1]);
         if (ctx->timed_host_frame) {
             MLGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[kEvD2HEnd]));
-            cudaEventElapsedTime(&ctx->last_ms[kH2D], ctx->ev[kEvH2DStart], ctx->ev[kVplp]);
+            cudaEventElapsedTime(&ctx->last_ms[kH2D], ctx->ev[kEvH2DStart], ctx->ev[kEvH2DEnd]);
             cudaEventElapsedTime(&ctx->last_ms[kD2H], ctx->ev[kFg + 1], ctx->ev[kEvD2HEnd]);
         }
     }
@@ -671,13 +691,12 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
                           f->gbuffer.depth, f->gbuffer.normal, nullptr};
     for (int i = 0; i < 8 && st == MLGI_OK; ++i) st = ensure(ctx, *bufs[i], std::max<size_t>(sizes[i], 16));
     if (st != MLGI_OK) return st;
-    cudaStream_t s = ctx->stream;
-    mark(ctx, kEvH2DStart, s);
-    for (int i = 0; i < 7; ++i) {
-        if (!sizes[i]) continue;
-        if (!srcs[i]) return fail(ctx, MLGI_EINVAL, "host input %d is NULL", i);
-        MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, s));
-    }
+    for (int i = 0; i < 7; ++i)
+        if (sizes[i] && !srcs[i]) return fail(ctx, MLGI_EINVAL, "host input %d is NULL", i);
+    // Uploads on the copy stream in the order the passes need them; the compute stream waits for
+    // each input just before its first reader, so the splat of a point range runs while the next
+    // range and the G-buffer are still arriving (atomicMin does not depend on the order).
+    cudaStream_t s = ctx->stream, c = ctx->copy;
     mlgi_frame_desc d = *f;
     d.rsm.depth = static_cast<const float*>(ctx->h_rsm_depth.p);
     d.rsm.normal = static_cast<const uint32_t*>(ctx->h_rsm_normal.p);
@@ -687,11 +706,66 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     d.gbuffer.depth = static_cast<const float*>(ctx->h_gdepth.p);
     d.gbuffer.normal = ctx->h_gnormal.p;
     mlgi_radiance out{f->gbuffer.width, f->gbuffer.height, static_cast<float*>(ctx->h_rgb.p)};
+    const int nb = f->points.n_buckets;
+    const int nchunks = std::max(1, std::min(kHostPointChunks, nb));
+    const size_t bucket_bytes = (size_t)f->points.bucket_stride * 16;
+    mark(ctx, kEvH2DStart, c);
+    for (int i = 0; i < 3; ++i)
+        if (sizes[i]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, c));
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_rsm, c));
+    if (sizes[4]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[4]->p, srcs[4], sizes[4], cudaMemcpyHostToDevice, c));
+    for (int k = 0; k < nchunks; ++k) {
+        const size_t b0 = (size_t)nb * k / nchunks, b1 = (size_t)nb * (k + 1) / nchunks;
+        if (b1 > b0 && bucket_bytes)
+            MLGI_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(bufs[3]->p) + b0 * bucket_bytes,
+                                           static_cast<const char*>(srcs[3]) + b0 * bucket_bytes,
+                                           (b1 - b0) * bucket_bytes, cudaMemcpyHostToDevice, c));
+        MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pts[k], c));
+    }
+    for (int i = 5; i < 7; ++i)
+        if (sizes[i]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, c));
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_gbuf, c));
+    mark(ctx, kEvH2DEnd, c);
+
+    // compute: the chain of run_frame with the waits placed at the first reader of each input
+    const int n = d.vpl.count;
+    st = ensure(ctx, ctx->vpl, (size_t)n * 48);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->packed, (size_t)n * 16);
+    const bool reduced = d.fg.vpl_format == MLGI_F16;
+    if (st == MLGI_OK && reduced) st = ensure(ctx, ctx->reduced, (size_t)n * 24);
+    const int aw = d.ism.grid_x * d.ism.ism_size, ah = d.ism.grid_y * d.ism.ism_size;
+    if (st == MLGI_OK) st = ensure(ctx, ctx->keys, (size_t)aw * ah * 4);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->depth, (size_t)aw * ah * (d.atlas_format == MLGI_F16 ? 2 : 4));
+    if (st != MLGI_OK) return st;
+    mlgi_vpl_buf vb{n, static_cast<float*>(ctx->vpl.p), static_cast<float*>(ctx->packed.p),
+                    reduced ? ctx->reduced.p : nullptr};
+    mlgi_atlas atlas{aw, ah, static_cast<uint32_t*>(ctx->keys.p), ctx->depth.p, d.atlas_format};
+    mlgi::SplatArgs sa;
+    if ((st = build_splat_args(ctx, &d.points, &vb, n, &d.ism, &atlas, sa)) != MLGI_OK) return st;
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_rsm, 0));
     mark(ctx, kVplp, s);
-    if ((st = run_frame(ctx, &d, &out, s)) != MLGI_OK) return st;
+    if ((st = mlgi_vpl_process(ctx, &d.rsm, &d.vpl, &vb, s)) != MLGI_OK) return st;
+    mark(ctx, kIsmClear, s);
+    MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas.keys, (size_t)aw * ah, s));
+    mark(ctx, kIsmCs, s);
+    for (int k = 0; k < nchunks; ++k) {
+        const int b0 = (int)((size_t)nb * k / nchunks), b1 = (int)((size_t)nb * (k + 1) / nchunks);
+        MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_pts[k], 0));
+        mlgi::SplatArgs part = sa;
+        part.bucket0 = b0;
+        part.n_groups = b1 - b0;
+        MLGI_CUDA(ctx, mlgi::launch_ism_splat(part, s));
+    }
+    mark(ctx, kPullPush, s);
+    if ((st = mlgi_pullpush(ctx, &atlas, &d.ism, s)) != MLGI_OK) return st;
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_gbuf, 0));
+    mark(ctx, kFg, s);
+    if ((st = mlgi_final_gather(ctx, &d.gbuffer, &vb, &atlas, &d.fg, &out, s)) != MLGI_OK) return st;
+    mark(ctx, kFg + 1, s);
     MLGI_CUDA(ctx, cudaMemcpyAsync(rgb_host, out.rgb, z.radiance, cudaMemcpyDeviceToHost, s));
     mark(ctx, kEvD2HEnd, s);
     MLGI_CUDA(ctx, cudaStreamSynchronize(s));
+    MLGI_CUDA(ctx, cudaStreamSynchronize(c));
     ctx->timed_frame = ctx->timed_host_frame = ctx->timing;
     return mlgi_check_device_status(ctx, s);
 }
