@@ -363,7 +363,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
     ctx.gi_frame_host(hfd, rgb_host)
     t = ctx.last_timings()
     ctx.set_timing(False)
-    e2e_passes = {"h2d_ms": float(t[5]), "d2h_ms": float(t[6])}
+    e2e_passes = {"h2d_ms": float(t[5]), "d2h_tail_ms": float(t[6])}
     sizes = mlgi.FrameHostSizes()
     mlgi.lib().mlgi_frame_host_sizes_get(mlgi.C.byref(hfd), mlgi.C.byref(sizes))
     h2d = sizes.rsm_depth + sizes.rsm_normal + sizes.rsm_diffuse + sizes.points + sizes.counts + \
@@ -404,9 +404,10 @@ def run_gpu(args, cfg, rank, world, local_rank):
         "e2e": {"value": e2e_total / frames, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), **e2e_passes,
                 "h2d_gbs": h2d / (e2e_passes["h2d_ms"] * 1e-3) / 1e9 if e2e_passes["h2d_ms"] > 0 else None,
-                "d2h_gbs": d2h / (e2e_passes["d2h_ms"] * 1e-3) / 1e9 if e2e_passes["d2h_ms"] > 0 else None,
-                "note": "uploads on a copy stream in the order the passes read them; each point range "
-                        "is splatted while the next arrives"},
+                "note": "uploads on a copy stream in the order the passes read them; each point range is "
+                        "splatted, and the ISM rows it completes pulled and pushed, while the next arrives; "
+                        "the gathering runs in bands of rows, each downloaded while the next is gathered "
+                        "(d2h_tail_ms: download time left after the last band)"},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": ab[dom_name], "traffic": traffic,

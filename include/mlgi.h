@@ -138,6 +138,27 @@ mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl
  * atlas->depth. Bit-exact with the reference's FP32 arithmetic for the FP32 format. */
 mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* params, mlgi_stream stream);
 
+/* No counterpart in the reference: the pieces of mlgi_ism_splat + mlgi_pullpush for callers that
+ * overlap them with their own uploads (mlgi_gi_frame_host does).
+ *   mlgi_ism_clear        the key clear of mlgi_ism_splat.
+ *   mlgi_ism_splat_range  the splat of buckets [bucket0, bucket0 + n_buckets) only, no clear.
+ *                         After one clear, splatting every bucket once, in any partition and
+ *                         order, gives mlgi_ism_splat's keys (atomicMin is order-independent).
+ *   mlgi_pullpush_rows    the pull-push of ISM rows [row0, row1) of the grid. The pyramid of an
+ *                         ISM reads only its own keys, so running every row once, in any
+ *                         partition, gives mlgi_pullpush's atlas; runs of different rows may
+ *                         execute concurrently on different streams. A row's keys are final once
+ *                         every bucket that splats into the row or into a row next to it is done:
+ *                         bucket b splats into the ISMs of VPLs b..b+15 (mod N), and rounding at
+ *                         a paraboloid's rim can put a point on the border texels of a
+ *                         neighbouring ISM; a point on a VPL's position lands on texel (0, 0). */
+mlgi_status mlgi_ism_clear(mlgi_ctx* ctx, mlgi_atlas* atlas, mlgi_stream stream);
+mlgi_status mlgi_ism_splat_range(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                                 const mlgi_ism_params* params, mlgi_atlas* atlas, int bucket0, int n_buckets,
+                                 mlgi_stream stream);
+mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* params, int row0, int row1,
+                               mlgi_stream stream);
+
 /* No counterpart in the reference. Allocation-free ISM rendering for callers that cannot
  * allocate device memory (their device memory is reserved up front by another allocator, or
  * they run in a plugin or callback that is only handed pre-allocated buffers): clears, splats
@@ -438,14 +459,21 @@ mlgi_status mlgi_frame_host_sizes_get(const mlgi_frame_desc* frame, mlgi_frame_h
 
 /* The same chain from HOST buffers: every pointer in `frame` is a host pointer; the call copies
  * the inputs to context-owned device buffers, runs the chain and copies the radiance back to
- * `rgb_host` before returning. */
+ * `rgb_host` before returning. Copies overlap the passes: point bucket ranges are splatted as they
+ * arrive, the ISM rows a range completes are pulled and pushed before the next range, and the
+ * gathering runs in bands of rows whose radiance is copied back while the next band runs. The
+ * result equals mlgi_gi_frame's bit for bit. Pinned host memory gives the full copy bandwidth. */
 mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* frame, float* rgb_host);
 
 /* Per-pass device times (ms) of the last mlgi_gi_frame / mlgi_gi_frame_host call when timing is
  * enabled, named after the reference's PerfCounter passes:
  * [0] VPLP, [1] ISM clear, [2] ISM CS (splat), [3] pull-push, [4] FG, [5] H2D, [6] D2H, then the
  * pull-push pass's launches: [7] pull level 1, [8] middle levels, [9] push level 1, [10] push level 0.
- * Reading them synchronises the context's stream. */
+ * After mlgi_gi_frame_host the passes overlap the copies: [2] spans the splat of every point range,
+ * [3] the pull-push of the ISM rows finished by the last range (rows finished earlier run on a
+ * second stream during [2]), [4] the banded gathering, [5] the whole upload, [6] the part of the
+ * download left after the last band, and [7..10] are 0. Reading them synchronises the context's
+ * stream. */
 mlgi_status mlgi_set_timing(mlgi_ctx* ctx, int enabled);
 mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n);
 

@@ -418,14 +418,20 @@ __global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
     __shared__ FgSmem<T * T> S;
     if (threadIdx.x == 0) mbar_init(&S.bar, 1);
     uint32_t parity = 0;
-    fg_tile<T, kReduced, kAtlasF16, kNormalF16>(a, blockIdx.x, blockIdx.y, S, parity);
+    fg_tile<T, kReduced, kAtlasF16, kNormalF16>(a, a.tile0 + blockIdx.x, blockIdx.y, S, parity);
 }
 
+// Tile rows [tr0, tr1): tiles are numbered row by row, so a band of tile rows is a contiguous
+// range of tile indices starting at tile0.
 template <int T>
-static cudaError_t launch_fg_t(const FgArgs& a, cudaStream_t s) {
-    const int I = a.interleave;
-    const int sw = (a.width + I - 1) / I, sh = (a.height + I - 1) / I;
-    const dim3 grid(((sw + T - 1) / T) * ((sh + T - 1) / T), I * I);
+static cudaError_t launch_fg_t(const FgArgs& args, cudaStream_t s, int tr0, int tr1) {
+    const int I = args.interleave;
+    const int sw = (args.width + I - 1) / I;
+    const int ntx = (sw + T - 1) / T;
+    if (tr1 <= tr0) return cudaSuccess;
+    FgArgs a = args;
+    a.tile0 = tr0 * ntx;
+    const dim3 grid(ntx * (tr1 - tr0), I * I);
     const int sel = (a.reduced ? 4 : 0) | (a.atlas_f16 ? 2 : 0) | (a.normal_f16 ? 1 : 0);
     switch (sel) {
         case 0: fg_kernel<T, false, false, false><<<grid, T * T, 0, s>>>(a); break;
@@ -440,10 +446,12 @@ static cudaError_t launch_fg_t(const FgArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s) {
+cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s, int tile_row0, int tile_row1) {
     if (a.width <= 0 || a.height <= 0) return cudaSuccess;
-    if (a.tile == 8) return launch_fg_t<8>(a, s);
-    return launch_fg_t<16>(a, s);
+    const int rows = fg_tile_rows(a);
+    const int tr0 = tile_row0 < 0 ? 0 : tile_row0, tr1 = tile_row1 < 0 || tile_row1 > rows ? rows : tile_row1;
+    if (a.tile == 8) return launch_fg_t<8>(a, s, tr0, tr1);
+    return launch_fg_t<16>(a, s, tr0, tr1);
 }
 
 // Persistent final gathering over a view table (16 x 16 tiles). Views are FP32 or fully reduced.

@@ -575,26 +575,32 @@ __device__ __forceinline__ bool multiple_of(const int x, const int d, const uint
     return d == 1 || x == div_small(x, m) * d;
 }
 
-// Per-texel pass on a kPpTileW x kPpTileH tile (tx, ty) of level 1.
+// Per-texel pass on a kPpTileW x kPpTileH tile (tx, ty) of level 1, tile rows counted from the
+// launch's first ISM row.
 __device__ __forceinline__ void pull1_tile(const PullPushArgs& a, const int tx, const int ty, const float* s_rad,
                                            const float* s_mdo) {
-    const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = ty * kPpTileH + (threadIdx.x / kPpTileW);
-    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
-    if (x < w1 && y < h1) a.lv1[(uint32_t)y * w1 + x] = pull1_texel(a, s_rad, s_mdo, x, y);
+    const int s1 = a.ism_size >> 1;
+    const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = a.row0 * s1 + ty * kPpTileH + (threadIdx.x / kPpTileW);
+    const int w1 = a.atlas_w >> 1;
+    if (x < w1 && y < a.row1 * s1) a.lv1[(uint32_t)y * w1 + x] = pull1_texel(a, s_rad, s_mdo, x, y);
 }
 
 // Quad passes on a kPpTileW x kPpTileH tile (tx, ty) of quads: level l has (w_l / 2 + 1) x
-// (h_l / 2 + 1) quads.
+// (h_l / 2 + 1) quads. A launch over ISM rows [row0, row1) writes the level's rows [Y0, Y1) =
+// [row0, row1) * edge, from quad rows Y0 / 2 .. Y1 / 2 (quad gy writes rows 2 gy - 1 and 2 gy);
+// a quad on the range's border also reads coarse texels of the neighbouring ISM row, with weight
+// 0 for the outputs written here, so their values do not matter.
 __device__ __forceinline__ void push1_quads(const PullPushArgs& a, const int tx, const int ty) {
-    const int gx = tx * kPpTileW + (threadIdx.x % kPpTileW), gy = ty * kPpTileH + (threadIdx.x / kPpTileW);
     const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1, w2 = a.atlas_w >> 2, h2 = a.atlas_h >> 2;
-    if (gx > w2 || gy > h2) return;
+    const int s1 = a.ism_size >> 1, Y0 = a.row0 * s1, Y1 = a.row1 * s1;
+    const int gx = tx * kPpTileW + (threadIdx.x % kPpTileW), gy = (Y0 >> 1) + ty * kPpTileH + (threadIdx.x / kPpTileW);
+    if (gx > w2 || gy > (Y1 >> 1)) return;
     const int sc = a.ism_size >> 2;  // ISM edge at level 2
     PushCoarse C;
     push_coarse(a.lv2, w2, w2, h2, gx, gy, 0.5f, C);
     const bool bx = multiple_of(gx, sc, a.m_c1), by = multiple_of(gy, sc, a.m_c1);
     const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
-    const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w1, oky0 = y0 >= 0, oky1 = y0 + 1 < h1;
+    const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w1, oky0 = y0 >= Y0, oky1 = y0 + 1 < Y1;
     float4* row0 = a.lv1 + (uint32_t)max(y0, 0) * w1;  // only used when oky0
     float4* row1 = a.lv1 + (uint32_t)min(y0 + 1, h1 - 1) * w1;  // only used when oky1
     if (oky0 && okx0) row0[x0] = push_output<true, 0, 0>(C, bx, by, row0[x0]);
@@ -615,15 +621,16 @@ __device__ __forceinline__ float key_depth(const PullPushArgs& a, const uint32_t
 }
 
 __device__ __forceinline__ void push0_quads(const PullPushArgs& a, const int tx, const int ty) {
-    const int gx = tx * kPpTileW + (threadIdx.x % kPpTileW), gy = ty * kPpTileH + (threadIdx.x / kPpTileW);
     const int w = a.atlas_w, h = a.atlas_h, w1 = w >> 1, h1 = h >> 1;
-    if (gx > w1 || gy > h1) return;
+    const int Y0 = a.row0 * a.ism_size, Y1 = a.row1 * a.ism_size;
+    const int gx = tx * kPpTileW + (threadIdx.x % kPpTileW), gy = (Y0 >> 1) + ty * kPpTileH + (threadIdx.x / kPpTileW);
+    if (gx > w1 || gy > (Y1 >> 1)) return;
     const int sc = a.ism_size >> 1;  // ISM edge at level 1
     PushCoarse C;
     push_coarse(a.lv1, w1, w1, h1, gx, gy, 1.0f, C);
     const bool bx = multiple_of(gx, sc, a.m_c0), by = multiple_of(gy, sc, a.m_c0);
     const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
-    const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w, oky0 = y0 >= 0, oky1 = y0 + 1 < h;
+    const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w, oky0 = y0 >= Y0, oky1 = y0 + 1 < Y1;
     const uint32_t r0 = (uint32_t)y0 * w, r1 = (uint32_t)(y0 + 1) * w;
     // level 0 writes only the depth channel (push.comp:33-37)
     if (oky0 && okx0)
@@ -699,16 +706,21 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) pull1_kernel(PullPushArgs
     pull1_tile(a, blockIdx.x, blockIdx.y, s_tab, s_tab + 256);
 }
 
-__global__ void __launch_bounds__(kPullMidThreads) pullmid_kernel(PullPushArgs a) {
+// NT threads per ISM: kPullMidThreads when the launch fills the GPU with ISM blocks, more when a
+// launch over a few ISM rows would leave most SMs idle (the pass is then bound by one block's time).
+template <int NT>
+__global__ void __launch_bounds__(NT) pullmid_kernel(PullPushArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    pullmid_ism(a, blockIdx.x, smem);
+    pullmid_ism(a, a.row0 * a.grid_x + blockIdx.x, smem);
 }
+constexpr int kPullMidWideThreads = 512;
+constexpr int kPullMidWideBelow = 2 * 152;  // ISMs per launch under which the wide form is used
 
 __global__ void __launch_bounds__(kPpTileW * kPpTileH) push1_kernel(PullPushArgs a) {
     push1_quads(a, blockIdx.x, blockIdx.y);
 }
 
-__global__ void __launch_bounds__(kPpTileW * kPpTileH) push0_kernel(PullPushArgs a) {
+__global__ void __launch_bounds__(kPpTileW * kPpTileH, 5) push0_kernel(PullPushArgs a) {
     push0_quads(a, blockIdx.x, blockIdx.y);
 }
 
@@ -731,40 +743,65 @@ __host__ __device__ __forceinline__ int tiles_y(int h) { return (h + kPpTileH - 
 __host__ __device__ __forceinline__ int row_items(int w) { return (tiles_x(w) + kPpBatchTiles - 1) / kPpBatchTiles; }
 
 cudaError_t pullpush_prepare(size_t smem) {
-    return cudaFuncSetAttribute(pullmid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(pullmid_kernel<kPullMidThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(pullmid_kernel<kPullMidWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e;
+}
+
+static void launch_pullmid(const PullPushArgs& a, int isms, size_t smem, cudaStream_t s) {
+    if (isms < kPullMidWideBelow)
+        pullmid_kernel<kPullMidWideThreads><<<isms, kPullMidWideThreads, smem, s>>>(a);
+    else
+        pullmid_kernel<kPullMidThreads><<<isms, kPullMidThreads, smem, s>>>(a);
+}
+
+// Grids of the four launches over ISM rows [a.row0, a.row1).
+struct PullPushGrids {
+    dim3 g1, q1, q0;
+    int isms;
+};
+
+static PullPushGrids pullpush_grids(const PullPushArgs& a) {
+    const int w1 = a.atlas_w >> 1, rows = a.row1 - a.row0;
+    const int s1 = a.ism_size >> 1, s0 = a.ism_size;
+    PullPushGrids g;
+    g.g1 = dim3(tiles_x(w1), tiles_y(rows * s1));
+    g.q1 = dim3(tiles_x(w1 / 2 + 1), tiles_y(((a.row1 * s1) >> 1) - ((a.row0 * s1) >> 1) + 1));
+    g.q0 = dim3(tiles_x(w1 + 1), tiles_y(((a.row1 * s0) >> 1) - ((a.row0 * s0) >> 1) + 1));
+    g.isms = rows * a.grid_x;
+    return g;
 }
 
 cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
-    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
-    const dim3 g1(tiles_x(w1), tiles_y(h1));
-    const dim3 q1(tiles_x(w1 / 2 + 1), tiles_y(h1 / 2 + 1)), q0(tiles_x(w1 + 1), tiles_y(h1 + 1));
-    pull1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    if (a.row1 <= a.row0) return cudaSuccess;
+    const PullPushGrids g = pullpush_grids(a);
+    pull1_kernel<<<g.g1, kPpTileW * kPpTileH, 0, s>>>(a);
     if (a.levels >= 2) {
-        pullmid_kernel<<<a.grid_x * a.grid_y, kPullMidThreads, pullmid_smem_bytes(a.ism_size, a.levels), s>>>(a);
-        push1_kernel<<<q1, kPpTileW * kPpTileH, 0, s>>>(a);
+        launch_pullmid(a, g.isms, pullmid_smem_bytes(a.ism_size, a.levels), s);
+        push1_kernel<<<g.q1, kPpTileW * kPpTileH, 0, s>>>(a);
     }
-    push0_kernel<<<q0, kPpTileW * kPpTileH, 0, s>>>(a);
+    push0_kernel<<<g.q0, kPpTileW * kPpTileH, 0, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks) {
-    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1;
-    const dim3 g1(tiles_x(w1), tiles_y(h1));
-    const dim3 q1(tiles_x(w1 / 2 + 1), tiles_y(h1 / 2 + 1)), q0(tiles_x(w1 + 1), tiles_y(h1 + 1));
-    pull1_kernel<<<g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    if (a.row1 <= a.row0) return cudaSuccess;
+    const PullPushGrids g = pullpush_grids(a);
+    pull1_kernel<<<g.g1, kPpTileW * kPpTileH, 0, s>>>(a);
     if (marks) cudaEventRecord(marks[0], s);
     if (a.levels >= 2) {
         const size_t smem = pullmid_smem_bytes(a.ism_size, a.levels);
-        cudaError_t e = cudaFuncSetAttribute(pullmid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = pullpush_prepare(smem);
         if (e != cudaSuccess) return e;
-        pullmid_kernel<<<a.grid_x * a.grid_y, kPullMidThreads, smem, s>>>(a);
+        launch_pullmid(a, g.isms, smem, s);
         if (marks) cudaEventRecord(marks[1], s);
-        push1_kernel<<<q1, kPpTileW * kPpTileH, 0, s>>>(a);
+        push1_kernel<<<g.q1, kPpTileW * kPpTileH, 0, s>>>(a);
     } else if (marks) {
         cudaEventRecord(marks[1], s);
     }
     if (marks) cudaEventRecord(marks[2], s);
-    push0_kernel<<<q0, kPpTileW * kPpTileH, 0, s>>>(a);
+    push0_kernel<<<g.q0, kPpTileW * kPpTileH, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -135,6 +135,8 @@ extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi
     q.m_c1 = mlgi::small_div_magic(p->ism_size >> 2);
     q.lv1 = static_cast<float4*>(pyramid);
     q.lv2 = p->levels >= 2 ? reinterpret_cast<float4*>(static_cast<char*>(pyramid) + lv2_off) : nullptr;
+    q.row0 = 0;
+    q.row1 = p->grid_y;
     if (mlgi::launch_pullpush(q, s) != cudaSuccess) return MLGI_ECUDA;
     return MLGI_OK;
 }

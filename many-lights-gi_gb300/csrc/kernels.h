@@ -53,6 +53,7 @@ struct PullPushArgs {
     float4* lv1;          // scratch: pyramid level 1, (atlas_w/2) x (atlas_h/2)
     float4* lv2;          // scratch: pyramid level 2, (atlas_w/4) x (atlas_h/4), when levels >= 2
     uint32_t m_c0, m_c1;  // ceil(2^32 / d) for d = ism_size / 2 and ism_size / 4 when d >= 2, else 0
+    int row0, row1;       // the launch covers ISM rows [row0, row1) of the grid (0, grid_y: all)
 };
 
 struct FgArgs {
@@ -85,7 +86,15 @@ struct FgArgs {
     const uint32_t* cl_masks;     // (tiles_x * tiles_y * 16) x cl_words
     const uint8_t* cl_slice;      // per pixel
     int cl_tiles_x, cl_words;
+    int tile0;                    // tile index of the launch's first block column (tile-row bands)
 };
+
+// Tile rows of the gathering (each covers tile * interleave image rows, all interleave classes).
+inline int fg_tile_rows(const FgArgs& a) {
+    const int T = a.tile == 8 ? 8 : 16, sh = (a.height + a.interleave - 1) / a.interleave;
+    return (sh + T - 1) / T;
+}
+inline int fg_rows_per_tile_row(const FgArgs& a) { return (a.tile == 8 ? 8 : 16) * a.interleave; }
 
 // ---- clustered culling (reference style) ---------------------------------------------------
 constexpr int kClusterPixels = 128, kClusterSlices = 16, kClusterSlicesIntoFirst = 3;
@@ -167,7 +176,8 @@ constexpr uint32_t kStatusTmaTimeout = 1u;
 cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s);
 cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s);
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s);
-// marks (optional): three events recorded after level 1, the middle levels and push level 1.
+// The pyramid of ISM rows [a.row0, a.row1). marks (optional): three events recorded after level
+// 1, the middle levels and push level 1.
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks = nullptr);
 // Raise the middle pass's dynamic shared-memory limit to `smem` outside any stream capture; then
 // launch_pullpush_captured issues the same launches as launch_pullpush without that attribute call.
@@ -178,6 +188,7 @@ cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s);
 size_t pullmid_smem_bytes(int ism_size, int levels);
 size_t pullpush_scratch_bytes(int atlas_w, int atlas_h, int levels, size_t* lv2_offset);
 int pullpush_batch_items(int pass, int atlas_w, int atlas_h, int ism_count, int levels);
-cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s);
+// Tile rows [tile_row0, tile_row1) of the gathering (tile_row1 < 0: through the last).
+cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s, int tile_row0 = 0, int tile_row1 = -1);
 
 }  // namespace mlgi

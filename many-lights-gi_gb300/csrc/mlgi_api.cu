@@ -31,8 +31,66 @@ enum SubPass { kPull1 = kNumPasses, kPullMid, kPush1, kPush0, kNumTimings };
 constexpr int kEvH2DStart = kNumPasses + 1, kEvD2HEnd = kNumPasses + 2, kEvH2DEnd = kNumPasses + 3,
               kNumEvents = kNumPasses + 4;
 // The host-buffer frame uploads the points in up to this many bucket ranges, each splatted as soon
-// as it has arrived.
-constexpr int kHostPointChunks = 4;
+// as it has arrived, and gathers and downloads the radiance in up to kHostBands bands of rows.
+constexpr int kHostPointChunks = 4, kHostBands = 8;
+
+// Order of a host frame's point upload and the chunk after whose splat each ISM row is final.
+// Bucket wg splats into the ISMs of VPLs (wg + i) mod N, i < 16 (ism.comp:93-107); a projected
+// point lands in its ISM's tile or, through rounding at the paraboloid's rim (|x|, |y| <= 1 up to a
+// few ulps for every point that passes the hemisphere cull), on the first or last texel line of a
+// neighbouring tile; a point at a VPL's position or a degenerate VPL frame projects to NaN, which
+// converts to texel (0, 0) of ISM 0. So an ISM row is final once every bucket that splats into
+// the row or its 8-neighbourhood has been splatted, and the row of ISM 0 is final only after all.
+// Only the plain layout (ISM i = VPL i, one bucket per VPL) is scheduled this way; any other
+// layout finishes every row after the last chunk.
+struct HostSchedule {
+    int key[9] = {-1};
+    int rot = 0;                 // upload position p carries bucket (rot + p) mod n_buckets
+    int chunks = 1;
+    int pos[kHostPointChunks + 1] = {};  // chunk k covers positions [pos[k], pos[k+1])
+    std::vector<int> row_chunk;  // per ISM row
+};
+
+void host_schedule(HostSchedule& h, const mlgi_frame_desc& f) {
+    const mlgi_ism_params& p = f.ism;
+    const int nb = f.points.n_buckets, n = f.vpl.count, gx = p.grid_x, gy = p.grid_y;
+    const int key[9] = {nb, n, gx, gy, p.vpl_start, p.vpl_end, p.scale_isms, p.points_only_scaled, kHostPointChunks};
+    if (std::equal(key, key + 9, h.key)) return;
+    std::copy(key, key + 9, h.key);
+    // the first chunk half as large as the others, so that the splat starts early
+    h.chunks = std::max(1, std::min(kHostPointChunks, nb));
+    for (int k = 1; k < h.chunks; ++k) h.pos[k] = (int)((int64_t)nb * (2 * k - 1) / (2 * h.chunks - 1));
+    h.pos[0] = 0;
+    h.pos[h.chunks] = nb;
+    const bool plain = nb == n && p.vpl_start == 0 && p.vpl_end == n && n <= gx * gy && nb > 0;
+    h.row_chunk.assign(gy, h.chunks - 1);
+    if (!plain) {
+        h.rot = 0;
+        return;
+    }
+    // start with the buckets whose ISMs wrap around to the first ones
+    h.rot = nb > 16 ? nb - 15 : 0;
+    std::vector<int> last(gx * gy, -1);  // last upload position that splats into each ISM
+    for (int q = 0; q < nb; ++q) {
+        const int b = (h.rot + q) % nb;
+        for (int i = 0; i < 16; ++i) {
+            const int j = (b + i) % n, tx = j % gx, ty = j / gx;
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int x = tx + dx, y = ty + dy;
+                    if (x >= 0 && y >= 0 && x < gx && y < gy) last[y * gx + x] = q;
+                }
+        }
+    }
+    last[0] = nb - 1;
+    for (int r = 0; r < gy; ++r) {
+        int q = -1;
+        for (int x = 0; x < gx; ++x) q = std::max(q, last[r * gx + x]);
+        int k = 0;
+        while (k + 1 < h.chunks && q >= h.pos[k + 1]) ++k;
+        h.row_chunk[r] = k;
+    }
+}
 
 }  // namespace
 
@@ -56,6 +114,11 @@ struct mlgi_ctx {
     // host-buffer frames: the upload stream and its events (RSM, point ranges, G-buffer)
     cudaStream_t copy = nullptr;
     cudaEvent_t ev_rsm = nullptr, ev_gbuf = nullptr, ev_pts[kHostPointChunks] = {};
+    // and the gathering's bands: a second compute stream and one event per band
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_band[kHostBands] = {};
+    cudaEvent_t ev_split[kHostPointChunks] = {}, ev_side = nullptr;  // early pull-push runs on `side`
+    HostSchedule sched;
     float last_ms[kNumTimings] = {};
 };
 
@@ -190,6 +253,13 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_gbuf, cudaEventDisableTiming);
     for (int i = 0; e == cudaSuccess && i < kHostPointChunks; ++i)
         e = cudaEventCreateWithFlags(&ctx->ev_pts[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    for (int i = 0; e == cudaSuccess && i < kHostBands; ++i)
+        e = cudaEventCreateWithFlags(&ctx->ev_band[i], cudaEventDisableTiming);
+    for (int i = 0; e == cudaSuccess && i < kHostPointChunks; ++i)
+        e = cudaEventCreateWithFlags(&ctx->ev_split[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_side, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         mlgi_destroy(ctx);
@@ -216,10 +286,17 @@ void mlgi_destroy(mlgi_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->ev_pts)
         if (e) cudaEventDestroy(e);
-    if (ctx->copy) {
-        cudaStreamSynchronize(ctx->copy);
-        cudaStreamDestroy(ctx->copy);
-    }
+    for (auto& e : ctx->ev_band)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->ev_split)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_side})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t cs : {ctx->copy, ctx->side})
+        if (cs) {
+            cudaStreamSynchronize(cs);
+            cudaStreamDestroy(cs);
+        }
     if (ctx->status) cudaFree(ctx->status);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -351,6 +428,8 @@ mlgi_status build_pullpush_args(mlgi_ctx* ctx, const mlgi_atlas* atlas, const ml
     a.m_c1 = mlgi::small_div_magic(p->ism_size >> 2);
     a.lv1 = static_cast<float4*>(scratch);
     a.lv2 = p->levels >= 2 ? reinterpret_cast<float4*>(static_cast<char*>(scratch) + lv2_off) : nullptr;
+    a.row0 = 0;
+    a.row1 = p->grid_y;
     return MLGI_OK;
 }
 
@@ -455,6 +534,46 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
     return MLGI_OK;
 }
 
+mlgi_status mlgi_ism_clear(mlgi_ctx* ctx, mlgi_atlas* atlas, mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!atlas || !atlas->keys || atlas->width <= 0 || atlas->height <= 0) return fail(ctx, MLGI_EINVAL, "bad atlas");
+    MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas->keys, (size_t)atlas->width * atlas->height, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_ism_splat_range(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                                 const mlgi_ism_params* p, mlgi_atlas* atlas, int bucket0, int n_buckets,
+                                 mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi::SplatArgs a;
+    const mlgi_status st = build_splat_args(ctx, pts, vpls, n_vpl, p, atlas, a);
+    if (st != MLGI_OK) return st;
+    if (bucket0 < 0 || n_buckets < 0 || (int64_t)bucket0 + n_buckets > pts->n_buckets)
+        return fail(ctx, MLGI_EINVAL, "bucket range [%d, %d + %d) outside the %d buckets", bucket0, bucket0, n_buckets,
+                    pts->n_buckets);
+    a.bucket0 = bucket0;
+    a.n_groups = n_buckets;
+    MLGI_CUDA(ctx, mlgi::launch_ism_splat(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* p, int row0, int row1,
+                               mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!atlas || !p) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    if (row0 < 0 || row1 < row0 || row1 > p->grid_y)
+        return fail(ctx, MLGI_EINVAL, "ISM rows [%d, %d) outside the grid's %d rows", row0, row1, p->grid_y);
+    mlgi_status st =
+        ensure(ctx, ctx->pp, std::max<size_t>(16, mlgi::pullpush_scratch_bytes(atlas->width, atlas->height, p->levels, nullptr)));
+    if (st != MLGI_OK) return st;
+    mlgi::PullPushArgs a;
+    if ((st = build_pullpush_args(ctx, atlas, p, ctx->pp.p, a)) != MLGI_OK) return st;
+    a.row0 = row0;
+    a.row1 = row1;
+    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
 mlgi_status mlgi_cluster_lights(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls, int n_vpl,
                                 const mlgi_cluster_params* p, uint32_t* used, uint32_t* masks, uint8_t* pixel_slice,
                                 mlgi_stream stream) {
@@ -486,11 +605,13 @@ mlgi_status mlgi_cluster_lights(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const
     return MLGI_OK;
 }
 
-mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls,
-                              const mlgi_atlas* atlas, const mlgi_fg_params* p, mlgi_radiance* out,
-                              mlgi_stream stream) {
-    if (!ctx) return MLGI_EINVAL;
-    mlgi::FgArgs a;
+}  // extern "C"
+
+namespace {
+
+// The gathering's arguments; with clustered culling also runs the cluster pass on `stream`.
+mlgi_status prepare_fg(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls, const mlgi_atlas* atlas,
+                       const mlgi_fg_params* p, mlgi_radiance* out, mlgi_stream stream, mlgi::FgArgs& a) {
     mlgi_status st = build_fg_args(ctx, g, vpls, atlas, p, out, a);
     if (st != MLGI_OK) return st;
     if (p->cull == 2) {  // the clusters' VPL masks first, in context scratch
@@ -515,6 +636,20 @@ mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const m
         a.cl_tiles_x = tx;
         a.cl_words = words;
     }
+    return MLGI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls,
+                              const mlgi_atlas* atlas, const mlgi_fg_params* p, mlgi_radiance* out,
+                              mlgi_stream stream) {
+    if (!ctx) return MLGI_EINVAL;
+    mlgi::FgArgs a;
+    const mlgi_status st = prepare_fg(ctx, g, vpls, atlas, p, out, stream, a);
+    if (st != MLGI_OK) return st;
     MLGI_CUDA(ctx, mlgi::launch_final_gather(a, pick(ctx, stream)));
     return MLGI_OK;
 }
@@ -611,7 +746,8 @@ mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n) {
         MLGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[kFg + 1]));
         for (int k = kVplp; k <= kFg; ++k) cudaEventElapsedTime(&ctx->last_ms[k], ctx->ev[k], ctx->ev[k + 1]);
         const cudaEvent_t pp[5] = {ctx->ev[kPullPush], ctx->ev_pp[0], ctx->ev_pp[1], ctx->ev_pp[2], ctx->ev[kPullPush + 1]};
-        for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&ctx->last_ms[kPull1 + k], pp[k], pp[k + 1]);
+        for (int k = 0; k < 4 && !ctx->timed_host_frame; ++k)
+            cudaEventElapsedTime(&ctx->last_ms[kPull1 + k], pp[k], pp[k + 1]);
         if (ctx->timed_host_frame) {
             MLGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[kEvD2HEnd]));
             cudaEventElapsedTime(&ctx->last_ms[kH2D], ctx->ev[kEvH2DStart], ctx->ev[kEvH2DEnd]);
@@ -678,9 +814,12 @@ mlgi_status mlgi_frame_host_sizes_get(const mlgi_frame_desc* f, mlgi_frame_host_
     return MLGI_OK;
 }
 
-mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host) {
-    if (!ctx) return MLGI_EINVAL;
-    if (!f || !rgb_host) return fail(ctx, MLGI_EINVAL, "NULL argument");
+}  // extern "C"
+
+namespace {
+
+// The body of mlgi_gi_frame_host; the caller synchronises every stream afterwards, also on error.
+mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host) {
     mlgi_frame_host_sizes z;
     mlgi_frame_host_sizes_get(f, &z);
     mlgi_status st = MLGI_OK;
@@ -693,10 +832,6 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     if (st != MLGI_OK) return st;
     for (int i = 0; i < 7; ++i)
         if (sizes[i] && !srcs[i]) return fail(ctx, MLGI_EINVAL, "host input %d is NULL", i);
-    // Uploads on the copy stream in the order the passes need them; the compute stream waits for
-    // each input just before its first reader, so the splat of a point range runs while the next
-    // range and the G-buffer are still arriving (atomicMin does not depend on the order).
-    cudaStream_t s = ctx->stream, c = ctx->copy;
     mlgi_frame_desc d = *f;
     d.rsm.depth = static_cast<const float*>(ctx->h_rsm_depth.p);
     d.rsm.normal = static_cast<const uint32_t*>(ctx->h_rsm_normal.p);
@@ -706,28 +841,8 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     d.gbuffer.depth = static_cast<const float*>(ctx->h_gdepth.p);
     d.gbuffer.normal = ctx->h_gnormal.p;
     mlgi_radiance out{f->gbuffer.width, f->gbuffer.height, static_cast<float*>(ctx->h_rgb.p)};
-    const int nb = f->points.n_buckets;
-    const int nchunks = std::max(1, std::min(kHostPointChunks, nb));
-    const size_t bucket_bytes = (size_t)f->points.bucket_stride * 16;
-    mark(ctx, kEvH2DStart, c);
-    for (int i = 0; i < 3; ++i)
-        if (sizes[i]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, c));
-    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_rsm, c));
-    if (sizes[4]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[4]->p, srcs[4], sizes[4], cudaMemcpyHostToDevice, c));
-    for (int k = 0; k < nchunks; ++k) {
-        const size_t b0 = (size_t)nb * k / nchunks, b1 = (size_t)nb * (k + 1) / nchunks;
-        if (b1 > b0 && bucket_bytes)
-            MLGI_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(bufs[3]->p) + b0 * bucket_bytes,
-                                           static_cast<const char*>(srcs[3]) + b0 * bucket_bytes,
-                                           (b1 - b0) * bucket_bytes, cudaMemcpyHostToDevice, c));
-        MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pts[k], c));
-    }
-    for (int i = 5; i < 7; ++i)
-        if (sizes[i]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, c));
-    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_gbuf, c));
-    mark(ctx, kEvH2DEnd, c);
 
-    // compute: the chain of run_frame with the waits placed at the first reader of each input
+    // every argument check before the first copy is queued
     const int n = d.vpl.count;
     st = ensure(ctx, ctx->vpl, (size_t)n * 48);
     if (st == MLGI_OK) st = ensure(ctx, ctx->packed, (size_t)n * 16);
@@ -736,38 +851,166 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     const int aw = d.ism.grid_x * d.ism.ism_size, ah = d.ism.grid_y * d.ism.ism_size;
     if (st == MLGI_OK) st = ensure(ctx, ctx->keys, (size_t)aw * ah * 4);
     if (st == MLGI_OK) st = ensure(ctx, ctx->depth, (size_t)aw * ah * (d.atlas_format == MLGI_F16 ? 2 : 4));
+    if (st == MLGI_OK)
+        st = ensure(ctx, ctx->pp, std::max<size_t>(16, mlgi::pullpush_scratch_bytes(aw, ah, d.ism.levels, nullptr)));
     if (st != MLGI_OK) return st;
     mlgi_vpl_buf vb{n, static_cast<float*>(ctx->vpl.p), static_cast<float*>(ctx->packed.p),
                     reduced ? ctx->reduced.p : nullptr};
     mlgi_atlas atlas{aw, ah, static_cast<uint32_t*>(ctx->keys.p), ctx->depth.p, d.atlas_format};
+    mlgi::VplArgs va;
     mlgi::SplatArgs sa;
+    mlgi::PullPushArgs pa;
+    mlgi::FgArgs fa;
+    if ((st = build_vpl_args(ctx, &d.rsm, &d.vpl, &vb, va)) != MLGI_OK) return st;
     if ((st = build_splat_args(ctx, &d.points, &vb, n, &d.ism, &atlas, sa)) != MLGI_OK) return st;
+    if ((st = build_pullpush_args(ctx, &atlas, &d.ism, ctx->pp.p, pa)) != MLGI_OK) return st;
+    if ((st = build_fg_args(ctx, &d.gbuffer, &vb, &atlas, &d.fg, &out, fa)) != MLGI_OK) return st;
+    HostSchedule& h = ctx->sched;
+    host_schedule(h, d);
+    const int nb = d.points.n_buckets;
+    const size_t bucket_bytes = (size_t)d.points.bucket_stride * 16;
+    // upload position range [q0, q1) as at most two runs of consecutive buckets
+    auto bucket_runs = [&](int q0, int q1, int (&runs)[2][2]) {
+        int m = 0;
+        for (int q = q0; q < q1;) {
+            const int b = (h.rot + q) % nb;
+            const int len = std::min(q1 - q, nb - b);
+            runs[m][0] = b;
+            runs[m][1] = b + len;
+            ++m;
+            q += len;
+        }
+        return m;
+    };
+
+    // Uploads on the copy stream in the order the passes read them; the compute stream waits for
+    // each input just before its first reader, so each point range is splatted, and the ISM rows
+    // it completes are pulled and pushed, while the next range and the G-buffer are arriving.
+    cudaStream_t s = ctx->stream, c = ctx->copy, s2 = ctx->side;
+    mark(ctx, kEvH2DStart, c);
+    for (int i = 0; i < 3; ++i)
+        if (sizes[i]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, c));
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_rsm, c));
+    if (sizes[4]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[4]->p, srcs[4], sizes[4], cudaMemcpyHostToDevice, c));
+    for (int k = 0; k < h.chunks; ++k) {
+        int runs[2][2];
+        const int m = bucket_runs(h.pos[k], h.pos[k + 1], runs);
+        for (int r = 0; r < m && bucket_bytes; ++r)
+            MLGI_CUDA(ctx, cudaMemcpyAsync(static_cast<char*>(bufs[3]->p) + runs[r][0] * bucket_bytes,
+                                           static_cast<const char*>(srcs[3]) + runs[r][0] * bucket_bytes,
+                                           (size_t)(runs[r][1] - runs[r][0]) * bucket_bytes, cudaMemcpyHostToDevice, c));
+        MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pts[k], c));
+    }
+    for (int i = 5; i < 7; ++i)
+        if (sizes[i]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, c));
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_gbuf, c));
+    mark(ctx, kEvH2DEnd, c);
+
     MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_rsm, 0));
     mark(ctx, kVplp, s);
-    if ((st = mlgi_vpl_process(ctx, &d.rsm, &d.vpl, &vb, s)) != MLGI_OK) return st;
+    MLGI_CUDA(ctx, mlgi::launch_vpl_process(va, s));
     mark(ctx, kIsmClear, s);
     MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas.keys, (size_t)aw * ah, s));
     mark(ctx, kIsmCs, s);
-    for (int k = 0; k < nchunks; ++k) {
-        const int b0 = (int)((size_t)nb * k / nchunks), b1 = (int)((size_t)nb * (k + 1) / nchunks);
+    // Rows are pulled and pushed in runs: rows completed by the chunks so far go to the side
+    // stream, concurrent with the next chunks' splats, once they make up a quarter of the grid
+    // (a run costs about four rows' time whatever its size); the rest after the last chunk,
+    // alternating between the two streams. Runs write disjoint rows.
+    const int gy = d.ism.grid_y;
+    std::vector<char> done(gy, 0);
+    MLGI_CUDA(ctx, mlgi::pullpush_prepare(mlgi::pullmid_smem_bytes(d.ism.ism_size, d.ism.levels)));
+    auto pull_rows = [&](int k, bool last, int& run) -> cudaError_t {
+        for (int r = 0; r < gy;) {  // runs of consecutive rows completed by chunks <= k
+            if (done[r] || h.row_chunk[r] > k) {
+                ++r;
+                continue;
+            }
+            int r1 = r;
+            while (r1 < gy && !done[r1] && h.row_chunk[r1] <= k) done[r1++] = 1;
+            mlgi::PullPushArgs part = pa;
+            part.row0 = r;
+            part.row1 = r1;
+            const cudaError_t e = mlgi::launch_pullpush_captured(part, last && (run & 1) == 0 ? s : s2);
+            if (e != cudaSuccess) return e;
+            ++run;
+            r = r1;
+        }
+        return cudaSuccess;
+    };
+    int run = 0;
+    for (int k = 0; k < h.chunks; ++k) {
         MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_pts[k], 0));
-        mlgi::SplatArgs part = sa;
-        part.bucket0 = b0;
-        part.n_groups = b1 - b0;
-        MLGI_CUDA(ctx, mlgi::launch_ism_splat(part, s));
+        int runs[2][2];
+        const int m = bucket_runs(h.pos[k], h.pos[k + 1], runs);
+        for (int r = 0; r < m; ++r) {
+            mlgi::SplatArgs part = sa;
+            part.bucket0 = runs[r][0];
+            part.n_groups = runs[r][1] - runs[r][0];
+            MLGI_CUDA(ctx, mlgi::launch_ism_splat(part, s));
+        }
+        int ready = 0;
+        for (int r = 0; r < gy; ++r) ready += !done[r] && h.row_chunk[r] <= k;
+        const bool last = k + 1 == h.chunks;
+        if (last) run = 0;  // the first of the last runs on the compute stream, beside the side stream's backlog
+        if (last || (ready > 0 && 4 * ready >= gy)) {
+            MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_split[k], s));
+            MLGI_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_split[k], 0));
+            if (last) mark(ctx, kPullPush, s);
+            MLGI_CUDA(ctx, pull_rows(k, last, run));
+        }
     }
-    mark(ctx, kPullPush, s);
-    if ((st = mlgi_pullpush(ctx, &atlas, &d.ism, s)) != MLGI_OK) return st;
-    MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_gbuf, 0));
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_side, s2));
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_side, 0));
     mark(ctx, kFg, s);
-    if ((st = mlgi_final_gather(ctx, &d.gbuffer, &vb, &atlas, &d.fg, &out, s)) != MLGI_OK) return st;
+
+    // the gathering in bands of tile rows over two streams; each band's rows are downloaded as
+    // soon as it is done (the download of a row takes about as long as its gathering, so narrow
+    // bands leave little download after the last one)
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_gbuf, 0));
+    if ((st = prepare_fg(ctx, &d.gbuffer, &vb, &atlas, &d.fg, &out, s, fa)) != MLGI_OK) return st;
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
+    const int tile_rows = mlgi::fg_tile_rows(fa), rows_per = mlgi::fg_rows_per_tile_row(fa);
+    const int bands = std::max(1, std::min(kHostBands, tile_rows));
+    const size_t row_bytes = (size_t)fa.width * 12;
+    int tr0 = 0;
+    for (int k = 0; k < bands; ++k) {
+        const int tr1 = tr0 + tile_rows / bands + (k < tile_rows % bands ? 1 : 0);  // wider bands first
+        cudaStream_t bs = (k & 1) ? s2 : s;
+        MLGI_CUDA(ctx, mlgi::launch_final_gather(fa, bs, tr0, tr1));
+        MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_band[k], bs));
+        const int y0 = tr0 * rows_per, y1 = std::min(tr1 * rows_per, fa.height);
+        MLGI_CUDA(ctx, cudaStreamWaitEvent(c, ctx->ev_band[k], 0));
+        if (y1 > y0)
+            MLGI_CUDA(ctx, cudaMemcpyAsync(reinterpret_cast<char*>(rgb_host) + y0 * row_bytes,
+                                           reinterpret_cast<const char*>(out.rgb) + y0 * row_bytes,
+                                           (size_t)(y1 - y0) * row_bytes, cudaMemcpyDeviceToHost, c));
+        tr0 = tr1;
+    }
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_band[bands - 1], 0));
+    if (bands > 1) MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_band[bands - 2], 0));
     mark(ctx, kFg + 1, s);
-    MLGI_CUDA(ctx, cudaMemcpyAsync(rgb_host, out.rgb, z.radiance, cudaMemcpyDeviceToHost, s));
-    mark(ctx, kEvD2HEnd, s);
-    MLGI_CUDA(ctx, cudaStreamSynchronize(s));
-    MLGI_CUDA(ctx, cudaStreamSynchronize(c));
+    mark(ctx, kEvD2HEnd, c);
+    return MLGI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!f || !rgb_host) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    const mlgi_status st = host_frame(ctx, f, rgb_host);
+    // nothing may still read the caller's buffers when the call returns, also after an error
+    const cudaError_t e1 = cudaStreamSynchronize(ctx->copy);
+    const cudaError_t e2 = cudaStreamSynchronize(ctx->side);
+    const cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
+    if (st != MLGI_OK) return st;
+    for (cudaError_t e : {e1, e2, e3})
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "host frame");
     ctx->timed_frame = ctx->timed_host_frame = ctx->timing;
-    return mlgi_check_device_status(ctx, s);
+    return mlgi_check_device_status(ctx, ctx->stream);
 }
 
 }  // extern "C"

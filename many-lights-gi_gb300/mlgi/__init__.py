@@ -171,6 +171,10 @@ _SIGS = {
     "mlgi_ism_splat": (C.c_int32, [_p, C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams),
                                    C.POINTER(Atlas), _p]),
     "mlgi_pullpush": (C.c_int32, [_p, C.POINTER(Atlas), C.POINTER(IsmParams), _p]),
+    "mlgi_ism_clear": (C.c_int32, [_p, C.POINTER(Atlas), _p]),
+    "mlgi_ism_splat_range": (C.c_int32, [_p, C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams),
+                                         C.POINTER(Atlas), C.c_int, C.c_int, _p]),
+    "mlgi_pullpush_rows": (C.c_int32, [_p, C.POINTER(Atlas), C.POINTER(IsmParams), C.c_int, C.c_int, _p]),
     "mlgi_ism_render_static": (C.c_int32, [C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams), _p,
                                            C.c_int, _p]),
     "mlgi_final_gather": (C.c_int32, [_p, C.POINTER(GBufferView), C.POINTER(VplBuf), C.POINTER(Atlas),
@@ -290,6 +294,17 @@ class Context:
 
     def pullpush(self, atlas: Atlas, params: IsmParams, stream: int = 0):
         return self._chk(lib().mlgi_pullpush(self.h, C.byref(atlas), C.byref(params), stream))
+
+    def ism_clear(self, atlas: Atlas, stream: int = 0):
+        return self._chk(lib().mlgi_ism_clear(self.h, C.byref(atlas), stream))
+
+    def ism_splat_range(self, pts: Points, vpls: VplBuf, n_vpl: int, params: IsmParams, atlas: Atlas, bucket0: int,
+                        n_buckets: int, stream: int = 0):
+        return self._chk(lib().mlgi_ism_splat_range(self.h, C.byref(pts), C.byref(vpls), n_vpl, C.byref(params),
+                                                    C.byref(atlas), bucket0, n_buckets, stream))
+
+    def pullpush_rows(self, atlas: Atlas, params: IsmParams, row0: int, row1: int, stream: int = 0):
+        return self._chk(lib().mlgi_pullpush_rows(self.h, C.byref(atlas), C.byref(params), row0, row1, stream))
 
     def final_gather(self, g: GBufferView, vpls: VplBuf, atlas: Atlas, params: FgParams, out: Radiance,
                      stream: int = 0):

@@ -139,6 +139,49 @@ def test_pullpush_bit_exact(ctx, cfg):
     assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
 
 
+@pytest.mark.parametrize("cfg", [mlgi.C0, mlgi.C2, mlgi.C3B.replace(reduced=False, name="c3b_fp32")],
+                         ids=lambda c: c.name)
+def test_splat_ranges_and_pullpush_rows_equal_whole_passes(ctx, cfg):
+    """mlgi_ism_splat_range over a shuffled partition of the buckets after one clear, then
+    mlgi_pullpush_rows over a shuffled partition of the ISM rows spread over two streams, give
+    mlgi_ism_splat's keys and mlgi_pullpush's atlas bit for bit."""
+    import torch
+
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    ip = mlgi.ism_params(cfg)
+    ctx.ism_splat(df.points_view(), df.vpl_buf(), cfg.n_vpl, ip, df.atlas_view())
+    ctx.pullpush(df.atlas_view(), ip)
+    torch.cuda.synchronize()
+    keys, fin = df.keys_np().copy(), df.atlas_np().copy()
+    rng = np.random.default_rng(11)
+    cuts = np.unique(np.concatenate([[0, cfg.n_vpl], rng.integers(0, cfg.n_vpl, 9)]))
+    parts = list(zip(cuts[:-1], cuts[1:]))
+    rng.shuffle(parts)
+    df.atlas.zero_()
+    ctx.ism_clear(df.atlas_view())
+    for b0, b1 in parts:
+        ctx.ism_splat_range(df.points_view(), df.vpl_buf(), cfg.n_vpl, ip, df.atlas_view(), int(b0), int(b1 - b0))
+    torch.cuda.synchronize()
+    assert (df.keys_np() == keys).all()
+    cuts = np.unique(np.concatenate([[0, cfg.grid_y], rng.integers(0, cfg.grid_y, 4)]))
+    rows = list(zip(cuts[:-1], cuts[1:]))
+    rng.shuffle(rows)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    streams = [ctx.stream(), side.cuda_stream]
+    torch.cuda.synchronize()
+    for i, (r0, r1) in enumerate(rows):
+        ctx.pullpush_rows(df.atlas_view(), ip, int(r0), int(r1), streams[i % 2])
+    torch.cuda.synchronize()
+    assert (df.atlas_np().view(np.uint32) == fin.view(np.uint32)).all()
+    with pytest.raises(mlgi.MlgiError):
+        ctx.pullpush_rows(df.atlas_view(), ip, 0, cfg.grid_y + 1)
+    with pytest.raises(mlgi.MlgiError):
+        ctx.ism_splat_range(df.points_view(), df.vpl_buf(), cfg.n_vpl, ip, df.atlas_view(), cfg.n_vpl - 1, 2)
+
+
 def test_pullpush_fp16_atlas_is_rounded_fp32(ctx):
     import torch
 
@@ -258,6 +301,27 @@ def test_frame_chain_and_host_frame_agree(ctx):
                          cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.z_far, cfg.gi_intensity, cfg.clamp_value,
                          cfg.interleave, dtype=np.float64)
     assert rel_l2(dev, ref) < FG_REL_L2
+
+
+@pytest.mark.parametrize("cfg", [mlgi.C0, mlgi.CREF, mlgi.C2, mlgi.C3B, mlgi.C1.replace(cull=2, name="c1_clustered")],
+                         ids=lambda c: c.name)
+def test_host_frame_equals_device_frame(ctx, cfg):
+    """The host-buffer frame splats point ranges as they arrive, pulls and pushes the ISM rows each
+    range completes, and gathers and downloads in bands of rows: bit for bit the device frame."""
+    import torch
+
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    ctx.gi_frame(df.frame_desc(), df.radiance())
+    torch.cuda.synchronize()
+    dev = df.rgb_np().copy()
+    pinned = pinned_inputs(sc)
+    for _ in range(2):  # the second call reuses the cached upload schedule
+        pinned["rgb"].zero_()
+        ctx.gi_frame_host(host_frame_desc(sc, pinned), pinned["rgb"].numpy())
+        host = pinned["rgb"].numpy().reshape(dev.shape)
+        assert np.abs(dev).max() > 0
+        assert (dev.view(np.uint32) == host.view(np.uint32)).all()
 
 
 def test_frame_is_deterministic(ctx):
