@@ -102,6 +102,9 @@ struct SplatSmem {
     float4 tasks[kSplatThreads / 32][128];  // per warp: (point xyz, VPL slot << 8 | radius byte)
     v3 s[16], u[16];
     float tx[16], ty[16];   // the VPL's ISM tile offsets, float(x) and float(y) (ism_utils.glsl:35-37)
+    // per byte value b of a point's packed word, computed with the shader's own operations:
+    float unorm[256];       // float(b) / 255 * 2 - 1, a normal component (ism.comp:81-85)
+    uint8_t rbyte[256];     // uint(float(b) / 255 * 25 * 10 / 2), the key's radius byte (ism.comp:87, 131-136)
 };
 
 // 1/x when x is a power of two (then v / x == v * (1/x) bit for bit: both are the rounding of the
@@ -141,6 +144,11 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         S.tx[threadIdx.x] = float(f2i(ismIndex - ty * fgx));
         S.ty[threadIdx.x] = float(f2i(ty));
     }
+    for (int b = threadIdx.x; b < 256; b += kSplatThreads) {
+        const float f = float(b) / 255.0f;
+        S.unorm[b] = f * 2.0f - 1.0f;
+        S.rbyte[b] = (uint8_t)f2u(f * 25.0f * 10.0f / 2.0f);  // / sqrt(maxVplCollectCount)
+    }
     __syncthreads();
 
     const uint32_t first = (uint32_t)chunk * kSplatChunk;
@@ -166,8 +174,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             pt = __ldg(bucket + j);
             const v3 position = mk(pt.x, pt.y, pt.z);
             const uint32_t nr = __float_as_uint(pt.w);
-            const v3 pn = mk(float(nr & 0xFFu) / 255.0f * 2.0f - 1.0f, float((nr >> 8) & 0xFFu) / 255.0f * 2.0f - 1.0f,
-                             float((nr >> 16) & 0xFFu) / 255.0f * 2.0f - 1.0f);
+            const v3 pn = mk(S.unorm[nr & 0xFFu], S.unorm[(nr >> 8) & 0xFFu], S.unorm[(nr >> 16) & 0xFFu]);
             // gather up to 4 VPLs that pass the two-sided cull (ism.comp:93-107), as 4-bit indices
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
@@ -191,8 +198,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         const int total = __shfl_sync(0xffffffffu, pre, 31);
         pre -= found;
         if (found > 0) {
-            const float pointRadius = float(__float_as_uint(pt.w) >> 24) / 255.0f * 25.0f;
-            const uint32_t rbyte = f2u(pointRadius * 10.0f / 2.0f);  // / sqrt(maxVplCollectCount)
+            const uint32_t rbyte = S.rbyte[__float_as_uint(pt.w) >> 24];
             for (int k = 0; k < found; ++k)
                 tasks[pre + k] = make_float4(pt.x, pt.y, pt.z, __uint_as_float((((used >> (4 * k)) & 15u) << 8) | rbyte));
         }
@@ -285,18 +291,44 @@ __device__ __forceinline__ bool sqrt_gt(float d2, float r) {
     return sqrt_gt_band(d2, r);
 }
 
-// x / n for the sample counts and weight sums that occur (n >= 1). Division by a power of two is
-// exact, so it equals the multiply by the reciprocal bit for bit; other n use IEEE division.
+// RN(1/n) for n = 1..16 (entry 0 unused), folded by the compiler in IEEE single precision.
+__device__ const float kRcpSmall[17] = {0.0f,        1.0f,        1.0f / 2.0f,  1.0f / 3.0f,  1.0f / 4.0f,  1.0f / 5.0f,
+                                        1.0f / 6.0f, 1.0f / 7.0f, 1.0f / 8.0f,  1.0f / 9.0f,  1.0f / 10.0f, 1.0f / 11.0f,
+                                        1.0f / 12.0f, 1.0f / 13.0f, 1.0f / 14.0f, 1.0f / 15.0f, 1.0f / 16.0f};
+
+// x / n rounded to nearest for the sample counts and weight sums that occur (1 <= n <= 16), from
+// R = RN(1/n) and one correction by the exact residual (Markstein's division): q = RN(x R),
+// r = x - q n (exact by FMA), result RN(q + r R). That equals IEEE x / n for every float
+// significand and every n <= 16 (checked exhaustively in tests/test_small_division.py); scaling by
+// a power of two is exact, so it holds for every x whose intermediates stay normal. Zero, tiny,
+// huge and non-finite x take the IEEE division.
+__device__ __forceinline__ float div_corrected(float x, float d, float R) {
+    const float ax = fabsf(x);
+    if (!(ax >= 0x1p-100f && ax <= 0x1p+100f)) return x / d;
+    const float q = x * R;
+    const float r = fmaf(-q, d, x);
+    return fmaf(r, R, q);
+}
+
+// The push's weight sums 1..16, without branches (for a power of two R is exact and the
+// correction adds 0).
 __device__ __forceinline__ float div_count(float x, int n) {
+    return n <= 16 ? div_corrected(x, float(n), __ldg(kRcpSmall + n)) : x / float(n);
+}
+
+// The pull's valid-sample counts 1..4: only 3 needs a division; the others are exact multiplies.
+__device__ __forceinline__ float div_count4(float x, int n) {
     switch (n) {
         case 1: return x;
         case 2: return x * 0.5f;
-        case 4: return x * 0.25f;
-        case 8: return x * 0.125f;
-        case 16: return x * 0.0625f;
-        default: return x / float(n);
+        case 3: return div_corrected(x, 3.0f, 1.0f / 3.0f);
+        default: return x * 0.25f;
     }
 }
+
+// x / 3.14f rounded to nearest by the same correction (checked exhaustively for this
+// divisor in tests/test_small_division.py).
+__device__ __forceinline__ float div_314(float x) { return div_corrected(x, 3.14f, 1.0f / 3.14f); }
 
 // Two 256-entry tables indexed by a key's radius byte b, each entry computed with the shader's own
 // operations so that lookups are bit-identical:
@@ -344,8 +376,8 @@ __device__ __forceinline__ float4 pull_combine(const PullSample (&q)[4], const f
         numValid++;
     }
     if (numValid == 0) return make_float4(1.0f, 0.f, 0.f, 0.f);
-    return make_float4(div_count(depthAcc, numValid), maxValid, div_count(radiusAcc, numValid),
-                       __uint_as_float(pack_half2(div_count(dax, numValid), div_count(day, numValid))));
+    return make_float4(div_count4(depthAcc, numValid), maxValid, div_count4(radiusAcc, numValid),
+                       __uint_as_float(pack_half2(div_count4(dax, numValid), div_count4(day, numValid))));
 }
 
 __device__ constexpr int kPullOff[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};
@@ -365,7 +397,7 @@ __device__ __forceinline__ float4 pull1_texel(const PullPushArgs& a, const float
         q[k].depth = depthSample;
         q[k].maxDepth = depthSample + s_mdo[key[k] & 0xFFu];
         const float distToCamera = depthSample * a.z_far;
-        float radius = s_rad[key[k] & 0xFFu] / distToCamera / 3.14f * fs;
+        float radius = div_314(s_rad[key[k] & 0xFFu] / distToCamera) * fs;
         radius = radius * 1.3f;
         q[k].radius = gmin(radius, 15.0f);
         q[k].ndx = kPullOff[k][0] ? 0.25f : -0.25f;
