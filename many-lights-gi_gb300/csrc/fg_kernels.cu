@@ -109,24 +109,27 @@ __device__ __forceinline__ df df_mul_f(df a, float b) {
     const float e = __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p));
     return fast_two_sum(p, e);
 }
-// a / b rounded to FP32 from double-float operands: one Newton correction of the FP32 quotient.
-__device__ __forceinline__ float df_div(df a, df b) {
-    const float q = __fdiv_rn(a.hi, b.hi);
-    // r = a - q*b: the FMA remainder a.hi - q*b.hi is exact; add the low-order parts
+// a / b rounded to FP32 from double-float operands, given rb ~ 1/b.hi (within a few ulps): the
+// quotient a.hi * rb, then one correction by the remainder a - q b (the FMA part a.hi - q b.hi is
+// exact); the error left is the square of rb's relative error plus the final rounding.
+__device__ __forceinline__ float df_div(df a, df b, float rb) {
+    const float q = __fmul_rn(a.hi, rb);
     const float r = __fadd_rn(__fmaf_rn(-q, b.hi, a.hi), __fmaf_rn(-q, b.lo, a.lo));
-    return __fadd_rn(q, __fdiv_rn(r, b.hi));
+    return __fmaf_rn(r, rb, q);
 }
-// 2*k/n - 1 as double-float (k, n small integers): the pixel-corner NDC coordinate.
-__device__ __forceinline__ df ndc_coord(int k, int n) {
+// 2*k/n - 1 as double-float (k, n small integers, rn = RN(1/n)): the pixel-corner NDC coordinate.
+// q = k rn is within an ulp of k/n; the remainder k - q n is exact, and its quotient is the low part.
+__device__ __forceinline__ df ndc_coord(int k, int n, float rn) {
     const float fk = float(k), fn = float(n);
-    const float q = __fdiv_rn(fk, fn);
-    const float ql = __fdiv_rn(__fmaf_rn(-q, fn, fk), fn);
+    const float q = __fmul_rn(fk, rn);
+    const float ql = __fmul_rn(__fmaf_rn(-q, fn, fk), rn);
     const df t = two_sum(__fmul_rn(q, 2.0f), -1.0f);
     return fast_two_sum(t.hi, __fadd_rn(t.lo, __fmul_rn(ql, 2.0f)));
 }
 // world = (inv_vp * (ndc, 1)).xyz / w, each row summed in double-float.
-__device__ __forceinline__ v3 reconstruct_world(const float* m, int x, int y, int w, int h, float d) {
-    const df nx = ndc_coord(x, w), ny = ndc_coord(y, h);
+__device__ __forceinline__ v3 reconstruct_world(const float* m, int x, int y, int w, int h, float rw, float rh,
+                                                float d) {
+    const df nx = ndc_coord(x, w, rw), ny = ndc_coord(y, h, rh);
     const df nz = two_sum(__fmul_rn(d, 2.0f), -1.0f);
     df r[4];
 #pragma unroll
@@ -137,8 +140,16 @@ __device__ __forceinline__ v3 reconstruct_world(const float* m, int x, int y, in
         acc = df_add(acc, df{m[12 + k], 0.0f});
         r[k] = acc;
     }
-    return mk(df_div(r[0], r[3]), df_div(r[1], r[3]), df_div(r[2], r[3]));
+    // one reciprocal of w for the three divides (the hardware approximation); each quotient is
+    // corrected by its remainder, as in double-float division (Dekker 1971)
+    float rb;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(rb) : "f"(r[3].hi));
+    return mk(df_div(r[0], r[3], rb), df_div(r[1], r[3], rb), df_div(r[2], r[3], rb));
 }
+
+// normalize(v) with the hardware reciprocal square root (about 2 ulps; the gathering's bar is a
+// relative L2 of 1e-3).
+__device__ __forceinline__ v3 normalize_fast(v3 v) { return v * rsqrtf(dot(v, v)); }
 
 __device__ __forceinline__ v3 oct_decode(float ex, float ey) {
     v3 n = mk(ex, ey, 1.0f - fabsf(ex) - fabsf(ey));
@@ -147,7 +158,7 @@ __device__ __forceinline__ v3 oct_decode(float ex, float ey) {
         n.x = (1.0f - fabsf(ey)) * sx;
         n.y = (1.0f - fabsf(ex)) * sy;
     }
-    return normalize(n);
+    return normalize_fast(n);
 }
 
 // Shared memory of one final-gathering block (one tile of one interleave class).
@@ -188,7 +199,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     if (valid) {
         const size_t pix = (size_t)y * a.width + x;
         const float d = __ldg(a.depth + pix);
-        fw = reconstruct_world(a.inv_vp, x, y, a.width, a.height, d);
+        fw = reconstruct_world(a.inv_vp, x, y, a.width, a.height, a.inv_w, a.inv_h, d);
         float ex, ey;
         if (kNormalF16) {
             const __half2 h = reinterpret_cast<const __half2*>(a.normal)[pix];
@@ -267,12 +278,14 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         for (int k = tid; k < cnt; k += NT) {
             v3 p, n, f;
             decode_vpl<kReduced>(S.raw + (size_t)k * kRec, p, n, f);
-            v3 s, u;
-            look_at_rows(n, s, u);
+            // lookAtRH rows (ism_utils.glsl:5-13) with the fast normalisation
+            const v3 s = normalize_fast(cross(n, mk(0.0f, 1.0f, 0.01f)));
+            const v3 u = cross(s, n);
             const int vid = vbase + base + k;
-            const float ismIndex = float(vid) - float(a.ism_index_offset);
-            const int ty = int(ismIndex / float(a.gx));
-            const int tx = int(ismIndex - float(ty) * float(a.gx));
+            // int(ismIndex / gx) of small non-negative integers equals the integer quotient
+            const int ism = vid - a.ism_index_offset;
+            const int ty = ism / a.gx;
+            const int tx = ism - ty * a.gx;
             S.a[k] = make_float4(p.x, p.y, p.z, f.x);
             S.b[k] = make_float4(n.x, n.y, n.z, f.y);
             S.c[k] = make_float4(s.x, s.y, s.z, f.z);
@@ -406,9 +419,9 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     if (valid) {
         const size_t pix = (size_t)y * a.width + x;
         // vec3(acc * giIntensityFactor / vplCount) * interleavedPixels
-        a.out[3 * pix + 0] = accx * a.gi_intensity / a.vpl_count_f * a.i2;
-        a.out[3 * pix + 1] = accy * a.gi_intensity / a.vpl_count_f * a.i2;
-        a.out[3 * pix + 2] = accz * a.gi_intensity / a.vpl_count_f * a.i2;
+        a.out[3 * pix + 0] = accx * a.gi_scale;
+        a.out[3 * pix + 1] = accy * a.gi_scale;
+        a.out[3 * pix + 2] = accz * a.gi_scale;
     }
     return true;
 }

@@ -72,10 +72,9 @@ struct FgArgs {
     int interleave;
     int shadowing;
     int ism_index_offset;
-    float z_far, gi_scale;    // gi_scale = giIntensity / vplCount * I^2 applied as in the shader
-    float gi_intensity;
-    float vpl_count_f;       // float(vplEndIndex - vplStartIndex)
-    float i2;
+    float z_far;
+    float gi_scale;           // giIntensity / vplCount * I^2 (final_gathering.comp:133), folded on the host
+    float inv_w, inv_h;       // 1 / width, 1 / height
     float clamp_value;
     int tile;                 // tile edge (threads = tile*tile)
     int cull;                 // per-tile culling on/off

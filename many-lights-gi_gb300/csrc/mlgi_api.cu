@@ -480,9 +480,9 @@ mlgi_status build_fg_args(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_
     a.shadowing = p->shadowing;
     a.ism_index_offset = p->scale_isms ? p->vpl_start : 0;
     a.z_far = p->z_far;
-    a.gi_intensity = p->gi_intensity;
-    a.vpl_count_f = (float)(p->vpl_end - p->vpl_start);
-    a.i2 = (float)(I * I);
+    a.gi_scale = (float)((double)p->gi_intensity / (double)(p->vpl_end - p->vpl_start) * (double)(I * I));
+    a.inv_w = 1.0f / (float)g->width;
+    a.inv_h = 1.0f / (float)g->height;
     a.clamp_value = p->clamp_value;
     a.tile = p->tile == 0 ? 16 : p->tile;
     a.cull = p->cull;
