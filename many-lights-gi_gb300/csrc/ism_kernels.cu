@@ -664,17 +664,16 @@ __device__ __forceinline__ void push0_quads(const PullPushArgs& a, const int tx,
     const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
     const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w, oky0 = y0 >= Y0, oky1 = y0 + 1 < Y1;
     const uint32_t r0 = (uint32_t)y0 * w, r1 = (uint32_t)(y0 + 1) * w;
+    // the four keys first, so that their loads overlap each other and the coarse terms
+    const float k00 = oky0 && okx0 ? key_depth(a, r0 + x0) : 0.f;
+    const float k10 = oky0 && okx1 ? key_depth(a, r0 + x0 + 1) : 0.f;
+    const float k01 = oky1 && okx0 ? key_depth(a, r1 + x0) : 0.f;
+    const float k11 = oky1 && okx1 ? key_depth(a, r1 + x0 + 1) : 0.f;
     // level 0 writes only the depth channel (push.comp:33-37)
-    if (oky0 && okx0)
-        store_depth(a, r0 + x0, push_output<false, 0, 0>(C, bx, by, make_float4(key_depth(a, r0 + x0), 0.f, 0.f, 0.f)).x);
-    if (oky0 && okx1)
-        store_depth(a, r0 + x0 + 1,
-                    push_output<false, 1, 0>(C, bx, by, make_float4(key_depth(a, r0 + x0 + 1), 0.f, 0.f, 0.f)).x);
-    if (oky1 && okx0)
-        store_depth(a, r1 + x0, push_output<false, 0, 1>(C, bx, by, make_float4(key_depth(a, r1 + x0), 0.f, 0.f, 0.f)).x);
-    if (oky1 && okx1)
-        store_depth(a, r1 + x0 + 1,
-                    push_output<false, 1, 1>(C, bx, by, make_float4(key_depth(a, r1 + x0 + 1), 0.f, 0.f, 0.f)).x);
+    if (oky0 && okx0) store_depth(a, r0 + x0, push_output<false, 0, 0>(C, bx, by, make_float4(k00, 0.f, 0.f, 0.f)).x);
+    if (oky0 && okx1) store_depth(a, r0 + x0 + 1, push_output<false, 1, 0>(C, bx, by, make_float4(k10, 0.f, 0.f, 0.f)).x);
+    if (oky1 && okx0) store_depth(a, r1 + x0, push_output<false, 0, 1>(C, bx, by, make_float4(k01, 0.f, 0.f, 0.f)).x);
+    if (oky1 && okx1) store_depth(a, r1 + x0 + 1, push_output<false, 1, 1>(C, bx, by, make_float4(k11, 0.f, 0.f, 0.f)).x);
 }
 
 // Levels 2..L of one ISM in shared memory (tables first, then level 2, 3, ...): pull from lv1,
@@ -731,11 +730,14 @@ __device__ __forceinline__ void pullmid_ism(const PullPushArgs& a, const int ism
         a.lv2[(size_t)(iy * s2 + i / s2) * w2 + ix * s2 + i % s2] = l2[i];
 }
 
+// kPull1Rows tile rows per block, so that the key tables are filled once for several tiles.
+constexpr int kPull1Rows = 4;
 __global__ void __launch_bounds__(kPpTileW * kPpTileH) pull1_kernel(PullPushArgs a) {
     __shared__ float s_tab[512];
     fill_key_tables(s_tab, s_tab + 256, a.z_far);
     __syncthreads();
-    pull1_tile(a, blockIdx.x, blockIdx.y, s_tab, s_tab + 256);
+#pragma unroll 1
+    for (int j = 0; j < kPull1Rows; ++j) pull1_tile(a, blockIdx.x, blockIdx.y * kPull1Rows + j, s_tab, s_tab + 256);
 }
 
 // NT threads per ISM: kPullMidThreads when the launch fills the GPU with ISM blocks, more when a
@@ -798,7 +800,7 @@ static PullPushGrids pullpush_grids(const PullPushArgs& a) {
     const int w1 = a.atlas_w >> 1, rows = a.row1 - a.row0;
     const int s1 = a.ism_size >> 1, s0 = a.ism_size;
     PullPushGrids g;
-    g.g1 = dim3(tiles_x(w1), tiles_y(rows * s1));
+    g.g1 = dim3(tiles_x(w1), (tiles_y(rows * s1) + kPull1Rows - 1) / kPull1Rows);
     g.q1 = dim3(tiles_x(w1 / 2 + 1), tiles_y(((a.row1 * s1) >> 1) - ((a.row0 * s1) >> 1) + 1));
     g.q0 = dim3(tiles_x(w1 + 1), tiles_y(((a.row1 * s0) >> 1) - ((a.row0 * s0) >> 1) + 1));
     g.isms = rows * a.grid_x;
