@@ -343,25 +343,28 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
                 }
                 const float4 A = S.a[k], B = S.b[k];
                 const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
+                // the cosine terms have the signs of these dot products with the unnormalised
+                // direction: most pairs end here, before the square root (max(0, a1) *
+                // max(0, a2) > 0 needs a1 > 0 and a2 > 0)
+                const float e1 = B.x * dx + B.y * dy + B.z * dz;
+                const float e2 = fn.x * dx + fn.y * dy + fn.z * dz;
+                if (!(e1 > 0.f && e2 < 0.f)) return false;
                 const float d2 = dx * dx + dy * dy + dz * dz;
                 const float inv = rsqrtf(d2);
-                const float ndx = dx * inv, ndy = dy * inv, ndz = dz * inv;
-                const float a1 = B.x * ndx + B.y * ndy + B.z * ndz;
-                const float a2 = -(fn.x * ndx + fn.y * ndy + fn.z * ndz);
-                const float angle = fmaxf(0.f, a1) * fmaxf(0.f, a2);
-                if (!(angle > 0.f)) return false;
+                const float a1 = e1 * inv, a2 = -e2 * inv;
                 const float att = (inv * inv) * (inv * inv);
-                const float G = fminf(angle * att, clampv);
+                const float G = fminf((a1 * a2) * att, clampv);
                 const float4 C = S.c[k];
                 fG = make_float3(A.w * G, B.w * G, C.w * G);
                 if (shadow) {
                     const float4 D = S.d[k];
                     const float2 org = S.org[k];
                     // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false):
-                    // x = s.d / (1 - (-n).d), texel = floor(((x + 1)/2 + tile) * ismSize)
-                    const float rz = __fdividef(1.0f, 1.0f + a1);
-                    const float px = (C.x * ndx + C.y * ndy + C.z * ndz) * rz;
-                    const float py = (D.x * ndx + D.y * ndy + D.z * ndz) * rz;
+                    // x = s.d / (1 - (-n).d), texel = floor(((x + 1)/2 + tile) * ismSize), d the
+                    // normalised direction: s.d = (s.(p - v)) / |p - v|
+                    const float rz = __fdividef(inv, 1.0f + a1);
+                    const float px = (C.x * dx + C.y * dy + C.z * dz) * rz;
+                    const float py = (D.x * dx + D.y * dy + D.z * dz) * rz;
                     int ix = __float2int_rd(fmaf(px, hs, org.x));
                     int iy = __float2int_rd(fmaf(py, hs, org.y));
                     if (ix >= aw) ix -= aw;  // GL_REPEAT
