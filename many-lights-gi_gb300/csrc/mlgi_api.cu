@@ -100,6 +100,7 @@ struct mlgi_ctx {
     std::string err;
     std::map<int, int32_t*> shuffle_dev;  // per VPL count
     uint32_t* status = nullptr;           // device error word
+    uint32_t* status_host = nullptr;      // pinned copy of it, written by host frames
     // frame-level buffers
     DevBuf vpl, packed, reduced, keys, depth;
     DevBuf pp;  // pull-push pyramid levels 1 and 2
@@ -246,6 +247,7 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->status, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(ctx->status, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->status_host, sizeof(uint32_t), cudaHostAllocDefault);
     for (int i = 0; e == cudaSuccess && i < kNumEvents; ++i) e = cudaEventCreate(&ctx->ev[i]);
     for (int i = 0; e == cudaSuccess && i < 3; ++i) e = cudaEventCreate(&ctx->ev_pp[i]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking);
@@ -298,6 +300,7 @@ void mlgi_destroy(mlgi_ctx* ctx) {
             cudaStreamDestroy(cs);
         }
     if (ctx->status) cudaFree(ctx->status);
+    if (ctx->status_host) cudaFreeHost(ctx->status_host);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -914,9 +917,11 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     mark(ctx, kIsmCs, s);
     // Rows are pulled and pushed in runs: rows completed by the chunks so far go to the side
     // stream, concurrent with the next chunks' splats, once they make up a quarter of the grid
-    // (a run costs about four rows' time whatever its size); the rest after the last chunk,
-    // alternating between the two streams. Runs write disjoint rows.
+    // (a run costs about four rows' time whatever its size); the rest after the last chunk, in
+    // runs of at most 3/16 of the grid alternating between the two streams. Runs write disjoint
+    // rows.
     const int gy = d.ism.grid_y;
+    const int final_rows = std::max(2, 3 * gy / 16);
     std::vector<char> done(gy, 0);
     MLGI_CUDA(ctx, mlgi::pullpush_prepare(mlgi::pullmid_smem_bytes(d.ism.ism_size, d.ism.levels)));
     auto pull_rows = [&](int k, bool last, int& run) -> cudaError_t {
@@ -926,7 +931,7 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
                 continue;
             }
             int r1 = r;
-            while (r1 < gy && !done[r1] && h.row_chunk[r1] <= k) done[r1++] = 1;
+            while (r1 < gy && !done[r1] && h.row_chunk[r1] <= k && (!last || r1 - r < final_rows)) done[r1++] = 1;
             mlgi::PullPushArgs part = pa;
             part.row0 = r;
             part.row1 = r1;
@@ -991,6 +996,9 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     if (bands > 1) MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_band[bands - 2], 0));
     mark(ctx, kFg + 1, s);
     mark(ctx, kEvD2HEnd, c);
+    // the device error word rides behind the last band's copy (the copy stream has waited for
+    // every band, so every kernel of the frame is done)
+    MLGI_CUDA(ctx, cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c));
     return MLGI_OK;
 }
 
@@ -1010,7 +1018,8 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     for (cudaError_t e : {e1, e2, e3})
         if (e != cudaSuccess) return cuda_fail(ctx, e, "host frame");
     ctx->timed_frame = ctx->timed_host_frame = ctx->timing;
-    return mlgi_check_device_status(ctx, ctx->stream);
+    if (*ctx->status_host == 0) return MLGI_OK;
+    return mlgi_check_device_status(ctx, ctx->stream);  // reports and clears the error word
 }
 
 }  // extern "C"
