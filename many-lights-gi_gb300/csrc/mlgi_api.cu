@@ -54,11 +54,15 @@ struct HostSchedule {
 void host_schedule(HostSchedule& h, const mlgi_frame_desc& f) {
     const mlgi_ism_params& p = f.ism;
     const int nb = f.points.n_buckets, n = f.vpl.count, gx = p.grid_x, gy = p.grid_y;
-    const int key[9] = {nb, n, gx, gy, p.vpl_start, p.vpl_end, p.scale_isms, p.points_only_scaled, kHostPointChunks};
+    const int key[9] = {nb, n, gx, gy, p.vpl_start, p.vpl_end, p.scale_isms, p.points_only_scaled,
+                        (int)std::min<int64_t>((int64_t)f.points.bucket_stride, 1 << 30)};
     if (std::equal(key, key + 9, h.key)) return;
     std::copy(key, key + 9, h.key);
-    // the first chunk half as large as the others, so that the splat starts early
-    h.chunks = std::max(1, std::min(kHostPointChunks, nb));
+    // about one range per 16 MB of points (each costs a few API calls and a splat launch's
+    // latency, which small frames do not win back); the first half as large as the others, so
+    // that the splat starts early
+    const int64_t point_bytes = (int64_t)nb * f.points.bucket_stride * 16;
+    h.chunks = (int)std::max<int64_t>(1, std::min<int64_t>({kHostPointChunks, nb, point_bytes >> 24}));
     for (int k = 1; k < h.chunks; ++k) h.pos[k] = (int)((int64_t)nb * (2 * k - 1) / (2 * h.chunks - 1));
     h.pos[0] = 0;
     h.pos[h.chunks] = nb;
@@ -921,7 +925,7 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     // runs of at most 3/16 of the grid alternating between the two streams. Runs write disjoint
     // rows.
     const int gy = d.ism.grid_y;
-    const int final_rows = std::max(2, 3 * gy / 16);
+    const int final_rows = h.chunks > 1 ? std::max(2, 3 * gy / 16) : gy;
     std::vector<char> done(gy, 0);
     MLGI_CUDA(ctx, mlgi::pullpush_prepare(mlgi::pullmid_smem_bytes(d.ism.ism_size, d.ism.levels)));
     auto pull_rows = [&](int k, bool last, int& run) -> cudaError_t {
@@ -976,8 +980,10 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
     MLGI_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
     const int tile_rows = mlgi::fg_tile_rows(fa), rows_per = mlgi::fg_rows_per_tile_row(fa);
-    const int bands = std::max(1, std::min(kHostBands, tile_rows));
     const size_t row_bytes = (size_t)fa.width * 12;
+    // about one band per 3 MB of radiance
+    const int bands = (int)std::max<size_t>(1, std::min<size_t>({(size_t)kHostBands, (size_t)tile_rows,
+                                                                  z.radiance / (3u << 20)}));
     int tr0 = 0;
     for (int k = 0; k < bands; ++k) {
         const int tr1 = tr0 + tile_rows / bands + (k < tile_rows % bands ? 1 : 0);  // wider bands first
