@@ -343,6 +343,12 @@ def run_gpu(args, cfg, rank, world, local_rank):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(step_ms)
 
+    # the splat's atomicMin count for this frame (outside the timed region; a counting run of the
+    # same cull and projection)
+    ctx.vpl_process(df.rsm_view(), mlgi.vpl_params(scene.cfg, scene), df.vpl_buf())
+    atomics = ctx.ism_splat_count(df.points_view(), df.vpl_buf(), scene.cfg.n_vpl, mlgi.ism_params(scene.cfg),
+                                  df.atlas_view())
+
     # ---- end to end through the host-buffer C ABI call (e2e) ----
     pinned = pinned_inputs(scene)
     hfd = host_frame_desc(scene, pinned)
@@ -398,6 +404,8 @@ def run_gpu(args, cfg, rank, world, local_rank):
         "data": "synthetic (seeded procedural room)", "config": config_dict(cfg),
         "gpixel_vpl_per_s": frames * cfg.width * cfg.height * cfg.n_vpl / (total_ms * 1e-3) / 1e9,
         "evaluated_pairs_per_s": frames * cfg.pairs / (total_ms * 1e-3),
+        "splat_atomics_per_frame": atomics,
+        "splat_atomics_per_s": atomics / (kernel_ms["ism_splat"] * 1e-3) if kernel_ms.get("ism_splat") else None,
         "passes_ms": {n: float(v) for n, v in zip(PASSES, mean_pass)},
         "kernels_ms": kernel_ms,
         "gpu_launches": launches_per_frame(cfg) * args.steps,

@@ -153,6 +153,12 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
  *                         a paraboloid's rim can put a point on the border texels of a
  *                         neighbouring ISM; a point on a VPL's position lands on texel (0, 0). */
 mlgi_status mlgi_ism_clear(mlgi_ctx* ctx, mlgi_atlas* atlas, mlgi_stream stream);
+/* No counterpart in the reference: the number of atomicMin operations mlgi_ism_splat issues for
+ * these inputs (projections that land inside the atlas, at most 4 per point), from the splat's own
+ * cull and projection run without the atomics. Synchronous on the context's stream; for reporting
+ * the splat's atomic rate. */
+mlgi_status mlgi_ism_splat_count(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                                 const mlgi_ism_params* params, const mlgi_atlas* atlas, uint64_t* atomics);
 mlgi_status mlgi_ism_splat_range(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
                                  const mlgi_ism_params* params, mlgi_atlas* atlas, int bucket0, int n_buckets,
                                  mlgi_stream stream);

@@ -118,7 +118,10 @@ __device__ __forceinline__ float pow2_recip(int x) {
 // Work item `item` of a splat: chunk item % chunks of bucket item / chunks, i.e. the bucket's
 // points [chunk * kSplatChunk, (chunk + 1) * kSplatChunk), the last chunk up to the bucket's count
 // (one block each).
-__device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item, SplatSmem& S) {
+// kCount: count the atomics the splat would issue (into *atomics) instead of issuing them.
+template <bool kCount = false>
+__device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item, SplatSmem& S,
+                                             unsigned long long* atomics = nullptr) {
     const int local = item / a.chunks, chunk = item - local * a.chunks;
     const int wg = a.bucket0 + local;
     __syncthreads();  // the previous bucket's use of S is over
@@ -163,6 +166,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
     uint32_t* const keys = a.keys;
     const int lane = threadIdx.x & 31;
     float4* tasks = S.tasks[threadIdx.x >> 5];
+    unsigned issued = 0;  // kCount: this thread's in-range projections
     // Each warp takes 32 points at a time; a point's projections into its <= 4 VPLs become tasks
     // that the whole warp then runs, so lanes do not idle on points with fewer VPLs.
     for (uint32_t base = first + threadIdx.x - lane; base < cnt; base += kSplatThreads) {
@@ -238,9 +242,16 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             const uint32_t key = (f2u(vz) << 8) | rbyte;
             const int px = f2i(vx), py = f2i(vy);
             if (px < 0 || py < 0 || px >= atlas_w || py >= atlas_h) continue;  // image op out of range: no-op
-            atomicMin(keys + (size_t)py * atlas_w + px, key);
+            if (kCount)
+                ++issued;
+            else
+                atomicMin(keys + (size_t)py * atlas_w + px, key);
         }
         __syncwarp();  // the warp's tasks are consumed before the next points overwrite them
+    }
+    if (kCount) {
+        for (int o = 16; o > 0; o >>= 1) issued += __shfl_xor_sync(0xffffffffu, issued, o);
+        if (lane == 0 && issued) atomicAdd(atomics, (unsigned long long)issued);
     }
 }
 
@@ -252,6 +263,17 @@ __global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s) {
     if (a.n_groups <= 0) return cudaSuccess;
     ism_splat_kernel<<<a.n_groups * a.chunks, kSplatThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(kSplatThreads) ism_splat_count_kernel(SplatArgs a, unsigned long long* count) {
+    __shared__ SplatSmem S;
+    splat_bucket<true>(a, blockIdx.x, S, count);
+}
+
+cudaError_t launch_ism_splat_count(const SplatArgs& a, unsigned long long* count, cudaStream_t s) {
+    if (a.n_groups <= 0) return cudaSuccess;
+    ism_splat_count_kernel<<<a.n_groups * a.chunks, kSplatThreads, 0, s>>>(a, count);
     return cudaGetLastError();
 }
 

@@ -175,6 +175,8 @@ constexpr uint32_t kStatusTmaTimeout = 1u;
 cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s);
 cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s);
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s);
+// The atomics launch_ism_splat would issue (projections that land inside the atlas), added to *count.
+cudaError_t launch_ism_splat_count(const SplatArgs& a, unsigned long long* count, cudaStream_t s);
 // The pyramid of ISM rows [a.row0, a.row1). marks (optional): three events recorded after level
 // 1, the middle levels and push level 1.
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks = nullptr);

@@ -109,6 +109,7 @@ struct mlgi_ctx {
     DevBuf vpl, packed, reduced, keys, depth;
     DevBuf pp;  // pull-push pyramid levels 1 and 2
     DevBuf cl;  // clustered culling: used slices, cluster masks, pixel slices
+    DevBuf cnt;  // splat atomics counter
     // host-frame input copies
     DevBuf h_rsm_depth, h_rsm_normal, h_rsm_diffuse, h_points, h_counts, h_gdepth, h_gnormal, h_rgb;
     bool timing = false;
@@ -280,7 +281,7 @@ void mlgi_destroy(mlgi_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->shuffle_dev) cudaFree(kv.second);
-    for (DevBuf* b : {&ctx->vpl, &ctx->packed, &ctx->reduced, &ctx->keys, &ctx->depth, &ctx->pp, &ctx->cl, &ctx->h_rsm_depth,
+    for (DevBuf* b : {&ctx->vpl, &ctx->packed, &ctx->reduced, &ctx->keys, &ctx->depth, &ctx->pp, &ctx->cl, &ctx->cnt, &ctx->h_rsm_depth,
                       &ctx->h_rsm_normal, &ctx->h_rsm_diffuse, &ctx->h_points, &ctx->h_counts, &ctx->h_gdepth,
                       &ctx->h_gnormal, &ctx->h_rgb})
         if (b->p) cudaFree(b->p);
@@ -561,6 +562,24 @@ mlgi_status mlgi_ism_splat_range(mlgi_ctx* ctx, const mlgi_points* pts, const ml
     a.bucket0 = bucket0;
     a.n_groups = n_buckets;
     MLGI_CUDA(ctx, mlgi::launch_ism_splat(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_ism_splat_count(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
+                                 const mlgi_ism_params* p, const mlgi_atlas* atlas, uint64_t* atomics) {
+    if (!ctx) return MLGI_EINVAL;
+    if (!atomics) return fail(ctx, MLGI_EINVAL, "NULL argument");
+    mlgi::SplatArgs a;
+    mlgi_status st = build_splat_args(ctx, pts, vpls, n_vpl, p, atlas, a);
+    if (st != MLGI_OK) return st;
+    if ((st = ensure(ctx, ctx->cnt, sizeof(unsigned long long))) != MLGI_OK) return st;
+    unsigned long long* d = static_cast<unsigned long long*>(ctx->cnt.p);
+    unsigned long long h = 0;
+    MLGI_CUDA(ctx, cudaMemsetAsync(d, 0, sizeof(h), ctx->stream));
+    MLGI_CUDA(ctx, mlgi::launch_ism_splat_count(a, d, ctx->stream));
+    MLGI_CUDA(ctx, cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    MLGI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *atomics = h;
     return MLGI_OK;
 }
 

@@ -172,6 +172,8 @@ _SIGS = {
                                    C.POINTER(Atlas), _p]),
     "mlgi_pullpush": (C.c_int32, [_p, C.POINTER(Atlas), C.POINTER(IsmParams), _p]),
     "mlgi_ism_clear": (C.c_int32, [_p, C.POINTER(Atlas), _p]),
+    "mlgi_ism_splat_count": (C.c_int32, [_p, C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams),
+                                         C.POINTER(Atlas), C.POINTER(C.c_uint64)]),
     "mlgi_ism_splat_range": (C.c_int32, [_p, C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams),
                                          C.POINTER(Atlas), C.c_int, C.c_int, _p]),
     "mlgi_pullpush_rows": (C.c_int32, [_p, C.POINTER(Atlas), C.POINTER(IsmParams), C.c_int, C.c_int, _p]),
@@ -294,6 +296,12 @@ class Context:
 
     def pullpush(self, atlas: Atlas, params: IsmParams, stream: int = 0):
         return self._chk(lib().mlgi_pullpush(self.h, C.byref(atlas), C.byref(params), stream))
+
+    def ism_splat_count(self, pts: Points, vpls: VplBuf, n_vpl: int, params: IsmParams, atlas: Atlas) -> int:
+        n = C.c_uint64(0)
+        self._chk(lib().mlgi_ism_splat_count(self.h, C.byref(pts), C.byref(vpls), n_vpl, C.byref(params),
+                                             C.byref(atlas), C.byref(n)))
+        return int(n.value)
 
     def ism_clear(self, atlas: Atlas, stream: int = 0):
         return self._chk(lib().mlgi_ism_clear(self.h, C.byref(atlas), stream))

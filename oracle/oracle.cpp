@@ -172,12 +172,14 @@ struct SplatParams {
     int n_groups;           // dispatched work groups (sampledVplCount)
 };
 
+// issued (optional): the number of imageAtomicMin calls that land inside the atlas.
 template <class T>
 void ism_splat(const float* points, const uint32_t* counts, const T* vpl_pos, const uint32_t* vpl_pn, const SplatParams& p,
-               T zFar, uint32_t* atlas, int threads) {
+               T zFar, uint32_t* atlas, int threads, int64_t* issued = nullptr) {
     const int vplCount = p.vpl_end - p.vpl_start;
     const int maxTest = 16, maxCollect = 4;
-#pragma omp parallel for schedule(dynamic, 4) num_threads(set_threads(threads))
+    int64_t n_issued = 0;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(set_threads(threads)) reduction(+ : n_issued)
     for (int wg = 0; wg < p.n_groups; ++wg) {
         if (p.points_only_scaled && wg > vplCount) continue;
         V3<T> vp[16];
@@ -224,9 +226,11 @@ void ism_splat(const float* points, const uint32_t* counts, const T* vpl_pos, co
                 int tx = to_int(v.x), ty = to_int(v.y);
                 if (tx < 0 || ty < 0 || tx >= p.atlas_w || ty >= p.atlas_h) continue;  // image op out of range: no-op
                 atomic_min_u32(&atlas[(size_t)ty * p.atlas_w + tx], key);
+                ++n_issued;
             }
         }
     }
+    if (issued) *issued = n_issued;
 }
 
 // ---- S4/S5: pull.comp / push.comp driven by ImperfectShadowmap::pullpush --------------------
@@ -807,6 +811,15 @@ void oracle_ism_splat_f32(const float* points, const uint32_t* counts, int n_gro
                           int threads) {
     SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_groups);
     ism_splat<float>(points, counts, vpl_pos, vpl_pn, p, zfar, atlas, threads);
+}
+int64_t oracle_ism_splat_count_f32(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride,
+                                   const float* vpl_pos, const uint32_t* vpl_pn, int n_vpl, int vpl_start, int vpl_end,
+                                   int scale_isms, int points_only, int gx, int gy, int aw, int ah, float zfar,
+                                   uint32_t* atlas, int threads) {
+    SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_groups);
+    int64_t issued = 0;
+    ism_splat<float>(points, counts, vpl_pos, vpl_pn, p, zfar, atlas, threads, &issued);
+    return issued;
 }
 void oracle_ism_splat_f64(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride,
                           const double* vpl_pos, const uint32_t* vpl_pn, int n_vpl, int vpl_start, int vpl_end,

@@ -26,6 +26,7 @@ def lib() -> C.CDLL:
             mod.build()
         _lib = C.CDLL(LIB_PATH)
         _lib.oracle_max_threads.restype = C.c_int
+        _lib.oracle_ism_splat_count_f32.restype = C.c_int64
     return _lib
 
 
@@ -67,18 +68,23 @@ def vpl_process(rsm_depth, rsm_normal, rsm_diffuse, n, inv_bpv, intensity, shuff
 
 
 def ism_splat(points, counts, bucket_stride, vpl_pos, vpl_pn, n_vpl, ism_size, grid_x, grid_y, z_far,
-              vpl_start=0, vpl_end=None, scale_isms=0, points_only=0, threads=0, dtype=np.float32):
-    """ism.comp:54-139 after the atlas clear of ImperfectShadowmap.cpp:212. Returns uint32 keys (H, W)."""
+              vpl_start=0, vpl_end=None, scale_isms=0, points_only=0, threads=0, dtype=np.float32, count=False):
+    """ism.comp:54-139 after the atlas clear of ImperfectShadowmap.cpp:212. Returns uint32 keys (H, W);
+    with count=True (FP32 only) also the number of atomicMin calls that land inside the atlas."""
     vpl_end = n_vpl if vpl_end is None else vpl_end
     aw, ah = grid_x * ism_size, grid_y * ism_size
     atlas = np.full((ah, aw), 0xFFFFFFFF, np.uint32)
     n_groups = (vpl_end - vpl_start) if points_only else n_vpl
-    fn = lib().oracle_ism_splat_f32 if dtype == np.float32 else lib().oracle_ism_splat_f64
-    fn(_p(np.ascontiguousarray(points, np.float32)), _p(np.ascontiguousarray(counts, np.uint32)), n_groups,
-       C.c_int64(bucket_stride), _p(np.ascontiguousarray(vpl_pos, dtype)), _p(np.ascontiguousarray(vpl_pn, np.uint32)),
-       n_vpl, vpl_start, vpl_end, scale_isms, points_only, grid_x, grid_y, aw, ah, _f(dtype)(z_far), _p(atlas),
-       threads)
-    return atlas
+    if count:
+        assert dtype == np.float32
+        fn = lib().oracle_ism_splat_count_f32
+    else:
+        fn = lib().oracle_ism_splat_f32 if dtype == np.float32 else lib().oracle_ism_splat_f64
+    issued = fn(_p(np.ascontiguousarray(points, np.float32)), _p(np.ascontiguousarray(counts, np.uint32)), n_groups,
+                C.c_int64(bucket_stride), _p(np.ascontiguousarray(vpl_pos, dtype)),
+                _p(np.ascontiguousarray(vpl_pn, np.uint32)), n_vpl, vpl_start, vpl_end, scale_isms, points_only,
+                grid_x, grid_y, aw, ah, _f(dtype)(z_far), _p(atlas), threads)
+    return (atlas, int(issued)) if count else atlas
 
 
 def pullpush(keys, ism_size, levels, z_far, threads=0, dtype=np.float32):

@@ -84,6 +84,20 @@ def test_ism_splat_bit_exact(ctx, cfg):
     assert mism == 0, f"{mism} of {keys.size} atlas words differ"
 
 
+@pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2], ids=lambda c: c.name)
+def test_ism_splat_atomics_count(ctx, cfg):
+    """mlgi_ism_splat_count: the atomics the splat issues, equal to the oracle's count of
+    imageAtomicMin calls that land inside the atlas."""
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    n = ctx.ism_splat_count(df.points_view(), df.vpl_buf(), cfg.n_vpl, mlgi.ism_params(cfg), df.atlas_view())
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    _, want = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                          cfg.grid_y, cfg.z_far, count=True)
+    assert n == want and 0 < n <= 4 * int(sc.counts.sum())
+
+
 def test_ism_splat_vpl_subrange_and_scaled_isms(ctx):
     """VPLStartIndex/EndIndex with ScaleISMs and PointsOnlyToScaledISMs (ism.comp:31-40,56-66)."""
     import torch
