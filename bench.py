@@ -199,6 +199,19 @@ def config_dict(cfg):
                   "back inside the timed region)"}
 
 
+def reduce_max(values, world):
+    """Each value's maximum over the ranks (replicas run in parallel, so the job takes as long as
+    its slowest rank); the values themselves at world size 1."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 def run_reference(args, cfg, rank, world):
     if rank != 0:
         return
@@ -378,10 +391,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
 
     post = post_passes(ctx, df, scene, cfg, stream, flush, min(args.steps, 200), args.warmup)
 
-    if world > 1:
-        t = torch.tensor([total_ms, e2e_total], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms, e2e_total = float(t[0]), float(t[1])
+    total_ms, e2e_total = reduce_max([total_ms, e2e_total], world)
     if rank != 0:
         ctx.close()
         return
