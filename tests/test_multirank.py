@@ -17,7 +17,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank(rank, world, port, out):
+def _rank(rank, world, port, out_dir):
     import torch.distributed as dist
 
     sys.path.insert(0, ROOT)
@@ -25,19 +25,20 @@ def _rank(rank, world, port, out):
 
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     try:
-        out[rank] = bench.reduce_max([1.0 + rank, 10.0 - rank, 3.5], world)
+        got = bench.reduce_max([1.0 + rank, 10.0 - rank, 3.5], world)
+        with open(os.path.join(out_dir, f"rank{rank}.json"), "w") as f:
+            json.dump(got, f)
     finally:
         dist.destroy_process_group()
 
 
-def test_timings_reduce_to_the_slowest_rank():
+def test_timings_reduce_to_the_slowest_rank(tmp_path):
     import torch.multiprocessing as mp
 
     port = _free_port()
-    with mp.Manager() as m:
-        out = m.dict()
-        mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
-        assert out[0] == out[1] == [2.0, 10.0, 3.5]
+    mp.spawn(_rank, args=(2, port, str(tmp_path)), nprocs=2, join=True)  # spawn start method
+    got = [json.load(open(tmp_path / f"rank{r}.json")) for r in range(2)]
+    assert got[0] == got[1] == [2.0, 10.0, 3.5]
 
 
 def test_reference_arm_under_torchrun_two_ranks():
