@@ -243,7 +243,9 @@ def _oracle_fg(cfg, sc, df, dtype, tile=0, cutoff=0.0, reduced_inputs=False):
 
 
 @pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C1.replace(interleave=8, tile=8, name="c1_i8_t8"),
-                                              mlgi.C1.replace(interleave=1, name="c1_i1")], ids=lambda c: c.name)
+                                              mlgi.C1.replace(interleave=1, name="c1_i1"),
+                                              mlgi.C1.replace(width=637, height=357, cull=1, name="c1_ragged_cull")],
+                         ids=lambda c: c.name)
 def test_final_gather_matches_fp64_oracle(ctx, cfg):
     import torch
 
@@ -336,6 +338,34 @@ def test_host_frame_equals_device_frame(ctx, cfg):
         host = pinned["rgb"].numpy().reshape(dev.shape)
         assert np.abs(dev).max() > 0
         assert (dev.view(np.uint32) == host.view(np.uint32)).all()
+
+
+def test_host_frame_vpl_subrange_scaled_isms(ctx):
+    """A layout the overlapped schedule does not split (VPL subrange, scaled ISMs, points only into
+    them): every ISM row is pulled and pushed after the last point range; still the device frame's
+    result bit for bit."""
+    import torch
+
+    cfg = mlgi.C2
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    start, end = 256, 768
+    fd = df.frame_desc()
+    fd.ism.vpl_start, fd.ism.vpl_end, fd.ism.scale_isms, fd.ism.points_only_scaled = start, end, 1, 1
+    fd.points.n_buckets = end - start
+    fd.fg.vpl_start, fd.fg.vpl_end, fd.fg.scale_isms = start, end, 1
+    ctx.gi_frame(fd, df.radiance())
+    torch.cuda.synchronize()
+    dev = df.rgb_np().copy()
+    pinned = pinned_inputs(sc)
+    hfd = host_frame_desc(sc, pinned)
+    hfd.ism.vpl_start, hfd.ism.vpl_end, hfd.ism.scale_isms, hfd.ism.points_only_scaled = start, end, 1, 1
+    hfd.points.n_buckets = end - start
+    hfd.fg.vpl_start, hfd.fg.vpl_end, hfd.fg.scale_isms = start, end, 1
+    ctx.gi_frame_host(hfd, pinned["rgb"].numpy())
+    host = pinned["rgb"].numpy().reshape(dev.shape)
+    assert np.abs(dev).max() > 0
+    assert (dev.view(np.uint32) == host.view(np.uint32)).all()
 
 
 def test_frame_is_deterministic(ctx):
