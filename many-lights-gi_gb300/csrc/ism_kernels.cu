@@ -369,11 +369,15 @@ struct PullSample {
 };
 
 // One pull output from its four samples in the order (0,0), (0,1), (1,0), (1,1) (pull.comp:60-120).
-__device__ __forceinline__ float4 pull_combine(const PullSample (&q)[4], const float scale) {
+// dist1 >= 0: every sample's displacement length is this value (already rounded as sqrt rounds it).
+__device__ __forceinline__ float4 pull_combine(const PullSample (&q)[4], const float scale, const float dist1 = -1.0f) {
     bool valid[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k)  // dist <= radius * scale, dist = length(displacement)
-        valid[k] = q[k].depth != 1.0f && !sqrt_gt(q[k].ndx * q[k].ndx + q[k].ndy * q[k].ndy, q[k].radius * scale);
+    for (int k = 0; k < 4; ++k) {  // dist <= radius * scale, dist = length(displacement)
+        const bool far = dist1 >= 0.f ? dist1 > q[k].radius * scale
+                                      : sqrt_gt(q[k].ndx * q[k].ndx + q[k].ndy * q[k].ndy, q[k].radius * scale);
+        valid[k] = q[k].depth != 1.0f && !far;
+    }
     float minimum = __int_as_float(0x7f800000);
     float maxDepth = 0.f;
 #pragma unroll
@@ -425,7 +429,8 @@ __device__ __forceinline__ float4 pull1_texel(const PullPushArgs& a, const float
         q[k].ndx = kPullOff[k][0] ? 0.25f : -0.25f;
         q[k].ndy = kPullOff[k][1] ? 0.25f : -0.25f;
     }
-    return pull_combine(q, 0.5f);
+    // |(+-0.25, +-0.25)|^2 = 0.125 exactly, so every sample's length is RN(sqrt(0.125))
+    return pull_combine(q, 0.5f, sqrtf(0.125f));
 }
 
 // Pull level l >= 2 at global level-l texel (gox, goy); `in` is level l-1 with row pitch `pin`
