@@ -193,6 +193,7 @@ def config_dict(cfg):
             "points": cfg.n_points, "rsm": f"{cfg.rsm}x{cfg.rsm}",
             "ism": f"{cfg.ism_size}^2 x {cfg.grid_x}x{cfg.grid_y} = {cfg.atlas_w}x{cfg.atlas_h}",
             "pullpush_levels": cfg.levels, "interleave": cfg.interleave, "tile": cfg.tile, "cull": bool(cfg.cull),
+            "influence_cutoff": cfg.influence_cutoff,
             "precision": "fp16/bf16 storage, fp32 math" if cfg.reduced else "fp32",
             "scene": "seeded procedural room (100-unit Cornell box, boxes, spheres, spot light)",
             "l2": "flushed between steps (256 MiB write, then a 256 MiB read so that no dirty line is written "

@@ -429,8 +429,10 @@ class Config:
 # Plain method, small, FP32, one frame (640x360, 256 VPLs, 2^18 points, 64^2 ISMs, 4 levels, I=4).
 C1 = Config("c1_640x360_n256", 640, 360, 256, 256, 1 << 18, 64, 16, 16, 4, 4, 4, 2, tile=16, cull=0)
 # Plain method, full size (1080p, 1024 VPLs, 2^22 points, 128^2 ISMs in a 4096^2 atlas, 6 levels, I=8,
-# 16x16 tiles with per-tile culling).
-C2 = Config("c2_1920x1080_n1024", 1920, 1080, 512, 1024, 1 << 22, 128, 32, 32, 6, 8, 16, 8, tile=16, cull=1)
+# 16x16 tiles with per-tile culling: the VPL's half-space against the tile's box, and an influence
+# radius from flux, (max flux / cutoff)^(1/4); the cutoff 1e-8 is 1e-5 of the per-pair clamp).
+C2 = Config("c2_1920x1080_n1024", 1920, 1080, 512, 1024, 1 << 22, 128, 32, 32, 6, 8, 16, 8, tile=16, cull=1,
+            influence_cutoff=1e-8)
 # Reduced-precision form of C1 (FP16 atlas, FP16 normals, BF16 flux).
 C3 = C1.replace(name="c3_640x360_n256_fp16", reduced=True)
 # Reduced precision with 2048 VPLs at 96^2 ISMs on a 64x32 grid (6144x3072 atlas), 2^23 points.

@@ -261,15 +261,20 @@ def test_final_gather_matches_fp64_oracle(ctx, cfg):
 
 
 def test_final_gather_culling_c2(ctx):
-    """C2: 16x16 same-class tiles with culling. The lossless half-space cull must match the FP64
-    oracle that applies the same rule, and the no-cull FP64 oracle within the same bar."""
+    """C2: 16x16 same-class tiles with culling: the lossless half-space cull and the influence
+    radius from flux (cutoff 1e-8). The result must match the FP64 oracle that applies the same
+    rules, and the no-cull FP64 oracle, within the same bar."""
     import torch
 
     cfg = mlgi.C2
+    assert cfg.cull == 1 and cfg.influence_cutoff > 0
     sc, df = _fg_inputs(ctx, cfg)
     ctx.final_gather(df.gbuffer_view(), df.vpl_buf(), df.atlas_view(), df.fg(), df.radiance())
     torch.cuda.synchronize()
     rgb = df.rgb_np()
+    ref_cull = _oracle_fg(cfg, sc, df, np.float64, tile=cfg.tile, cutoff=cfg.influence_cutoff)
+    e = rel_l2(rgb, ref_cull)
+    assert e < FG_REL_L2, f"C2 culled vs culled FP64: rel L2 {e:.3e}"
     ref_nocull = _oracle_fg(cfg, sc, df, np.float64)
     e = rel_l2(rgb, ref_nocull)
     assert e < FG_REL_L2, f"C2 culled vs unculled FP64: rel L2 {e:.3e}"
