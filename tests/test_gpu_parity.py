@@ -402,3 +402,52 @@ def test_invalid_arguments_are_rejected(ctx):
     fp.interleave = 3  # 64 VPLs are not a multiple of 9
     with pytest.raises(mlgi.MlgiError):
         ctx.final_gather(df.gbuffer_view(), df.vpl_buf(), df.atlas_view(), fp, df.radiance())
+
+
+def _rejected(fn):
+    with pytest.raises(mlgi.MlgiError) as e:
+        fn()
+    assert e.value.status == mlgi.EINVAL, e.value
+
+
+def test_limits_and_inconsistent_layouts_are_rejected(ctx):
+    """Sizes past the kernels' limits and inconsistent layouts fail with EINVAL before any launch;
+    the context stays usable."""
+    import torch
+
+    cfg = mlgi.C0
+    df = DeviceFrame(scene(cfg))
+    run_vpl(ctx, df)
+    pts, vb, at = df.points_view(), df.vpl_buf(), df.atlas_view()
+
+    def ism(**kw):
+        ip = mlgi.ism_params(cfg)
+        for k, v in kw.items():
+            setattr(ip, k, v)
+        return ip
+
+    big = mlgi.Atlas(8 * 8192, 8 * 32, at.keys, at.depth, at.format)  # 65536 texels wide
+    _rejected(lambda: ctx.ism_splat(pts, vb, cfg.n_vpl, ism(ism_size=8192, grid_x=8, grid_y=8, levels=3), big))
+    _rejected(lambda: ctx.pullpush(at, ism(levels=0)))
+    _rejected(lambda: ctx.pullpush(at, ism(levels=11)))
+    _rejected(lambda: ctx.ism_splat(pts, vb, cfg.n_vpl, ism(grid_x=4, grid_y=4),
+                                    mlgi.Atlas(4 * cfg.ism_size, 4 * cfg.ism_size, at.keys, at.depth, at.format)))
+    bad_pts = df.points_view()
+    bad_pts.n_buckets = cfg.n_vpl - 1  # the splat samples one bucket per VPL
+    _rejected(lambda: ctx.ism_splat(bad_pts, vb, cfg.n_vpl, ism(), at))
+    _rejected(lambda: ctx.ism_splat(pts, vb, cfg.n_vpl, ism(vpl_start=8, vpl_end=8), at))
+    _rejected(lambda: ctx.ism_splat(pts, vb, cfg.n_vpl, ism(z_far=0.0), at))
+    for field, value in (("tile", 12), ("cull", 3), ("vpl_format", 7)):
+        fp = df.fg()
+        setattr(fp, field, value)
+        _rejected(lambda: ctx.final_gather(df.gbuffer_view(), vb, at, fp, df.radiance()))
+    # a NULL host input of the host-buffer frame
+    pinned = pinned_inputs(scene(cfg))
+    hfd = host_frame_desc(scene(cfg), pinned)
+    hfd.gbuffer.depth = None
+    _rejected(lambda: ctx.gi_frame_host(hfd, pinned["rgb"].numpy()))
+    # still usable: a valid frame runs after the rejections
+    ctx.gi_frame(df.frame_desc(), df.radiance())
+    ctx.check_device_status()
+    torch.cuda.synchronize()
+    assert np.abs(df.rgb_np()).max() > 0
