@@ -366,7 +366,7 @@ mlgi_status mlgi_ctx_reserve(mlgi_ctx* ctx, int max_vpl, size_t max_atlas_texels
 
 /* ---- request server ------------------------------------------------------------------------- */
 
-/* Continuous-batching server of GI frames on one GPU (served form of the frame driver; the
+/* Continuous-batching server of GI frames on one GPU (the served form of mlgi_gi_frame; the
  * reference renders one view per frame and has no server). A request names a room seed, a frame
  * shape and a pose; a scheduler thread admits queued requests FIFO into free slots (each slot a
  * context with its own stream and per-frame buffers), so frames of different requests overlap on
