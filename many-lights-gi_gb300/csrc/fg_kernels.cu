@@ -289,10 +289,15 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
             const int ism = vid - a.ism_index_offset;
             const int ty = ism / a.gx;
             const int tx = ism - ty * a.gx;
+            // the lookAtRH rows scaled by half the ISM size (the texel offset from the ISM centre is
+            // hs * s.d / (1 + a1)); d.w = 1 marks an ISM on or beyond the atlas border (a scaled
+            // layout gives VPLs outside the range ISM indices off the grid), the only ones whose
+            // texel can leave the atlas: |x| < 1 for every pair that reaches the lookup
+            const bool border = tx <= 0 || ty <= 0 || tx >= a.gx - 1 || ty >= a.gy - 1;
             S.a[k] = make_float4(p.x, p.y, p.z, f.x);
             S.b[k] = make_float4(n.x, n.y, n.z, f.y);
-            S.c[k] = make_float4(s.x, s.y, s.z, f.z);
-            S.d[k] = make_float4(u.x, u.y, u.z, 0.f);
+            S.c[k] = make_float4(s.x * hs, s.y * hs, s.z * hs, f.z);
+            S.d[k] = make_float4(u.x * hs, u.y * hs, u.z * hs, border ? 1.0f : 0.0f);
             S.org[k] = make_float2(float(tx * a.ism_size) + hs, float(ty * a.ism_size) + hs);
             bool keep = true;
             if (a.cull == 1) {
@@ -363,14 +368,14 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
                     // x = s.d / (1 - (-n).d), texel = floor(((x + 1)/2 + tile) * ismSize), d the
                     // normalised direction: s.d = (s.(p - v)) / |p - v|
                     const float rz = __fdividef(inv, 1.0f + a1);
-                    const float px = (C.x * dx + C.y * dy + C.z * dz) * rz;
-                    const float py = (D.x * dx + D.y * dy + D.z * dz) * rz;
-                    int ix = __float2int_rd(fmaf(px, hs, org.x));
-                    int iy = __float2int_rd(fmaf(py, hs, org.y));
-                    if (ix >= aw) ix -= aw;  // GL_REPEAT
-                    if (ix < 0) ix += aw;
-                    if (iy >= ah) iy -= ah;
-                    if (iy < 0) iy += ah;
+                    int ix = __float2int_rd(fmaf(C.x * dx + C.y * dy + C.z * dz, rz, org.x));
+                    int iy = __float2int_rd(fmaf(D.x * dx + D.y * dy + D.z * dz, rz, org.y));
+                    if (D.w != 0.f) {  // GL_REPEAT, for border ISMs only (uniform over the block)
+                        ix %= aw;
+                        if (ix < 0) ix += aw;
+                        iy %= ah;
+                        if (iy < 0) iy += ah;
+                    }
                     t = (uint32_t)iy * (uint32_t)aw + (uint32_t)ix;  // atlas sides <= 65535
                     vz = (d2 * inv) * inv_zfar;
                 }

@@ -260,6 +260,39 @@ def test_final_gather_matches_fp64_oracle(ctx, cfg):
     assert np.abs(ref).max() > 0
 
 
+def test_final_gather_scaled_isms_wrap_off_the_grid(ctx):
+    """ScaleISMs with vplStart 192 of 256 VPLs on an 8x8 grid: VPLs below the range have ISM
+    indices far off the grid (down to -192, tile rows down to -24), whose texels wrap around the
+    atlas (GL_REPEAT, a true modulo). Against the FP64 oracle with the same layout."""
+    import torch
+
+    cfg = mlgi.C1.replace(grid_x=8, grid_y=8, name="c1_grid8")
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    start, end = 192, 256
+    ip = mlgi.ism_params(cfg)
+    ip.vpl_start, ip.vpl_end, ip.scale_isms, ip.points_only_scaled = start, end, 1, 1
+    pts = df.points_view()
+    pts.n_buckets = end - start
+    ctx.ism_splat(pts, df.vpl_buf(), cfg.n_vpl, ip, df.atlas_view())
+    ctx.pullpush(df.atlas_view(), ip)
+    fp = df.fg()
+    fp.vpl_start, fp.vpl_end, fp.scale_isms = start, end, 1
+    ctx.final_gather(df.gbuffer_view(), df.vpl_buf(), df.atlas_view(), fp, df.radiance())
+    ctx.check_device_status()
+    torch.cuda.synchronize()
+    pos, nrm, col, _ = df.vpl_records()
+    ref = O.final_gather(sc.gbuf_depth, sc.gbuf_normal, sc.mat("inv_view_proj").astype(np.float64),
+                         pos.astype(np.float64), nrm.astype(np.float64), col.astype(np.float64), df.atlas_np(),
+                         cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.z_far, cfg.gi_intensity, cfg.clamp_value,
+                         cfg.interleave, vpl_count=end - start, ism_offset=start, dtype=np.float64)
+    got = df.rgb_np()
+    assert np.abs(ref).max() > 0
+    e = rel_l2(got, ref)
+    assert e < FG_REL_L2, f"rel L2 {e:.3e}"
+
+
 def test_final_gather_culling_c2(ctx):
     """C2: 16x16 same-class tiles with culling: the lossless half-space cull and the influence
     radius from flux (cutoff 1e-8). The result must match the FP64 oracle that applies the same
