@@ -98,10 +98,10 @@ cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s) {
 constexpr int kSplatThreads = 256;
 
 struct SplatSmem {
-    float4 pos[16], n[16];  // xyz used; float4 for 16-byte shared loads
+    // per VPL, 16-byte rows: (position, ISM tile x), (normal, ISM tile y), (lookAtRH s, 0),
+    // (lookAtRH u, 0); the tile offsets are float(x) and float(y) of ism_utils.glsl:35-37
+    float4 pos[16], n[16], s[16], u[16];
     float4 tasks[kSplatThreads / 32][128];  // per warp: (point xyz, VPL slot << 8 | radius byte)
-    v3 s[16], u[16];
-    float tx[16], ty[16];   // the VPL's ISM tile offsets, float(x) and float(y) (ism_utils.glsl:35-37)
     // per byte value b of a point's packed word, computed with the shader's own operations:
     float unorm[256];       // float(b) / 255 * 2 - 1, a normal component (ism.comp:81-85)
     uint8_t rbyte[256];     // uint(float(b) / 255 * 25 * 10 / 2), the key's radius byte (ism.comp:87, 131-136)
@@ -137,15 +137,13 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         const v3 n = unpack3SN(__float_as_uint(pk.w));
         v3 s, u;
         look_at_rows(n, s, u);
-        S.pos[threadIdx.x] = make_float4(pk.x, pk.y, pk.z, 0.f);
-        S.n[threadIdx.x] = make_float4(n.x, n.y, n.z, 0.f);
-        S.s[threadIdx.x] = s;
-        S.u[threadIdx.x] = u;
+        S.s[threadIdx.x] = make_float4(s.x, s.y, s.z, 0.f);
+        S.u[threadIdx.x] = make_float4(u.x, u.y, u.z, 0.f);
         const float ismIndex = a.scale_isms ? float(index) - float(a.vpl_start) : float(index);
         const float fgx = float(a.gx);
         const float ty = float(f2i(ismIndex / fgx));
-        S.tx[threadIdx.x] = float(f2i(ismIndex - ty * fgx));
-        S.ty[threadIdx.x] = float(f2i(ty));
+        S.pos[threadIdx.x] = make_float4(pk.x, pk.y, pk.z, float(f2i(ismIndex - ty * fgx)));
+        S.n[threadIdx.x] = make_float4(n.x, n.y, n.z, float(f2i(ty)));
     }
     for (int b = threadIdx.x; b < 256; b += kSplatThreads) {
         const float f = float(b) / 255.0f;
@@ -218,8 +216,9 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
             const float dist = length(rel);
             const v3 n = mk(vn.x, vn.y, vn.z);
-            float vx = dot(S.s[i], rel);
-            float vy = dot(S.u[i], rel);
+            const float4 vs = S.s[i], vu = S.u[i];
+            float vx = dot(mk(vs.x, vs.y, vs.z), rel);
+            float vy = dot(mk(vu.x, vu.y, vu.z), rel);
             float vz = ((-n.x) * rel.x + (-n.y) * rel.y) + (-n.z) * rel.z;
             const float signOfV = gsign(vz);
             vx = vx / dist;
@@ -232,8 +231,8 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             vz = vz * -signOfV;
             vx = (vx + 1.0f) / 2.0f;
             vy = (vy + 1.0f) / 2.0f;
-            vx = vx + S.tx[i];
-            vy = vy + S.ty[i];
+            vx = vx + vp.w;  // ISM tile x
+            vy = vy + vn.w;  // ISM tile y
             vx = rgx != 0.f ? vx * rgx : vx / fgx;
             vy = rgy != 0.f ? vy * rgy : vy / fgy;
             vx = vx * fw;
