@@ -188,6 +188,17 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     const int tid = threadIdx.x;
     const int I = a.interleave;
     const int cx = c % I, cy = c / I;
+    // the first VPL chunk's bulk copy starts now and completes behind the pixel setup (the
+    // previous tile's use of S.raw ended at its last barrier)
+    const int vbase = c * a.per_class;
+    const bool use_tma = ((size_t)vbase * kRec) % 16 == 0;
+    const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
+    const size_t bytes0 = (size_t)min(kMaxVplChunk, a.per_class) * kRec;
+    const bool early = use_tma && bytes0 % 16 == 0;
+    if (early && tid == 0) {
+        mbar_expect_tx(&S.bar, (uint32_t)bytes0);
+        tma_bulk_g2s(S.raw, src + (size_t)vbase * kRec, (uint32_t)bytes0, &S.bar);
+    }
     const int sw = (a.width + I - 1) / I;
     const int ntx = (sw + T - 1) / T;
     const int tix = tile % ntx, tiy = tile / ntx;
@@ -247,9 +258,6 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
 
     __syncthreads();  // the previous tile's use of S is over
 
-    const int vbase = c * a.per_class;
-    const bool use_tma = ((size_t)vbase * kRec) % 16 == 0;
-    const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
     const float hs = float(a.ism_size) * 0.5f;
     const float inv_zfar = 1.0f / a.z_far;
     float accx = 0.f, accy = 0.f, accz = 0.f;
@@ -258,7 +266,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         const int cnt = min(kMaxVplChunk, a.per_class - base);
         const size_t bytes = (size_t)cnt * kRec;
         if (use_tma && bytes % 16 == 0) {
-            if (tid == 0) {
+            if (tid == 0 && !(base == 0 && early)) {  // the first chunk's copy was issued at the start
                 mbar_expect_tx(&S.bar, (uint32_t)bytes);
                 tma_bulk_g2s(S.raw, src + (size_t)(vbase + base) * kRec, (uint32_t)bytes, &S.bar);
             }
