@@ -30,6 +30,19 @@ METRICS = [
 ]
 
 
+_BYTES = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+
+
+def _value(hdr, units, row, key, scale):
+    """The metric's value in base units (scale maps its unit to a factor), or None if absent."""
+    if key not in hdr or not row[hdr.index(key)]:
+        return None
+    u = units[hdr.index(key)]
+    if u not in scale:
+        return None
+    return float(row[hdr.index(key)].replace(",", "")) * scale[u]
+
+
 def report(path):
     out = subprocess.run(["ncu", "-i", path, "--page", "raw", "--csv"], stdout=subprocess.PIPE, text=True).stdout
     rows = list(csv.reader(io.StringIO(out)))
@@ -41,6 +54,19 @@ def report(path):
         for key, label in METRICS:
             if key in hdr:
                 print(f"| {label} (`{key}`) | {r[hdr.index(key)]} {units[hdr.index(key)]} |")
+        # achieved rates of this launch: DRAM and L2 bytes, and L2 atomic/reduction requests, per second
+        dur = _value(hdr, units, r, "gpu__time_duration.sum", {"nsecond": 1e-9, "ns": 1e-9, "usecond": 1e-6,
+                                                                  "us": 1e-6, "msecond": 1e-3, "ms": 1e-3})
+        if dur:
+            dram = sum(_value(hdr, units, r, k, _BYTES) or 0.0 for k in ("dram__bytes_read.sum", "dram__bytes_write.sum"))
+            print(f"| achieved DRAM GB/s (read + write / duration) | {dram / dur / 1e9:.1f} GB/s |")
+            sectors = _value(hdr, units, r, "lts__t_sectors.sum", {"sector": 1.0, "": 1.0})
+            if sectors is not None:
+                print(f"| achieved L2 GB/s (`lts__t_sectors.sum` x 32 B / duration) | {sectors * 32 / dur / 1e9:.1f} GB/s |")
+            atom = sum(_value(hdr, units, r, k, {"request": 1.0, "": 1.0}) or 0.0
+                       for k in ("lts__t_requests_srcunit_tex_op_red.sum", "lts__t_requests_srcunit_tex_op_atom.sum"))
+            if atom:
+                print(f"| L2 atomic and reduction requests | {atom:.0f} ({atom / dur / 1e9:.1f} G/s) |")
         stalls = []
         for i, h in enumerate(hdr):
             if h.startswith("smsp__average_warps_issue_stalled") and h.endswith("per_issue_active.ratio") and r[i]:
