@@ -95,14 +95,15 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+def ncu_traffic(kernel, key="traffic"):
+    """Per-launch DRAM bytes (key "traffic") or issue-slot use in percent (key "issue") of `kernel`
+    from the committed ncu summary, if any."""
     for fn in sorted(os.listdir(os.path.join(ROOT, "profiles"))) if os.path.isdir(os.path.join(ROOT, "profiles")) else []:
         try:
             txt = open(os.path.join(ROOT, "profiles", fn)).read()
         except Exception:
             continue
-        m = re.search(r"traffic\[" + re.escape(kernel) + r"\]\s*=\s*([0-9.eE+]+)", txt)
+        m = re.search(re.escape(key) + r"\[" + re.escape(kernel) + r"\]\s*=\s*([0-9.eE+]+)", txt)
         if m:
             return float(m.group(1))
     return None
@@ -430,8 +431,10 @@ def run_gpu(args, cfg, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": ab[dom_name], "traffic": traffic,
-                     "note": "FP32-issue-bound kernels (bit-exact IEEE division, no FMA contraction); "
-                             "issue-slot use is in the committed ncu summary"},
+                     "issue_busy_pct": ncu_traffic(dom_name, "issue"),
+                     "note": "FP32-issue-bound kernels (bit-exact IEEE division, no FMA contraction): "
+                             "issue_busy_pct is the dominant kernel's issue-slot use from the committed "
+                             "ncu summary"},
         "per_pass_frac": {n: ab[n] / (mean_pass[i] * 1e-3) / 1e9 / peak for i, n in enumerate(PASSES)
                           if mean_pass[i] > 0},
         "per_kernel_frac": {n: ab[n] / (t * 1e-3) / 1e9 / peak for n, t in kernel_ms.items() if t > 0},

@@ -4,7 +4,8 @@
     python -m mlgi.ncu_summary launches.csv    > launches_<workload>.md
 
 A report summary ends each kernel with a `traffic[<kernel>] = <bytes>` line (DRAM read + write of
-one launch), which bench.py reads for the roofline's `traffic`.
+one launch) and an `issue[<kernel>] = <percent>` line (issue slots busy), which bench.py reads for
+the roofline's `traffic` and `issue_busy_pct`.
 """
 import collections
 import csv
@@ -83,7 +84,11 @@ def report(path):
         passes = {"vpl_process_kernel": "vpl_process", "ism_clear_kernel": "ism_clear", "ism_splat_kernel": "ism_splat",
                   "pull1_kernel": "pull1", "pullmid_kernel": "pullmid", "push1_kernel": "push1",
                   "push0_kernel": "push0", "fg_kernel": "final_gather"}
-        print(f"traffic[{passes.get(short, short)}] = {rd + wr:.4e}  (DRAM read + write bytes of this launch)\n")
+        print(f"traffic[{passes.get(short, short)}] = {rd + wr:.4e}  (DRAM read + write bytes of this launch)")
+        issue = _value(hdr, units, r, "smsp__issue_active.avg.pct_of_peak_sustained_active", {"%": 1.0})
+        if issue is not None:
+            print(f"issue[{passes.get(short, short)}] = {issue:.1f}  (% of issue slots busy while a warp is resident)")
+        print()
 
 
 def launches(path):

@@ -1,0 +1,27 @@
+"""The committed ncu summary of the C2 frame carries, for every kernel of the frame that ncu
+captured, the per-launch DRAM bytes and issue-slot use that bench.py reports beside the roofline
+fraction, and bench.py reads them back."""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+KERNELS = ["ism_clear", "ism_splat", "pull1", "pullmid", "push1", "push0", "final_gather"]
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_summary_has_traffic_and_issue(kernel):
+    traffic = bench.ncu_traffic(kernel)
+    issue = bench.ncu_traffic(kernel, "issue")
+    assert traffic is not None and 1e6 < traffic < 1e9, traffic
+    assert issue is not None and 0.0 < issue <= 100.0, issue
+
+
+def test_unknown_kernel_reads_none():
+    assert bench.ncu_traffic("no_such_kernel") is None
+    assert bench.ncu_traffic("no_such_kernel", "issue") is None
