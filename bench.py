@@ -164,29 +164,45 @@ def cpu_frame_runner(cfg, scene):
 
     perm = mlgi.shuffle_table(cfg.n_vpl)
 
-    def frame():
+    def frame(passes=None):
+        """One frame; `passes`, when given, receives each pass's wall time in ms (the splat pass
+        includes the atlas clear, as the oracle's splat returns a fresh atlas)."""
+        t = [time.perf_counter()]
         pos, nrm, col, pn = O.vpl_process(scene.rsm_depth, scene.rsm_normal, scene.rsm_diffuse, cfg.n_vpl,
                                           scene.mat("inv_biased_light_vp"), cfg.light_intensity, 1, perm)
+        t.append(time.perf_counter())
         keys = O.ism_splat(scene.points, scene.counts, scene.bucket_stride, pos, pn, cfg.n_vpl, cfg.ism_size,
                            cfg.grid_x, cfg.grid_y, cfg.z_far)
+        t.append(time.perf_counter())
         fin = O.pullpush(keys, cfg.ism_size, cfg.levels, cfg.z_far)
-        return O.final_gather(scene.gbuf_depth, scene.gbuf_normal, scene.mat("inv_view_proj"), pos, nrm, col, fin,
-                              cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.z_far, cfg.gi_intensity, cfg.clamp_value,
-                              cfg.interleave, tile=cfg.tile if cfg.cull else 0, cutoff=cfg.influence_cutoff)
+        t.append(time.perf_counter())
+        out = O.final_gather(scene.gbuf_depth, scene.gbuf_normal, scene.mat("inv_view_proj"), pos, nrm, col, fin,
+                             cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.z_far, cfg.gi_intensity, cfg.clamp_value,
+                             cfg.interleave, tile=cfg.tile if cfg.cull else 0, cutoff=cfg.influence_cutoff)
+        t.append(time.perf_counter())
+        if passes is not None:
+            for name, a, b in zip(CPU_PASSES, t, t[1:]):
+                passes.setdefault(name, []).append((b - a) * 1e3)
+        return out
 
     return frame, O.max_threads()
 
 
+CPU_PASSES = ("vpl_process", "ism_clear+ism_splat", "pullpush", "final_gather")
+
+
 def time_cpu(cfg, scene, budget_s, min_frames=2):
+    """Median ms per frame of the CPU chain, the median of each pass, the threads used and the
+    number of frames timed."""
     frame, threads = cpu_frame_runner(cfg, scene)
     frame()  # warm
-    times = []
+    times, passes = [], {}
     t_end = time.perf_counter() + budget_s
     while len(times) < min_frames or time.perf_counter() < t_end:
         t0 = time.perf_counter()
-        frame()
+        frame(passes)
         times.append((time.perf_counter() - t0) * 1e3)
-    return statistics.median(times), threads, len(times)
+    return statistics.median(times), threads, len(times), {n: statistics.median(v) for n, v in passes.items()}
 
 
 def config_dict(cfg):
@@ -224,11 +240,11 @@ def run_reference(args, cfg, rank, world):
     for _ in range(min(args.warmup, 1)):
         frame()
     # each step is one full frame on the host cores; the run is bounded to about a minute of frames
-    times = []
+    times, passes = [], {}
     t_start = time.perf_counter()
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        frame()
+        frame(passes)
         times.append((time.perf_counter() - t0) * 1e3)
         if time.perf_counter() - t_start > args.reference_seconds and len(times) >= 3:
             break
@@ -240,7 +256,8 @@ def run_reference(args, cfg, rank, world):
             "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{len(times)} of {args.steps} full frames of {cfg.name} (bounded to about "
                                        f"{args.reference_seconds:.0f} s), FP32 oracle restatement of the reference "
-                                       f"shaders, OpenMP on {threads} threads"},
+                                       f"shaders, OpenMP on {threads} threads",
+                             "passes_ms": {n: statistics.mean(v) for n, v in passes.items()}},
             "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -443,10 +460,11 @@ def run_gpu(args, cfg, rank, world, local_rank):
         "post": post,
     }
     if not args.no_cpu_baseline and world == 1:
-        ms, threads, nframes = time_cpu(cfg, scene, args.cpu_seconds)
+        ms, threads, nframes, cpu_passes = time_cpu(cfg, scene, args.cpu_seconds)
         line["cpu_baseline"] = {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{nframes} full {cfg.name} frames (median), FP32 oracle restatement "
-                                          f"of the reference shaders, OpenMP on {threads} threads"}
+                                          f"of the reference shaders, OpenMP on {threads} threads",
+                                "passes_ms": cpu_passes}
     print(json.dumps(line), flush=True)
     ctx.close()
 

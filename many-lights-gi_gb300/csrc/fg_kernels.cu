@@ -5,7 +5,9 @@
 // Work mapping. Pixel (x, y) belongs to interleave class c = (x % I) + (y % I) * I and gathers
 // the class's VPL slice [c*N/I^2, (c+1)*N/I^2). A block is a T x T tile of one class in the
 // de-interleaved sub-image (pixels (i*I + cx, j*I + cy)), so every thread of a block walks the
-// same VPL list and reads each VPL from shared memory as a broadcast. The slice is staged with
+// same VPL list and reads each VPL from shared memory as a broadcast. A thread owns two
+// horizontally adjacent pixels of the tile and evaluates a VPL for both with packed FP32x2
+// arithmetic (T*T/2 threads a block). The slice is staged with
 // a 1-D bulk TMA copy (cp.async.bulk) completed on an mbarrier whose wait is bounded; per-VPL
 // derived data (lookAtRH rows, ISM tile origin) is computed once per block. With culling on,
 // the block reduces its pixels' world-space bounding box and drops VPLs whose front half-space
@@ -20,10 +22,13 @@
 
 namespace mlgi {
 
-constexpr int kMaxVplChunk = 128;
-// pixel-VPL pairs evaluated per iteration of the gather loop (3 measured best: 4 spills at the
-// 64-register budget of four blocks per SM, and fewer blocks cost more than they gain)
-constexpr int kPairs = 3;
+// VPLs staged per chunk: 64 for 16 x 16 tiles (13 KB of shared memory a block; with 128 the
+// gathering ran 5 % slower at 1080p, the larger carve-out leaving less L1 for the atlas and
+// G-buffer loads) and 32 for 8 x 8 tiles (one-warp blocks, many resident)
+template <int T>
+__host__ __device__ constexpr int fg_chunk() {
+    return T == 16 ? 64 : 32;
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -164,36 +169,84 @@ __device__ __forceinline__ v3 oct_decode(float ex, float ey) {
     return normalize_fast(n);
 }
 
-// Shared memory of one final-gathering block (one tile of one interleave class).
-template <int NT>
+// ---- two pixels per thread on packed FP32x2 arithmetic ---------------------------------------
+// Blackwell's add/sub/mul/fma.f32x2 perform two FP32 operations in one instruction. A thread owns
+// two horizontally adjacent pixels of the de-interleaved tile (lane 0 and lane 1 of every packed
+// value), and every value of a VPL is stored twice in shared memory, so that one 128-bit load
+// yields two packed operands that apply to both pixels. Each pixel still accumulates its VPLs in
+// ascending list order.
+struct f2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ f2 pk(float a) { return pk(a, a); }
+__device__ __forceinline__ void split(f2 a, float& x, float& y) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+}
+__device__ __forceinline__ f2 operator+(f2 a, f2 b) {
+    f2 r;
+    asm("add.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 operator-(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 operator*(f2 a, f2 b) {
+    f2 r;
+    asm("mul.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {  // a * b + c
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// One VPL with every value twice, as (v, v) 64-bit pairs: position, normal, the lookAtRH rows
+// scaled by half the ISM size, the ISM tile origin, flux and the border flag.
+struct VplPk {
+    ulonglong2 r[9];  // (p.x, p.y) (p.z, n.x) (n.y, n.z) (s.x, s.y) (s.z, u.x) (u.y, u.z) (org) (f.x, f.y) (f.z, border)
+};
+
+// Shared memory of one final-gathering block (one T x T tile of one interleave class).
+template <int T>
 struct FgSmem {
-    __align__(128) unsigned char raw[kMaxVplChunk * 48];  // VPL records staged by the bulk copy
-    float4 a[kMaxVplChunk], b[kMaxVplChunk], c[kMaxVplChunk], d[kMaxVplChunk];
-    float2 org[kMaxVplChunk];  // ISM tile origin (texels) + half ISM size folded in
-    int list[kMaxVplChunk];
-    unsigned char flag[kMaxVplChunk];
-    float box[6][NT / 32];
+    static constexpr int kChunk = fg_chunk<T>(), kThreads = T * T / 2;
+    __align__(128) unsigned char raw[kChunk * 48];  // VPL records staged by the bulk copy
+    VplPk v[kChunk];
+    int list[kChunk];
+    unsigned char flag[kChunk];
+    float box[6][(kThreads + 31) / 32];
     int n;
     __align__(8) uint64_t bar;
 };
 
-// One T x T tile of interleave class c. The caller initialises S.bar once and keeps `parity`
-// across calls. Returns false (block-uniform) when the VPL staging wait timed out.
-// kClusters: compile the clustered-culling path (cull == 2), which batched views do not use
+// One T x T tile of interleave class c with T*T/2 threads. The caller initialises S.bar once and
+// keeps `parity` across calls. Returns false (block-uniform) when the VPL staging wait timed out.
+// kClusters: compile the clustered-culling path (cull == 2), which batched views do not use.
 template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16, bool kClusters = true>
-__device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const int c, FgSmem<T * T>& S,
+__device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const int c, FgSmem<T>& S,
                                         uint32_t& parity) {
-    constexpr int NT = T * T;
+    constexpr int NT = T * T / 2, HT = T / 2, NW = (NT + 31) / 32, kChunk = fg_chunk<T>();
     constexpr int kRec = kReduced ? 24 : 48;
     const int tid = threadIdx.x;
     const int I = a.interleave;
     const int cx = c % I, cy = c / I;
-    // the first VPL chunk's bulk copy starts now and completes behind the pixel setup (the
-    // previous tile's use of S.raw ended at its last barrier)
     const int vbase = c * a.per_class;
     const bool use_tma = ((size_t)vbase * kRec) % 16 == 0;
     const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
-    const size_t bytes0 = (size_t)min(kMaxVplChunk, a.per_class) * kRec;
+    const size_t bytes0 = (size_t)min(kChunk, a.per_class) * kRec;
     const bool early = use_tma && bytes0 % 16 == 0;
     if (early && tid == 0) {
         mbar_expect_tx(&S.bar, (uint32_t)bytes0);
@@ -202,15 +255,19 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     const int sw = (a.width + I - 1) / I;
     const int ntx = (sw + T - 1) / T;
     const int tix = tile % ntx, tiy = tile / ntx;
-    const int x = (tix * T + tid % T) * I + cx;
-    const int y = (tiy * T + tid / T) * I + cy;
-    const bool valid = x < a.width && y < a.height;
+    // a warp takes a band of adjacent tile rows: its pixels' ISM texels for one VPL are close
+    // together (rows interleaved over the warps ran 2 % slower)
+    const int y = (tiy * T + tid / HT) * I + cy;
+    const int x0 = (tix * T + 2 * (tid % HT)) * I + cx, x1 = x0 + I;
+    const bool v0 = x0 < a.width && y < a.height, v1 = x1 < a.width && y < a.height;
 
     // ---- pixel setup: world position from depth (final_gathering.comp:70-76, evaluated with
     // compensated arithmetic) and the octahedral normal ----
-    v3 fw = mk(0.f, 0.f, 0.f), fn = mk(0.f, 0.f, 1.f);
-    const uint32_t* cl_row = nullptr;  // cull == 2: the keep bits of the pixel's cluster
-    if (valid) {
+    auto setup = [&](int x, bool valid, v3& fw, v3& fn, const uint32_t*& cl_row) {
+        fw = mk(0.f, 0.f, 0.f);
+        fn = mk(0.f, 0.f, 1.f);
+        cl_row = nullptr;
+        if (!valid) return;
         const size_t pix = (size_t)y * a.width + x;
         const float d = __ldg(a.depth + pix);
         fw = reconstruct_world(a.inv_vp, x, y, a.width, a.height, a.inv_w, a.inv_h, d);
@@ -229,14 +286,19 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
             const int cluster = ((y / kClusterPixels) * a.cl_tiles_x + x / kClusterPixels) * kClusterSlices + a.cl_slice[pix];
             cl_row = a.cl_masks + (size_t)cluster * a.cl_words;
         }
-    }
+    };
+    v3 w0, n0, w1, n1;
+    const uint32_t *cl0, *cl1;
+    setup(x0, v0, w0, n0, cl0);
+    setup(x1, v1, w1, n1, cl1);
 
     // ---- per-tile bounds for culling ----
     v3 bmin = mk(0.f, 0.f, 0.f), bmax = mk(0.f, 0.f, 0.f);
     if (a.cull == 1) {
         const float inf = __int_as_float(0x7f800000);
-        float b[6] = {valid ? fw.x : inf,  valid ? fw.y : inf,  valid ? fw.z : inf,
-                      valid ? -fw.x : inf, valid ? -fw.y : inf, valid ? -fw.z : inf};
+        float b[6] = {fminf(v0 ? w0.x : inf, v1 ? w1.x : inf),   fminf(v0 ? w0.y : inf, v1 ? w1.y : inf),
+                      fminf(v0 ? w0.z : inf, v1 ? w1.z : inf),   fminf(v0 ? -w0.x : inf, v1 ? -w1.x : inf),
+                      fminf(v0 ? -w0.y : inf, v1 ? -w1.y : inf), fminf(v0 ? -w0.z : inf, v1 ? -w1.z : inf)};
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
 #pragma unroll
@@ -250,7 +312,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             r[k] = S.box[k][0];
-            for (int w = 1; w < NT / 32; ++w) r[k] = fminf(r[k], S.box[k][w]);
+            for (int w = 1; w < NW; ++w) r[k] = fminf(r[k], S.box[k][w]);
         }
         bmin = mk(r[0], r[1], r[2]);
         bmax = mk(-r[3], -r[4], -r[5]);
@@ -260,10 +322,12 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
 
     const float hs = float(a.ism_size) * 0.5f;
     const float inv_zfar = 1.0f / a.z_far;
-    float accx = 0.f, accy = 0.f, accz = 0.f;
+    const f2 fwx = pk(w0.x, w1.x), fwy = pk(w0.y, w1.y), fwz = pk(w0.z, w1.z);
+    const f2 fnx = pk(n0.x, n1.x), fny = pk(n0.y, n1.y), fnz = pk(n0.z, n1.z);
+    f2 accx = pk(0.f), accy = pk(0.f), accz = pk(0.f);
 
-    for (int base = 0; base < a.per_class; base += kMaxVplChunk) {
-        const int cnt = min(kMaxVplChunk, a.per_class - base);
+    for (int base = 0; base < a.per_class; base += kChunk) {
+        const int cnt = min(kChunk, a.per_class - base);
         const size_t bytes = (size_t)cnt * kRec;
         if (use_tma && bytes % 16 == 0) {
             if (tid == 0 && !(base == 0 && early)) {  // the first chunk's copy was issued at the start
@@ -285,7 +349,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
                     __ldg(reinterpret_cast<const uint32_t*>(src + (size_t)(vbase + base) * kRec + k));
             __syncthreads();
         }
-        // derive per-VPL data and the cull flag
+        // derive per-VPL data (every value stored twice) and the cull flag
         for (int k = tid; k < cnt; k += NT) {
             v3 p, n, f;
             decode_vpl<kReduced>(S.raw + (size_t)k * kRec, p, n, f);
@@ -297,16 +361,21 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
             const int ism = vid - a.ism_index_offset;
             const int ty = ism / a.gx;
             const int tx = ism - ty * a.gx;
-            // the lookAtRH rows scaled by half the ISM size (the texel offset from the ISM centre is
-            // hs * s.d / (1 + a1)); d.w = 1 marks an ISM on or beyond the atlas border (a scaled
-            // layout gives VPLs outside the range ISM indices off the grid), the only ones whose
-            // texel can leave the atlas: |x| < 1 for every pair that reaches the lookup
+            // the lookAtRH rows are scaled by half the ISM size (the texel offset from the ISM
+            // centre is hs * s.d / (1 + a1)); border = 1 marks an ISM on or beyond the atlas border
+            // (a scaled layout gives VPLs outside the range ISM indices off the grid), the only
+            // ones whose texel can leave the atlas: |x| < 1 for every pair that reaches the lookup
             const bool border = tx <= 0 || ty <= 0 || tx >= a.gx - 1 || ty >= a.gy - 1;
-            S.a[k] = make_float4(p.x, p.y, p.z, f.x);
-            S.b[k] = make_float4(n.x, n.y, n.z, f.y);
-            S.c[k] = make_float4(s.x * hs, s.y * hs, s.z * hs, f.z);
-            S.d[k] = make_float4(u.x * hs, u.y * hs, u.z * hs, border ? 1.0f : 0.0f);
-            S.org[k] = make_float2(float(tx * a.ism_size) + hs, float(ty * a.ism_size) + hs);
+            VplPk& R = S.v[k];
+            R.r[0] = make_ulonglong2(pk(p.x).v, pk(p.y).v);
+            R.r[1] = make_ulonglong2(pk(p.z).v, pk(n.x).v);
+            R.r[2] = make_ulonglong2(pk(n.y).v, pk(n.z).v);
+            R.r[3] = make_ulonglong2(pk(s.x * hs).v, pk(s.y * hs).v);
+            R.r[4] = make_ulonglong2(pk(s.z * hs).v, pk(u.x * hs).v);
+            R.r[5] = make_ulonglong2(pk(u.y * hs).v, pk(u.z * hs).v);
+            R.r[6] = make_ulonglong2(pk(float(tx * a.ism_size) + hs).v, pk(float(ty * a.ism_size) + hs).v);
+            R.r[7] = make_ulonglong2(pk(f.x).v, pk(f.y).v);
+            R.r[8] = make_ulonglong2(pk(f.z).v, pk(border ? 1.0f : 0.0f).v);
             bool keep = true;
             if (a.cull == 1) {
                 // front half-space of the VPL against the box corner farthest along its normal
@@ -338,118 +407,154 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         }
         __syncthreads();
 
-        // ---- gather over the kept list (final_gathering.comp:97-130) ----
+        // ---- gather over the kept list (final_gathering.comp:97-130), two pixels per thread ----
         const int nk = S.n;
-        if (valid) {
+        if (v0 || v1) {
             const float* atlas32 = reinterpret_cast<const float*>(a.atlas);
             const __half* atlas16 = reinterpret_cast<const __half*>(a.atlas);
-            // per-pair parameters in registers (a may live in shared memory in the batched form)
             const float clampv = a.clamp_value;
             const bool shadow = a.shadowing != 0;
             const int aw = a.atlas_w, ah = a.atlas_h;
-            // One pair: fG = flux * G (the geometry term G clamped as in the shader), the ISM texel
-            // index t and the pixel's normalised distance vz for the shadow test.
-            auto prepare = [&](int k, float3& fG, float& vz, uint32_t& t) -> bool {
-                if (kClusters && cl_row) {  // outside the pixel's cluster list
+            const f2 one = pk(1.0f), izf = pk(inv_zfar);
+            // One VPL against both pixels: G the clamped geometry term per pixel (0 for a pixel the
+            // pair does not reach), the ISM texel index per pixel and the normalised distance vz.
+            auto prepare = [&](int k, f2& G, f2& vz, uint32_t& t0, uint32_t& t1, bool& ok0, bool& ok1) -> bool {
+                ok0 = v0;
+                ok1 = v1;
+                if (kClusters && a.cull == 2) {  // outside the pixel's cluster list
                     const int vid = vbase + base + k;
-                    if (!((__ldg(cl_row + (vid >> 5)) >> (vid & 31)) & 1u)) return false;
+                    if (cl0) ok0 = ok0 && ((__ldg(cl0 + (vid >> 5)) >> (vid & 31)) & 1u);
+                    if (cl1) ok1 = ok1 && ((__ldg(cl1 + (vid >> 5)) >> (vid & 31)) & 1u);
                 }
-                const float4 A = S.a[k], B = S.b[k];
-                const float dx = fw.x - A.x, dy = fw.y - A.y, dz = fw.z - A.z;
+                const VplPk& R = S.v[k];
+                const ulonglong2 R0 = R.r[0], R1 = R.r[1], R2 = R.r[2];
+                const f2 dx = fwx - f2{R0.x}, dy = fwy - f2{R0.y}, dz = fwz - f2{R1.x};
                 // the cosine terms have the signs of these dot products with the unnormalised
                 // direction: most pairs end here, before the square root (max(0, a1) *
                 // max(0, a2) > 0 needs a1 > 0 and a2 > 0)
-                const float e1 = B.x * dx + B.y * dy + B.z * dz;
-                const float e2 = fn.x * dx + fn.y * dy + fn.z * dz;
-                if (!(e1 > 0.f && e2 < 0.f)) return false;
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                const float inv = rsqrtf(d2);
-                const float a1 = e1 * inv, a2 = -e2 * inv;
-                const float att = (inv * inv) * (inv * inv);
-                const float G = fminf((a1 * a2) * att, clampv);
-                const float4 C = S.c[k];
-                fG = make_float3(A.w * G, B.w * G, C.w * G);
+                const f2 e1 = fma2(f2{R1.y}, dx, fma2(f2{R2.x}, dy, f2{R2.y} * dz));
+                const f2 e2 = fma2(fnx, dx, fma2(fny, dy, fnz * dz));
+                float e1a, e1b, e2a, e2b;
+                split(e1, e1a, e1b);
+                split(e2, e2a, e2b);
+                ok0 = ok0 && e1a > 0.f && e2a < 0.f;
+                ok1 = ok1 && e1b > 0.f && e2b < 0.f;
+                if (!(ok0 || ok1)) return false;
+                const f2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
+                float d2a, d2b;
+                split(d2, d2a, d2b);
+                const f2 inv = pk(rsqrtf(d2a), rsqrtf(d2b));
+                const f2 a1 = e1 * inv, a2n = e2 * inv;  // a2 = -a2n
+                const f2 i2 = inv * inv;
+                float ga, gb;  // -(a1 * a2) / d^4
+                split((a1 * a2n) * (i2 * i2), ga, gb);
+                G = pk(ok0 ? fminf(-ga, clampv) : 0.f, ok1 ? fminf(-gb, clampv) : 0.f);
                 if (shadow) {
-                    const float4 D = S.d[k];
-                    const float2 org = S.org[k];
-                    // paraboloid_project(diff, dist, n, zFar, ismIndex, grid, false):
-                    // x = s.d / (1 - (-n).d), texel = floor(((x + 1)/2 + tile) * ismSize), d the
-                    // normalised direction: s.d = (s.(p - v)) / |p - v|
-                    const float rz = __fdividef(inv, 1.0f + a1);
-                    int ix = __float2int_rd(fmaf(C.x * dx + C.y * dy + C.z * dz, rz, org.x));
-                    int iy = __float2int_rd(fmaf(D.x * dx + D.y * dy + D.z * dz, rz, org.y));
-                    if (D.w != 0.f) {  // GL_REPEAT, for border ISMs only (uniform over the block)
-                        ix %= aw;
-                        if (ix < 0) ix += aw;
-                        iy %= ah;
-                        if (iy < 0) iy += ah;
+                    const ulonglong2 R3 = R.r[3], R4 = R.r[4], R5 = R.r[5], R6 = R.r[6];
+                    float qa, qb;
+                    split(a1 + one, qa, qb);
+                    const f2 rz = inv * pk(rcp_approx(qa), rcp_approx(qb));
+                    const f2 sx = fma2(fma2(f2{R3.x}, dx, fma2(f2{R3.y}, dy, f2{R4.x} * dz)), rz, f2{R6.x});
+                    const f2 sy = fma2(fma2(f2{R4.y}, dx, fma2(f2{R5.x}, dy, f2{R5.y} * dz)), rz, f2{R6.y});
+                    float sxa, sxb, sya, syb;
+                    split(sx, sxa, sxb);
+                    split(sy, sya, syb);
+                    int ix0 = __float2int_rd(sxa), ix1 = __float2int_rd(sxb);
+                    int iy0 = __float2int_rd(sya), iy1 = __float2int_rd(syb);
+                    float bf, unused;
+                    split(f2{R.r[8].y}, bf, unused);
+                    if (bf != 0.f) {  // GL_REPEAT, for border ISMs only (uniform over the block)
+                        ix0 %= aw;
+                        if (ix0 < 0) ix0 += aw;
+                        ix1 %= aw;
+                        if (ix1 < 0) ix1 += aw;
+                        iy0 %= ah;
+                        if (iy0 < 0) iy0 += ah;
+                        iy1 %= ah;
+                        if (iy1 < 0) iy1 += ah;
                     }
-                    t = (uint32_t)iy * (uint32_t)aw + (uint32_t)ix;  // atlas sides <= 65535
-                    vz = (d2 * inv) * inv_zfar;
+                    t0 = ok0 ? (uint32_t)iy0 * (uint32_t)aw + (uint32_t)ix0 : 0u;
+                    t1 = ok1 ? (uint32_t)iy1 * (uint32_t)aw + (uint32_t)ix1 : 0u;
+                    vz = (d2 * inv) * izf;
                 }
                 return true;
             };
             auto occluder = [&](uint32_t t) -> float {
                 return kAtlasF16 ? __half2float(__ldg(atlas16 + t)) : __ldg(atlas32 + t);
             };
-            auto visibility = [&](float vz, float occ) -> float {  // smoothstep(0.98, 1, 1 - (vz - occ))
-                if (!shadow) return 1.0f;
-                const float sv0 = 1.0f - (vz - occ);
-                const float tt = __saturatef((sv0 - 0.98f) * 50.0f);
-                return tt * tt * (3.0f - 2.0f * tt);
+            // acc += flux * G * smoothstep(0.98, 1, 1 - (vz - occ)) for both pixels
+            auto accumulate = [&](int k, f2 G, f2 vz, float o0, float o1) {
+                f2 w = G;
+                if (shadow) {
+                    const f2 sv0 = one - (vz - pk(o0, o1));
+                    float sa, sb;
+                    split(fma2(sv0, pk(50.0f), pk(-49.0f)), sa, sb);
+                    const f2 tt = pk(__saturatef(sa), __saturatef(sb));
+                    w = G * ((tt * tt) * fma2(tt, pk(-2.0f), pk(3.0f)));
+                }
+                const ulonglong2 R7 = S.v[k].r[7], R8 = S.v[k].r[8];
+                accx = fma2(f2{R7.x}, w, accx);
+                accy = fma2(f2{R7.y}, w, accy);
+                accz = fma2(f2{R8.x}, w, accz);
             };
-            // kPairs pairs per iteration so that their ISM texel loads are in flight together;
-            // accumulation stays in ascending list order
             int q = 0;
-            for (; q + kPairs - 1 < nk; q += kPairs) {
-                float3 fG[kPairs];
-                float vz[kPairs], o[kPairs];
-                uint32_t t[kPairs];
-                bool ok[kPairs];
+            for (; q + 1 < nk; q += 2) {
+                int kk[2];
+                f2 G[2], vz[2];
+                uint32_t t[2][2];
+                bool ok[2][2], any[2];
 #pragma unroll
-                for (int j = 0; j < kPairs; ++j) {
-                    vz[j] = 0.f;
-                    t[j] = 0;
-                    ok[j] = prepare(S.list[q + j], fG[j], vz[j], t[j]);
+                for (int j = 0; j < 2; ++j) {
+                    kk[j] = S.list[q + j];
+                    G[j] = pk(0.f);
+                    vz[j] = pk(0.f);
+                    t[j][0] = t[j][1] = 0u;
+                    any[j] = prepare(kk[j], G[j], vz[j], t[j][0], t[j][1], ok[j][0], ok[j][1]);
+                }
+                float o[2][2];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    o[j][0] = (any[j] && shadow && ok[j][0]) ? occluder(t[j][0]) : 0.f;
+                    o[j][1] = (any[j] && shadow && ok[j][1]) ? occluder(t[j][1]) : 0.f;
                 }
 #pragma unroll
-                for (int j = 0; j < kPairs; ++j) o[j] = (ok[j] && shadow) ? occluder(t[j]) : 0.f;
-#pragma unroll
-                for (int j = 0; j < kPairs; ++j) {
-                    if (!ok[j]) continue;
-                    const float v = visibility(vz[j], o[j]);
-                    accx = fmaf(fG[j].x, v, accx);
-                    accy = fmaf(fG[j].y, v, accy);
-                    accz = fmaf(fG[j].z, v, accz);
-                }
+                for (int j = 0; j < 2; ++j)
+                    if (any[j]) accumulate(kk[j], G[j], vz[j], o[j][0], o[j][1]);
             }
-            for (; q < nk; ++q) {
-                float3 fG;
-                float vz = 0.f;
-                uint32_t t = 0;
-                if (prepare(S.list[q], fG, vz, t)) {
-                    const float v = visibility(vz, shadow ? occluder(t) : 0.f);
-                    accx = fmaf(fG.x, v, accx);
-                    accy = fmaf(fG.y, v, accy);
-                    accz = fmaf(fG.z, v, accz);
-                }
+            if (q < nk) {
+                const int k = S.list[q];
+                f2 G = pk(0.f), vz = pk(0.f);
+                uint32_t t0 = 0u, t1 = 0u;
+                bool ok0, ok1;
+                if (prepare(k, G, vz, t0, t1, ok0, ok1))
+                    accumulate(k, G, vz, (shadow && ok0) ? occluder(t0) : 0.f, (shadow && ok1) ? occluder(t1) : 0.f);
             }
         }
         __syncthreads();
     }
-    if (valid) {
-        const size_t pix = (size_t)y * a.width + x;
-        // vec3(acc * giIntensityFactor / vplCount) * interleavedPixels
-        a.out[3 * pix + 0] = accx * a.gi_scale;
-        a.out[3 * pix + 1] = accy * a.gi_scale;
-        a.out[3 * pix + 2] = accz * a.gi_scale;
+    float ax0, ax1, ay0, ay1, az0, az1;
+    split(accx, ax0, ax1);
+    split(accy, ay0, ay1);
+    split(accz, az0, az1);
+    if (v0) {
+        const size_t pix = (size_t)y * a.width + x0;
+        a.out[3 * pix + 0] = ax0 * a.gi_scale;
+        a.out[3 * pix + 1] = ay0 * a.gi_scale;
+        a.out[3 * pix + 2] = az0 * a.gi_scale;
+    }
+    if (v1) {
+        const size_t pix = (size_t)y * a.width + x1;
+        a.out[3 * pix + 0] = ax1 * a.gi_scale;
+        a.out[3 * pix + 1] = ay1 * a.gi_scale;
+        a.out[3 * pix + 2] = az1 * a.gi_scale;
     }
     return true;
 }
 
+// Eight 128-thread blocks (or 32 one-warp blocks) per SM: 64 registers a thread.
 template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16>
-__global__ void __launch_bounds__(T* T, T == 16 ? 4 : 16) fg_kernel(FgArgs a) {
-    __shared__ FgSmem<T * T> S;
+__global__ void __launch_bounds__(T* T / 2, T == 16 ? 8 : 32) fg_kernel(FgArgs a) {
+    __shared__ FgSmem<T> S;
     if (threadIdx.x == 0) mbar_init(&S.bar, 1);
     uint32_t parity = 0;
     fg_tile<T, kReduced, kAtlasF16, kNormalF16>(a, a.tile0 + blockIdx.x, blockIdx.y, S, parity);
@@ -468,14 +573,14 @@ static cudaError_t launch_fg_t(const FgArgs& args, cudaStream_t s, int tr0, int 
     const dim3 grid(ntx * (tr1 - tr0), I * I);
     const int sel = (a.reduced ? 4 : 0) | (a.atlas_f16 ? 2 : 0) | (a.normal_f16 ? 1 : 0);
     switch (sel) {
-        case 0: fg_kernel<T, false, false, false><<<grid, T * T, 0, s>>>(a); break;
-        case 1: fg_kernel<T, false, false, true><<<grid, T * T, 0, s>>>(a); break;
-        case 2: fg_kernel<T, false, true, false><<<grid, T * T, 0, s>>>(a); break;
-        case 3: fg_kernel<T, false, true, true><<<grid, T * T, 0, s>>>(a); break;
-        case 4: fg_kernel<T, true, false, false><<<grid, T * T, 0, s>>>(a); break;
-        case 5: fg_kernel<T, true, false, true><<<grid, T * T, 0, s>>>(a); break;
-        case 6: fg_kernel<T, true, true, false><<<grid, T * T, 0, s>>>(a); break;
-        default: fg_kernel<T, true, true, true><<<grid, T * T, 0, s>>>(a); break;
+        case 0: fg_kernel<T, false, false, false><<<grid, T * T / 2, 0, s>>>(a); break;
+        case 1: fg_kernel<T, false, false, true><<<grid, T * T / 2, 0, s>>>(a); break;
+        case 2: fg_kernel<T, false, true, false><<<grid, T * T / 2, 0, s>>>(a); break;
+        case 3: fg_kernel<T, false, true, true><<<grid, T * T / 2, 0, s>>>(a); break;
+        case 4: fg_kernel<T, true, false, false><<<grid, T * T / 2, 0, s>>>(a); break;
+        case 5: fg_kernel<T, true, false, true><<<grid, T * T / 2, 0, s>>>(a); break;
+        case 6: fg_kernel<T, true, true, false><<<grid, T * T / 2, 0, s>>>(a); break;
+        default: fg_kernel<T, true, true, true><<<grid, T * T / 2, 0, s>>>(a); break;
     }
     return cudaGetLastError();
 }
@@ -492,8 +597,8 @@ cudaError_t launch_final_gather(const FgArgs& a, cudaStream_t s, int tile_row0, 
 // One pass per precision (FP32 views in pass kBpFg, reduced views in kBpFg16), so that each
 // kernel holds one variant of the tile body, as the single-view kernels do.
 template <bool kReduced>
-__global__ void __launch_bounds__(256, 4) batch_fg_kernel(BatchTable t) {
-    __shared__ FgSmem<256> S;
+__global__ void __launch_bounds__(128, 8) batch_fg_kernel(BatchTable t) {
+    __shared__ FgSmem<16> S;
     __shared__ FgArgs args;  // the item's view arguments, staged when the block changes views
     __shared__ int tpc;
     if (threadIdx.x == 0) mbar_init(&S.bar, 1);
@@ -523,9 +628,9 @@ __global__ void __launch_bounds__(256, 4) batch_fg_kernel(BatchTable t) {
 cudaError_t launch_batch_fg(const BatchTable& t, int pass, int grid, cudaStream_t s) {
     if (grid <= 0) return cudaSuccess;
     if (pass == kBpFg16)
-        batch_fg_kernel<true><<<grid, 256, 0, s>>>(t);
+        batch_fg_kernel<true><<<grid, 128, 0, s>>>(t);
     else
-        batch_fg_kernel<false><<<grid, 256, 0, s>>>(t);
+        batch_fg_kernel<false><<<grid, 128, 0, s>>>(t);
     return cudaGetLastError();
 }
 

@@ -1266,7 +1266,7 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
     for (int p = 0; p < mlgi::kBpCount; ++p) {
         const int items = prefix[p * (n_views + 1) + n_views];
         const int per_sm = p == mlgi::kBpFg || p == mlgi::kBpFg16
-                               ? 4
+                               ? 8
                                : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
         b->grid[p] = std::min(items, std::max(1, sms) * per_sm);
     }

@@ -54,3 +54,6 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = lines[0]
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+    passes = d["cpu_baseline"]["passes_ms"]
+    assert set(passes) == {"vpl_process", "ism_clear+ism_splat", "pullpush", "final_gather"}
+    assert all(v >= 0 for v in passes.values()) and sum(passes.values()) <= d["value"] * 1.01
