@@ -95,10 +95,13 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel, key="traffic"):
+def ncu_traffic(kernel, key="traffic", workload="c2_1920x1080_n1024"):
     """Per-launch DRAM bytes (key "traffic") or issue-slot use in percent (key "issue") of `kernel`
-    from the committed ncu summary, if any."""
-    for fn in sorted(os.listdir(os.path.join(ROOT, "profiles"))) if os.path.isdir(os.path.join(ROOT, "profiles")) else []:
+    from the committed ncu summary of `workload` (a file under profiles/ named for it), if any."""
+    pdir = os.path.join(ROOT, "profiles")
+    for fn in sorted(os.listdir(pdir)) if os.path.isdir(pdir) else []:
+        if workload not in fn:
+            continue
         try:
             txt = open(os.path.join(ROOT, "profiles", fn)).read()
         except Exception:
@@ -425,7 +428,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
     dom_name = max(kernel_ms, key=kernel_ms.get)  # the dominant kernel
     peak, peak_kind = measured_peak_gbs()
     achieved = ab[dom_name] / (kernel_ms[dom_name] * 1e-3) / 1e9
-    traffic = ncu_traffic(dom_name)
+    traffic = ncu_traffic(dom_name, workload=cfg.name)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": False,
@@ -448,7 +451,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": ab[dom_name], "traffic": traffic,
-                     "issue_busy_pct": ncu_traffic(dom_name, "issue"),
+                     "issue_busy_pct": ncu_traffic(dom_name, "issue", cfg.name),
                      "note": "FP32-issue-bound kernels (bit-exact IEEE division, no FMA contraction): "
                              "issue_busy_pct is the dominant kernel's issue-slot use from the committed "
                              "ncu summary"},

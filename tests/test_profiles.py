@@ -25,3 +25,8 @@ def test_summary_has_traffic_and_issue(kernel):
 def test_unknown_kernel_reads_none():
     assert bench.ncu_traffic("no_such_kernel") is None
     assert bench.ncu_traffic("no_such_kernel", "issue") is None
+
+
+def test_other_workload_reads_none():
+    """Figures of the 1080p capture are not reported for another workload."""
+    assert bench.ncu_traffic("final_gather", workload="c1_640x360_n256") is None
