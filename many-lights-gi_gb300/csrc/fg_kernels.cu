@@ -88,73 +88,6 @@ __device__ __forceinline__ void decode_vpl(const unsigned char* rec, v3& p, v3& 
     }
 }
 
-// ---- compensated ("double-float") arithmetic for the world-position reconstruction ----------
-// inv_vp * ndc followed by the w divide cancels badly near the far plane (w is a small difference
-// of two ~0.5 terms), which makes a plain FP32 evaluation drift ~1e-4 world units from the exact
-// value -- enough to flip the clamped 1/d^4 term of near-coplanar VPLs. Each quantity is kept as an
-// unevaluated sum hi + lo using the error-free transformations TwoSum (Knuth) and TwoProduct via
-// FMA (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 2005); the
-// result is rounded once to FP32. Intrinsics keep the compiler from contracting or reordering.
-struct df {
-    float hi, lo;
-};
-__device__ __forceinline__ df two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-    return {s, e};
-}
-__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ df df_add(df a, df b) {
-    const df s = two_sum(a.hi, b.hi);
-    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
-}
-__device__ __forceinline__ df df_mul_f(df a, float b) {
-    const float p = __fmul_rn(a.hi, b);
-    const float e = __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p));
-    return fast_two_sum(p, e);
-}
-// a / b rounded to FP32 from double-float operands, given rb ~ 1/b.hi (within a few ulps): the
-// quotient a.hi * rb, then one correction by the remainder a - q b (the FMA part a.hi - q b.hi is
-// exact); the error left is the square of rb's relative error plus the final rounding.
-__device__ __forceinline__ float df_div(df a, df b, float rb) {
-    const float q = __fmul_rn(a.hi, rb);
-    const float r = __fadd_rn(__fmaf_rn(-q, b.hi, a.hi), __fmaf_rn(-q, b.lo, a.lo));
-    return __fmaf_rn(r, rb, q);
-}
-// 2*k/n - 1 as double-float (k, n small integers, rn = RN(1/n)): the pixel-corner NDC coordinate.
-// q = k rn is within an ulp of k/n; the remainder k - q n is exact, and its quotient is the low part.
-__device__ __forceinline__ df ndc_coord(int k, int n, float rn) {
-    const float fk = float(k), fn = float(n);
-    const float q = __fmul_rn(fk, rn);
-    const float ql = __fmul_rn(__fmaf_rn(-q, fn, fk), rn);
-    const df t = two_sum(__fmul_rn(q, 2.0f), -1.0f);
-    return fast_two_sum(t.hi, __fadd_rn(t.lo, __fmul_rn(ql, 2.0f)));
-}
-// world = (inv_vp * (ndc, 1)).xyz / w, each row summed in double-float.
-__device__ __forceinline__ v3 reconstruct_world(const float* m, int x, int y, int w, int h, float rw, float rh,
-                                                float d) {
-    const df nx = ndc_coord(x, w, rw), ny = ndc_coord(y, h, rh);
-    const df nz = two_sum(__fmul_rn(d, 2.0f), -1.0f);
-    df r[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        df acc = df_mul_f(nx, m[k]);
-        acc = df_add(acc, df_mul_f(ny, m[4 + k]));
-        acc = df_add(acc, df_mul_f(nz, m[8 + k]));
-        acc = df_add(acc, df{m[12 + k], 0.0f});
-        r[k] = acc;
-    }
-    // one reciprocal of w for the three divides (the hardware approximation); each quotient is
-    // corrected by its remainder, as in double-float division (Dekker 1971)
-    float rb;
-    asm("rcp.approx.f32 %0, %1;" : "=f"(rb) : "f"(r[3].hi));
-    return mk(df_div(r[0], r[3], rb), df_div(r[1], r[3], rb), df_div(r[2], r[3], rb));
-}
-
 // normalize(v) with the hardware reciprocal square root (about 2 ulps; the gathering's bar is a
 // relative L2 of 1e-3).
 __device__ __forceinline__ v3 normalize_fast(v3 v) { return v * rsqrtf(dot(v, v)); }
@@ -213,6 +146,84 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
+// ---- compensated ("double-float") world-position reconstruction, for both pixels at once ------
+// inv_vp * ndc followed by the w divide cancels badly near the far plane (w is a small difference
+// of two ~0.5 terms), which makes a plain FP32 evaluation drift ~1e-4 world units from the exact
+// value -- enough to flip the clamped 1/d^4 term of near-coplanar VPLs. Each quantity is kept as an
+// unevaluated sum hi + lo using the error-free transformations TwoSum (Knuth) and TwoProduct via
+// FMA (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 2005); the
+// result is rounded once to FP32. A product that TwoProduct needs rounded on its own is formed as
+// fma(a, b, z), z a zero the compiler cannot see, so that it is never fused into the add that
+// follows (packed multiplies feeding packed adds may be fused); the other products it could fuse
+// are exact (doublings) or add an exact zero.
+struct df2 {
+    f2 hi, lo;
+};
+__device__ __forceinline__ df2 two_sum2(f2 a, f2 b) {
+    const f2 s = a + b;
+    const f2 bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df2 fast_two_sum2(f2 a, f2 b) {  // |a| >= |b|
+    const f2 s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ df2 df_add2(df2 a, df2 b) {
+    const df2 s = two_sum2(a.hi, b.hi);
+    return fast_two_sum2(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ df2 df_add2(df2 a, f2 b) {  // b exact (low part zero)
+    const df2 s = two_sum2(a.hi, b);
+    return fast_two_sum2(s.hi, s.lo + a.lo);
+}
+__device__ __forceinline__ df2 df_mul_f2(df2 a, f2 b, f2 z) {
+    const f2 p = fma2(a.hi, b, z);
+    const f2 e = fma2(a.lo, b, fma2(a.hi, b, z - p));
+    return fast_two_sum2(p, e);
+}
+// a / b rounded to FP32 from double-float operands, given rb ~ 1/b.hi (within a few ulps): the
+// quotient a.hi * rb, then one correction by the remainder a - q b (the FMA part a.hi - q b.hi is
+// exact), as in double-float division (Dekker 1971)
+__device__ __forceinline__ f2 df_div2(df2 a, df2 b, f2 rb, f2 z) {
+    const f2 q = fma2(a.hi, rb, z);
+    const f2 nq = z - q;
+    const f2 r = fma2(nq, b.hi, a.hi) + fma2(nq, b.lo, a.lo);
+    return fma2(r, rb, q);
+}
+// 2*k/n - 1 as double-float (k, n small integers, rn = RN(1/n)): the pixel-corner NDC coordinate.
+// q = k rn is within an ulp of k/n; the remainder k - q n is exact, and its quotient is the low part.
+__device__ __forceinline__ df2 ndc_coord2(f2 k, f2 n, f2 rn, f2 z) {
+    const f2 q = fma2(k, rn, z);
+    const f2 ql = fma2(z - q, n, k) * rn;
+    const df2 t = two_sum2(q * pk(2.0f), pk(-1.0f));
+    return fast_two_sum2(t.hi, t.lo + ql * pk(2.0f));
+}
+// world = (inv_vp * (ndc, 1)).xyz / w for pixels (x0, y) and (x1, y) with window depths d0 and d1,
+// each row summed in double-float; one hardware reciprocal of w serves the three divides
+__device__ __forceinline__ void reconstruct_world2(const float* m, int x0, int x1, int y, int w, int h, float rw,
+                                                   float rh, float d0, float d1, f2 z, v3& p0, v3& p1) {
+    const df2 nx = ndc_coord2(pk(float(x0), float(x1)), pk(float(w)), pk(rw), z);
+    const df2 ny = ndc_coord2(pk(float(y)), pk(float(h)), pk(rh), z);
+    const df2 nz = two_sum2(pk(d0, d1) * pk(2.0f), pk(-1.0f));
+    df2 r[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        df2 acc = df_mul_f2(nx, pk(m[k]), z);
+        acc = df_add2(acc, df_mul_f2(ny, pk(m[4 + k]), z));
+        acc = df_add2(acc, df_mul_f2(nz, pk(m[8 + k]), z));
+        r[k] = df_add2(acc, pk(m[12 + k]));
+    }
+    float w0, w1;
+    split(r[3].hi, w0, w1);
+    const f2 rb = pk(rcp_approx(w0), rcp_approx(w1));
+    float ax, bx, ay, by, az, bz;
+    split(df_div2(r[0], r[3], rb, z), ax, bx);
+    split(df_div2(r[1], r[3], rb, z), ay, by);
+    split(df_div2(r[2], r[3], rb, z), az, bz);
+    p0 = mk(ax, ay, az);
+    p1 = mk(bx, by, bz);
+}
+
 // One VPL with every value twice, as (v, v) 64-bit pairs: position, normal, the lookAtRH rows
 // scaled by half the ISM size, the ISM tile origin, flux and the border flag.
 struct VplPk {
@@ -263,14 +274,13 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
 
     // ---- pixel setup: world position from depth (final_gathering.comp:70-76, evaluated with
     // compensated arithmetic) and the octahedral normal ----
-    auto setup = [&](int x, bool valid, v3& fw, v3& fn, const uint32_t*& cl_row) {
-        fw = mk(0.f, 0.f, 0.f);
+    auto setup = [&](int x, bool valid, float& d, v3& fn, const uint32_t*& cl_row) {
+        d = 0.5f;
         fn = mk(0.f, 0.f, 1.f);
         cl_row = nullptr;
         if (!valid) return;
         const size_t pix = (size_t)y * a.width + x;
-        const float d = __ldg(a.depth + pix);
-        fw = reconstruct_world(a.inv_vp, x, y, a.width, a.height, a.inv_w, a.inv_h, d);
+        d = __ldg(a.depth + pix);
         float ex, ey;
         if (kNormalF16) {
             const __half2 h = reinterpret_cast<const __half2*>(a.normal)[pix];
@@ -288,9 +298,14 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         }
     };
     v3 w0, n0, w1, n1;
+    float d0, d1;
     const uint32_t *cl0, *cl1;
-    setup(x0, v0, w0, n0, cl0);
-    setup(x1, v1, w1, n1, cl1);
+    setup(x0, v0, d0, n0, cl0);
+    setup(x1, v1, d1, n1, cl1);
+    // both pixels' world positions at once (a pixel outside the image gets a finite dummy)
+    reconstruct_world2(a.inv_vp, x0, x1, y, a.width, a.height, a.inv_w, a.inv_h, d0, d1, pk(a.z_far * 0.0f), w0, w1);
+    if (!v0) w0 = mk(0.f, 0.f, 0.f);
+    if (!v1) w1 = mk(0.f, 0.f, 0.f);
 
     // ---- per-tile bounds for culling ----
     v3 bmin = mk(0.f, 0.f, 0.f), bmax = mk(0.f, 0.f, 0.f);
