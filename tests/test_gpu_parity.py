@@ -244,7 +244,11 @@ def _oracle_fg(cfg, sc, df, dtype, tile=0, cutoff=0.0, reduced_inputs=False):
 
 @pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C1.replace(interleave=8, tile=8, name="c1_i8_t8"),
                                               mlgi.C1.replace(interleave=1, name="c1_i1"),
-                                              mlgi.C1.replace(width=637, height=357, cull=1, name="c1_ragged_cull")],
+                                              mlgi.C1.replace(width=637, height=357, cull=1, name="c1_ragged_cull"),
+                                              # one-warp 8x8 tiles with culling; 64 VPLs a class in
+                                              # two staging chunks
+                                              mlgi.C1.replace(interleave=8, tile=8, cull=1, name="c1_i8_t8_cull"),
+                                              mlgi.C1.replace(interleave=2, tile=8, cull=1, name="c1_i2_t8_cull")],
                          ids=lambda c: c.name)
 def test_final_gather_matches_fp64_oracle(ctx, cfg):
     import torch
