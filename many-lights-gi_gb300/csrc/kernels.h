@@ -76,7 +76,7 @@ struct FgArgs {
     float gi_scale;           // giIntensity / vplCount * I^2 (final_gathering.comp:133), folded on the host
     float inv_w, inv_h;       // 1 / width, 1 / height
     float clamp_value;
-    int tile;                 // tile edge (threads = tile*tile)
+    int tile;                 // tile edge (threads = tile*tile/2, two pixels each)
     int cull;                 // per-tile culling on/off
     float influence_cutoff;   // 0: off
     float* out;               // width*height*3
