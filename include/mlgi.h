@@ -88,7 +88,7 @@ typedef struct {
     int capacity;
     float* vpl;     /* capacity x 12 floats: pos, pad, normal, pad, flux, pad (48-byte stride) */
     float* packed;  /* capacity x 4 floats: pos, uintBitsToFloat(pack3SN(normal)) */
-    void* reduced;  /* capacity x 24 bytes, or NULL */
+    void* reduced;  /* capacity x 24 bytes, 16-byte aligned, or NULL */
 } mlgi_vpl_buf;
 
 /* VPLProcessor::process: regular RSM sampling into the VPL buffers. */

@@ -349,6 +349,8 @@ mlgi_status build_vpl_args(mlgi_ctx* ctx, const mlgi_rsm_view* rsm, const mlgi_v
         return fail(ctx, MLGI_EINVAL, "bad RSM view");
     if (!out->vpl || !out->packed || !aligned16(out->vpl) || !aligned16(out->packed))
         return fail(ctx, MLGI_EINVAL, "VPL buffers must be non-NULL and 16-byte aligned");
+    if (out->reduced && !aligned16(out->reduced))
+        return fail(ctx, MLGI_EINVAL, "reduced VPL records must be 16-byte aligned");
     a = mlgi::VplArgs{};
     a.n = p->count;
     a.ax = (uint32_t)std::ceil(std::sqrt((float)p->count));  // rsmSamples1d = uint(ceil(sqrt(N)))
@@ -459,6 +461,8 @@ mlgi_status build_fg_args(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_
     if (p->vpl_end <= p->vpl_start) return fail(ctx, MLGI_EINVAL, "empty VPL range");
     if (p->vpl_format != MLGI_F32 && p->vpl_format != MLGI_F16) return fail(ctx, MLGI_EINVAL, "bad VPL format");
     if (p->vpl_format == MLGI_F16 && !vpls->reduced) return fail(ctx, MLGI_EINVAL, "reduced VPL records missing");
+    if (p->vpl_format == MLGI_F16 && !aligned16(vpls->reduced))  // staged by a bulk copy
+        return fail(ctx, MLGI_EINVAL, "reduced VPL records must be 16-byte aligned");
     if (p->vpl_format == MLGI_F32 && (!vpls->vpl || !aligned16(vpls->vpl)))
         return fail(ctx, MLGI_EINVAL, "VPL records must be 16-byte aligned");
     if (p->shadowing && (!atlas->depth || atlas->width <= 0 || atlas->height <= 0 || atlas->width > 65535 ||

@@ -478,6 +478,12 @@ def test_limits_and_inconsistent_layouts_are_rejected(ctx):
         fp = df.fg()
         setattr(fp, field, value)
         _rejected(lambda: ctx.final_gather(df.gbuffer_view(), vb, at, fp, df.radiance()))
+    # reduced VPL records off a 16-byte boundary: written by the VPL pass, bulk-copied by the gathering
+    odd = mlgi.VplBuf(vb.capacity, vb.vpl, vb.packed, vb.reduced + 8)
+    _rejected(lambda: ctx.vpl_process(df.rsm_view(), mlgi.vpl_params(cfg, df.scene), odd))
+    fp = df.fg()
+    fp.vpl_format = mlgi.F16
+    _rejected(lambda: ctx.final_gather(df.gbuffer_view(), odd, at, fp, df.radiance()))
     # a NULL host input of the host-buffer frame
     pinned = pinned_inputs(scene(cfg))
     hfd = host_frame_desc(scene(cfg), pinned)
