@@ -468,7 +468,12 @@ mlgi_status mlgi_frame_host_sizes_get(const mlgi_frame_desc* frame, mlgi_frame_h
  * `rgb_host` before returning. Copies overlap the passes: point bucket ranges are splatted as they
  * arrive, the ISM rows a range completes are pulled and pushed before the next range, and the
  * gathering runs in bands of rows whose radiance is copied back while the next band runs. The
- * result equals mlgi_gi_frame's bit for bit. Pinned host memory gives the full copy bandwidth. */
+ * result equals mlgi_gi_frame's bit for bit. Pinned host memory gives the full copy bandwidth.
+ * A call whose `frame` (every pointer and parameter) and `rgb_host` equal the previous call's, with
+ * every host buffer pinned, captures the frame into a CUDA graph, and the calls after it replay
+ * the graph (one launch instead of about a hundred API calls); each replay copies what the host
+ * buffers hold at that time. A bucket count above bucket_stride (the bucket reads the next
+ * buckets' entries, as the reference's splat does) makes the frame upload every point first. */
 mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* frame, float* rgb_host);
 
 /* Per-pass device times (ms) of the last mlgi_gi_frame / mlgi_gi_frame_host call when timing is

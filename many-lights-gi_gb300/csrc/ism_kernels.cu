@@ -153,7 +153,14 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
     __syncthreads();
 
     const uint32_t first = (uint32_t)chunk * kSplatChunk;
-    const uint32_t count = __ldg(a.counts + wg);  // the last chunk takes any points beyond the stride
+    // A counter may run past its bucket (ism.geom:65-67 does not bound it): the shader then reads
+    // the next buckets' entries, and past the end of the buffer its imageLoad returns zero. All
+    // such points are the same zero point, and splatting it again changes no key (atomicMin), so
+    // the count stops one past the buffer's entries; that also bounds the block's work.
+    const int64_t in_buffer = max((int64_t)0, a.n_entries - (int64_t)wg * a.bucket_stride);
+    const uint32_t avail = (uint32_t)min(in_buffer, (int64_t)0xFFFFFFFE);
+    uint32_t count = __ldg(a.counts + wg);  // the last chunk takes any points beyond the stride
+    if (count > avail) count = avail + 1;
     const uint32_t cnt = chunk == a.chunks - 1 ? count : min(count, first + kSplatChunk);
     const float4* bucket = a.points + (int64_t)wg * a.bucket_stride;
     const float fw = float(a.atlas_w), fh = float(a.atlas_h), fgx = float(a.gx), fgy = float(a.gy);
@@ -173,7 +180,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         int found = 0;
         uint32_t used = 0;
         if (j < cnt) {
-            pt = __ldg(bucket + j);
+            if (j < avail) pt = __ldg(bucket + j);  // else the zero point
             const v3 position = mk(pt.x, pt.y, pt.z);
             const uint32_t nr = __float_as_uint(pt.w);
             const v3 pn = mk(S.unorm[nr & 0xFFu], S.unorm[(nr >> 8) & 0xFFu], S.unorm[(nr >> 16) & 0xFFu]);

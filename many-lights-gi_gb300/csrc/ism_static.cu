@@ -105,6 +105,7 @@ extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi
     a.points = reinterpret_cast<const float4*>(pts->points);
     a.counts = pts->counts;
     a.bucket_stride = pts->bucket_stride;
+    a.n_entries = (int64_t)pts->n_buckets * pts->bucket_stride;
     a.n_groups = pts->n_buckets;
     a.chunks = (int)std::max<int64_t>(1, (pts->bucket_stride + mlgi::kSplatChunk - 1) / mlgi::kSplatChunk);
     a.packed = reinterpret_cast<const float4*>(vpls->packed);

@@ -27,6 +27,7 @@ struct SplatArgs {
     const float4* points;
     const uint32_t* counts;
     int64_t bucket_stride;
+    int64_t n_entries;     // entries in the point buffer (n_buckets * bucket_stride)
     int n_groups;          // buckets of this launch: bucket0 .. bucket0 + n_groups - 1
     int chunks;            // work items per bucket: ceil(bucket_stride / kSplatChunk), at least 1
     int bucket0;           // first bucket of this launch (0 for a whole splat)

@@ -124,7 +124,19 @@ struct mlgi_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_band[kHostBands] = {};
     cudaEvent_t ev_split[kHostPointChunks] = {}, ev_side = nullptr;  // early pull-push runs on `side`
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // the copy and side streams fork from and join `stream`
     HostSchedule sched;
+    // The host frame as a CUDA graph: a call whose arguments (the whole frame description, the output
+    // pointer, whether a bucket counter runs past its stride) repeat the previous call's captures
+    // the frame, and later such calls replay it, which spares the hundred-odd API calls a frame issues.
+    // A call with new arguments runs directly (its buffers may need allocating, which a capture
+    // cannot do).
+    struct {
+        std::vector<unsigned char> key;
+        int calls = 0;           // calls with this key
+        bool failed = false;     // the capture did not succeed: this key runs directly
+        cudaGraphExec_t exec = nullptr;
+    } hgraph;
     float last_ms[kNumTimings] = {};
 };
 
@@ -267,6 +279,8 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
     for (int i = 0; e == cudaSuccess && i < kHostPointChunks; ++i)
         e = cudaEventCreateWithFlags(&ctx->ev_split[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_side, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_begin, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_end, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         mlgi_destroy(ctx);
@@ -297,8 +311,9 @@ void mlgi_destroy(mlgi_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->ev_split)
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_side})
+    for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_side, ctx->ev_begin, ctx->ev_end})
         if (e) cudaEventDestroy(e);
+    if (ctx->hgraph.exec) cudaGraphExecDestroy(ctx->hgraph.exec);
     for (cudaStream_t cs : {ctx->copy, ctx->side})
         if (cs) {
             cudaStreamSynchronize(cs);
@@ -394,6 +409,7 @@ mlgi_status build_splat_args(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_v
     a.points = reinterpret_cast<const float4*>(pts->points);
     a.counts = pts->counts;
     a.bucket_stride = pts->bucket_stride;
+    a.n_entries = (int64_t)pts->n_buckets * pts->bucket_stride;
     a.n_groups = pts->n_buckets;
     a.chunks = (int)std::max<int64_t>(1, (pts->bucket_stride + mlgi::kSplatChunk - 1) / mlgi::kSplatChunk);
     a.packed = reinterpret_cast<const float4*>(vpls->packed);
@@ -895,8 +911,22 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     if ((st = build_splat_args(ctx, &d.points, &vb, n, &d.ism, &atlas, sa)) != MLGI_OK) return st;
     if ((st = build_pullpush_args(ctx, &atlas, &d.ism, ctx->pp.p, pa)) != MLGI_OK) return st;
     if ((st = build_fg_args(ctx, &d.gbuffer, &vb, &atlas, &d.fg, &out, fa)) != MLGI_OK) return st;
-    HostSchedule& h = ctx->sched;
-    host_schedule(h, d);
+    host_schedule(ctx->sched, d);
+    // A bucket whose count runs past its stride reads the next buckets' entries (as the reference's
+    // splat does), which a pipelined upload may not have copied yet: such a frame uploads all its
+    // points before the first splat.
+    HostSchedule one;
+    bool overflow = false;
+    for (int b = 0; b < f->points.n_buckets && !overflow; ++b)
+        overflow = (int64_t)f->points.counts[b] > f->points.bucket_stride;
+    if (overflow) {
+        one.chunks = 1;
+        one.rot = 0;
+        one.pos[0] = 0;
+        one.pos[1] = f->points.n_buckets;
+        one.row_chunk.assign(d.ism.grid_y, 0);
+    }
+    const HostSchedule& h = overflow ? one : ctx->sched;
     const int nb = d.points.n_buckets;
     const size_t bucket_bytes = (size_t)d.points.bucket_stride * 16;
     // upload position range [q0, q1) as at most two runs of consecutive buckets
@@ -917,6 +947,9 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     // each input just before its first reader, so each point range is splatted, and the ISM rows
     // it completes are pulled and pushed, while the next range and the G-buffer are arriving.
     cudaStream_t s = ctx->stream, c = ctx->copy, s2 = ctx->side;
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_begin, s));  // fork (the frame can be captured from `s`)
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(c, ctx->ev_begin, 0));
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_begin, 0));
     mark(ctx, kEvH2DStart, c);
     for (int i = 0; i < 3; ++i)
         if (sizes[i]) MLGI_CUDA(ctx, cudaMemcpyAsync(bufs[i]->p, srcs[i], sizes[i], cudaMemcpyHostToDevice, c));
@@ -1028,6 +1061,43 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     // the device error word rides behind the last band's copy (the copy stream has waited for
     // every band, so every kernel of the frame is done)
     MLGI_CUDA(ctx, cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c));
+    MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_end, c));  // join
+    MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_end, 0));
+    return MLGI_OK;
+}
+
+// Every host buffer of the call is page-locked (a graph copies only from and to pinned memory).
+bool host_buffers_pinned(const mlgi_frame_desc* f, const float* rgb_host) {
+    const void* ps[] = {f->rsm.depth, f->rsm.normal, f->rsm.diffuse, f->points.points, f->points.counts,
+                        f->gbuffer.depth, f->gbuffer.normal, rgb_host};
+    for (const void* p : ps) {
+        if (!p) continue;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
+// Captures the host frame from the context's stream into ctx->hgraph.exec; on any failure the
+// capture is ended and discarded and the call reports why.
+mlgi_status capture_host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host) {
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "host frame capture");
+    const mlgi_status st = host_frame(ctx, f, rgb_host);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (st == MLGI_OK && e == cudaSuccess && graph)
+        e = cudaGraphInstantiate(&ctx->hgraph.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (st != MLGI_OK) return st;
+    if (e != cudaSuccess || !ctx->hgraph.exec) {
+        ctx->hgraph.exec = nullptr;
+        return cuda_fail(ctx, e != cudaSuccess ? e : cudaErrorUnknown, "host frame capture");
+    }
     return MLGI_OK;
 }
 
@@ -1038,7 +1108,39 @@ extern "C" {
 mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host) {
     if (!ctx) return MLGI_EINVAL;
     if (!f || !rgb_host) return fail(ctx, MLGI_EINVAL, "NULL argument");
-    const mlgi_status st = host_frame(ctx, f, rgb_host);
+    auto& g = ctx->hgraph;
+    std::vector<unsigned char> key(sizeof(*f) + sizeof(rgb_host) + 1);
+    std::memcpy(key.data(), f, sizeof(*f));
+    std::memcpy(key.data() + sizeof(*f), &rgb_host, sizeof(rgb_host));
+    bool overflow = false;  // selects the upload schedule (see host_frame)
+    for (int b = 0; f->points.counts && b < f->points.n_buckets && !overflow; ++b)
+        overflow = (int64_t)f->points.counts[b] > f->points.bucket_stride;
+    key.back() = overflow ? 1 : 0;
+    if (ctx->timing || key != g.key) {  // new arguments (or per-pass timing): run directly
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.key = ctx->timing ? std::vector<unsigned char>() : key;
+        g.calls = 0;
+        g.failed = false;
+    }
+    mlgi_status st;
+    if (g.exec) {
+        const cudaError_t e = cudaGraphLaunch(g.exec, ctx->stream);
+        st = e == cudaSuccess ? MLGI_OK : cuda_fail(ctx, e, "host frame graph launch");
+    } else if (!ctx->timing && g.calls > 0 && !g.failed && host_buffers_pinned(f, rgb_host)) {
+        st = capture_host_frame(ctx, f, rgb_host);
+        if (st == MLGI_OK) {
+            const cudaError_t e = cudaGraphLaunch(g.exec, ctx->stream);
+            st = e == cudaSuccess ? MLGI_OK : cuda_fail(ctx, e, "host frame graph launch");
+        } else {  // argument errors report as before; anything else runs this key directly
+            cudaGetLastError();
+            g.failed = true;
+            if (st == MLGI_ECUDA) st = host_frame(ctx, f, rgb_host);
+        }
+    } else {
+        st = host_frame(ctx, f, rgb_host);
+    }
+    ++g.calls;
     // nothing may still read the caller's buffers when the call returns, also after an error
     const cudaError_t e1 = cudaStreamSynchronize(ctx->copy);
     const cudaError_t e2 = cudaStreamSynchronize(ctx->side);

@@ -170,6 +170,7 @@ struct SplatParams {
     int gx, gy, atlas_w, atlas_h;
     int64_t bucket_stride;  // imageSize(pointBuffer).x / sampledVplCount
     int n_groups;           // dispatched work groups (sampledVplCount)
+    int64_t n_entries;      // imageSize(pointBuffer).x
 };
 
 // issued (optional): the number of imageAtomicMin calls that land inside the atlas.
@@ -195,9 +196,16 @@ void ism_splat(const float* points, const uint32_t* counts, const T* vpl_pos, co
             vp[l] = V3<T>(vpl_pos[3 * index], vpl_pos[3 * index + 1], vpl_pos[3 * index + 2]);
             vn[l] = vpl_pn[index];
         }
-        const uint cnt = counts[wg];
+        // A counter may run past its bucket (ism.geom:65-67 does not bound it): the loop then reads
+        // the next buckets' entries, and past the end of the buffer an imageLoad returns zero. All
+        // such points are the same zero point, and splatting it again changes no key (atomicMin),
+        // so the loop stops after one of them.
+        const int64_t first = (int64_t)wg * p.bucket_stride;
+        const int64_t avail = std::max<int64_t>(0, p.n_entries - first);
+        const uint cnt = (int64_t)counts[wg] > avail ? (uint)(avail + 1) : counts[wg];
+        static const float zero[4] = {0.f, 0.f, 0.f, 0.f};
         for (uint j = 0; j < cnt; ++j) {
-            const float* pt = points + 4 * ((int64_t)wg * p.bucket_stride + j);
+            const float* pt = (int64_t)j < avail ? points + 4 * (first + j) : zero;
             V3<T> position{T(pt[0]), T(pt[1]), T(pt[2])};
             V4<T> nr = unpackUnorm4x8<T>(floatBitsToUint(pt[3]));
             V3<T> pointNormal = V3<T>(nr.x, nr.y, nr.z) * T(2) - T(1);
@@ -796,36 +804,36 @@ void oracle_vpl_process_f64(int rsm_w, int rsm_h, const float* depth, const uint
 }
 
 static SplatParams make_splat(int n_vpl, int vpl_start, int vpl_end, int scale_isms, int points_only, int gx, int gy,
-                              int aw, int ah, int64_t bucket_stride, int n_groups) {
+                              int aw, int ah, int64_t bucket_stride, int64_t n_entries, int n_groups) {
     SplatParams p;
     p.n_vpl = n_vpl; p.vpl_start = vpl_start; p.vpl_end = vpl_end;
     p.scale_isms = scale_isms; p.points_only_scaled = points_only;
     p.gx = gx; p.gy = gy; p.atlas_w = aw; p.atlas_h = ah;
-    p.bucket_stride = bucket_stride; p.n_groups = n_groups;
+    p.bucket_stride = bucket_stride; p.n_groups = n_groups; p.n_entries = n_entries;
     return p;
 }
 
-void oracle_ism_splat_f32(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride,
+void oracle_ism_splat_f32(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride, int64_t n_entries,
                           const float* vpl_pos, const uint32_t* vpl_pn, int n_vpl, int vpl_start, int vpl_end,
                           int scale_isms, int points_only, int gx, int gy, int aw, int ah, float zfar, uint32_t* atlas,
                           int threads) {
-    SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_groups);
+    SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_entries, n_groups);
     ism_splat<float>(points, counts, vpl_pos, vpl_pn, p, zfar, atlas, threads);
 }
-int64_t oracle_ism_splat_count_f32(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride,
+int64_t oracle_ism_splat_count_f32(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride, int64_t n_entries,
                                    const float* vpl_pos, const uint32_t* vpl_pn, int n_vpl, int vpl_start, int vpl_end,
                                    int scale_isms, int points_only, int gx, int gy, int aw, int ah, float zfar,
                                    uint32_t* atlas, int threads) {
-    SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_groups);
+    SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_entries, n_groups);
     int64_t issued = 0;
     ism_splat<float>(points, counts, vpl_pos, vpl_pn, p, zfar, atlas, threads, &issued);
     return issued;
 }
-void oracle_ism_splat_f64(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride,
+void oracle_ism_splat_f64(const float* points, const uint32_t* counts, int n_groups, int64_t bucket_stride, int64_t n_entries,
                           const double* vpl_pos, const uint32_t* vpl_pn, int n_vpl, int vpl_start, int vpl_end,
                           int scale_isms, int points_only, int gx, int gy, int aw, int ah, double zfar,
                           uint32_t* atlas, int threads) {
-    SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_groups);
+    SplatParams p = make_splat(n_vpl, vpl_start, vpl_end, scale_isms, points_only, gx, gy, aw, ah, bucket_stride, n_entries, n_groups);
     ism_splat<double>(points, counts, vpl_pos, vpl_pn, p, zfar, atlas, threads);
 }
 

@@ -80,8 +80,11 @@ def ism_splat(points, counts, bucket_stride, vpl_pos, vpl_pn, n_vpl, ism_size, g
         fn = lib().oracle_ism_splat_count_f32
     else:
         fn = lib().oracle_ism_splat_f32 if dtype == np.float32 else lib().oracle_ism_splat_f64
-    issued = fn(_p(np.ascontiguousarray(points, np.float32)), _p(np.ascontiguousarray(counts, np.uint32)), n_groups,
-                C.c_int64(bucket_stride), _p(np.ascontiguousarray(vpl_pos, dtype)),
+    points = np.ascontiguousarray(points, np.float32)
+    # imageSize(pointBuffer): entries past it read as zero (a bucket's counter may run past its stride)
+    n_entries = points.size // 4
+    issued = fn(_p(points), _p(np.ascontiguousarray(counts, np.uint32)), n_groups,
+                C.c_int64(bucket_stride), C.c_int64(n_entries), _p(np.ascontiguousarray(vpl_pos, dtype)),
                 _p(np.ascontiguousarray(vpl_pn, np.uint32)), n_vpl, vpl_start, vpl_end, scale_isms, points_only,
                 grid_x, grid_y, aw, ah, _f(dtype)(z_far), _p(atlas), threads)
     return (atlas, int(issued)) if count else atlas

@@ -98,6 +98,59 @@ def test_ism_splat_atomics_count(ctx, cfg):
     assert n == want and 0 < n <= 4 * int(sc.counts.sum())
 
 
+def _overflowing_counts(sc):
+    """Bucket counters past their stride, which the reference's point producer does not bound:
+    one bucket reads 37 entries of the next, the last reads past the end of the buffer (zero
+    points there), and one counter is 2^32 - 1."""
+    c = sc.counts.astype(np.uint32).copy()
+    c[3] = sc.bucket_stride + 37
+    c[5] = 0xFFFFFFFF
+    c[-1] = 3 * sc.bucket_stride
+    return c
+
+
+def test_ism_splat_counts_past_the_stride(ctx):
+    import torch
+
+    cfg = mlgi.C0
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    run_vpl(ctx, df)
+    c = _overflowing_counts(sc)
+    df.counts.copy_(torch.from_numpy(c.view(np.int32)))
+    ctx.ism_splat(df.points_view(), df.vpl_buf(), cfg.n_vpl, mlgi.ism_params(cfg), df.atlas_view())
+    torch.cuda.synchronize()
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    assert sc.points.shape[0] == cfg.n_vpl * sc.bucket_stride  # the oracle's imageSize
+    okeys = O.ism_splat(sc.points, c, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x, cfg.grid_y,
+                        cfg.z_far)
+    plain = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    assert (okeys != plain).any()  # the overflowing counters do change the atlas
+    assert (df.keys_np() == okeys).all()
+
+
+def test_host_frame_counts_past_the_stride(ctx):
+    """Counters past the stride make a bucket read the next buckets' entries: the host-buffer frame
+    then uploads every point before splatting, and still equals the device frame bit for bit."""
+    import torch
+
+    cfg = mlgi.C2
+    sc = scene(cfg)
+    df = DeviceFrame(sc)
+    c = _overflowing_counts(sc)
+    df.counts.copy_(torch.from_numpy(c.view(np.int32)))
+    ctx.gi_frame(df.frame_desc(), df.radiance())
+    torch.cuda.synchronize()
+    dev = df.rgb_np().copy()
+    pinned = pinned_inputs(sc)
+    pinned["counts"].copy_(torch.from_numpy(c.view(np.int32)))
+    ctx.gi_frame_host(host_frame_desc(sc, pinned), pinned["rgb"].numpy())
+    host = pinned["rgb"].numpy().reshape(dev.shape)
+    assert np.abs(dev).max() > 0
+    assert (dev.view(np.uint32) == host.view(np.uint32)).all()
+
+
 def test_ism_splat_vpl_subrange_and_scaled_isms(ctx):
     """VPLStartIndex/EndIndex with ScaleISMs and PointsOnlyToScaledISMs (ism.comp:31-40,56-66)."""
     import torch
@@ -374,12 +427,36 @@ def test_host_frame_equals_device_frame(ctx, cfg):
     torch.cuda.synchronize()
     dev = df.rgb_np().copy()
     pinned = pinned_inputs(sc)
-    for _ in range(2):  # the second call reuses the cached upload schedule
+    for _ in range(3):  # runs directly, then captures the frame into a graph, then replays it
         pinned["rgb"].zero_()
         ctx.gi_frame_host(host_frame_desc(sc, pinned), pinned["rgb"].numpy())
         host = pinned["rgb"].numpy().reshape(dev.shape)
         assert np.abs(dev).max() > 0
         assert (dev.view(np.uint32) == host.view(np.uint32)).all()
+
+
+def test_host_frame_replay_reads_new_inputs(ctx):
+    """A repeated call replays the captured frame, which copies whatever the host buffers hold at the
+    time: new contents of the same buffers give the new frame's result."""
+    import torch
+
+    cfg = mlgi.C0
+    sa, sb = scene(cfg), scene(cfg.replace(seed=cfg.seed + 11, name="c0_b"))
+    pinned = pinned_inputs(sa)
+    hfd = host_frame_desc(sa, pinned)
+    for _ in range(3):  # direct, captured, replayed
+        ctx.gi_frame_host(hfd, pinned["rgb"].numpy())
+    for k, v in pinned_inputs(sb).items():  # same shapes, new contents, same buffers
+        pinned[k].copy_(v)
+    pinned["rgb"].zero_()
+    ctx.gi_frame_host(hfd, pinned["rgb"].numpy())
+    df = DeviceFrame(sb)
+    ctx.gi_frame(df.frame_desc(), df.radiance())
+    torch.cuda.synchronize()
+    dev = df.rgb_np()
+    host = pinned["rgb"].numpy().reshape(dev.shape)
+    assert np.abs(dev).max() > 0
+    assert (dev.view(np.uint32) == host.view(np.uint32)).all()
 
 
 def test_host_frame_vpl_subrange_scaled_isms(ctx):
