@@ -1042,7 +1042,9 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
                                                                   z.radiance / (3u << 20)}));
     int tr0 = 0;
     for (int k = 0; k < bands; ++k) {
-        const int tr1 = tr0 + tile_rows / bands + (k < tile_rows % bands ? 1 : 0);  // wider bands first
+        // narrower bands first: the downloads, which the link makes slower than the gathering,
+        // start after the first band
+        const int tr1 = tr0 + tile_rows / bands + (k >= bands - tile_rows % bands ? 1 : 0);
         cudaStream_t bs = (k & 1) ? s2 : s;
         MLGI_CUDA(ctx, mlgi::launch_final_gather(fa, bs, tr0, tr1));
         MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_band[k], bs));
