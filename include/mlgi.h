@@ -168,16 +168,17 @@ mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_
 /* No counterpart in the reference. Allocation-free ISM rendering for callers that cannot
  * allocate device memory (their device memory is reserved up front by another allocator, or
  * they run in a plugin or callback that is only handed pre-allocated buffers): clears, splats
- * and pull-pushes like mlgi_ism_splat + mlgi_pullpush, but keeps the intermediate key atlas in a
- * fixed device array inside the library instead of allocating one. Needs no context; runs on
+ * and pull-pushes like mlgi_ism_splat + mlgi_pullpush, but keeps its intermediates (the key
+ * atlas and pull-push pyramid levels 1 and 2) in fixed device arrays inside the library instead
+ * of allocating them. Needs no context; runs on
  * the current device and on `stream` (NULL = the legacy default stream).
  *   - Atlas limit: grid_x*ism_size * grid_y*ism_size <= 1,048,576 texels (e.g. 1024 x 1024);
- *     larger atlases return MLGI_EINVAL. Each GPU that loads the library holds that 4 MiB array
- *     until the process exits.
- *   - The first call on a device looks the array up with that device current; make it before
+ *     larger atlases return MLGI_EINVAL. Each GPU that loads the library holds these arrays
+ *     (4 MiB of keys, 5 MiB of pyramid levels) until the process exits.
+ *   - The first call on a device looks the arrays up with that device current; make it before
  *     any stream capture.
- *   - Every call shares the array (it is cleared at the start of each call); calls whose work
- *     overlaps on the GPU race on it.
+ *   - Every call shares the arrays (the keys are cleared at the start of each call); calls whose
+ *     work overlaps on the GPU race on them.
  *   - Calls no cudaMalloc, cudaFree or allocating library routine. */
 mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi_vpl_buf* vpls, int n_vpl,
                                    const mlgi_ism_params* params, void* depth_out, int depth_format,
