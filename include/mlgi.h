@@ -173,10 +173,15 @@ mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_
  * of allocating them. Needs no context; runs on
  * the current device and on `stream` (NULL = the legacy default stream).
  *   - Atlas limit: grid_x*ism_size * grid_y*ism_size <= 1,048,576 texels (e.g. 1024 x 1024);
- *     larger atlases return MLGI_EINVAL. Each GPU that loads the library holds these arrays
- *     (4 MiB of keys, 5 MiB of pyramid levels) until the process exits.
- *   - The first call on a device looks the arrays up with that device current; make it before
- *     any stream capture.
+ *     larger atlases, and any geometry mlgi_ism_splat refuses, return MLGI_EINVAL.
+ *   - The arrays (4 MiB of keys, 5 MiB of pyramid levels) are reserved on a device by the first
+ *     call on it (under the CUDA runtime's default lazy module loading; at context creation with
+ *     CUDA_MODULE_LOADING=EAGER) and stay until the process exits. A caller whose own allocator
+ *     reserves the device memory up front should make that first call before the reservation;
+ *     without room for the arrays the first call returns MLGI_ENOMEM. The first call looks the
+ *     arrays up with the device current; make it before any stream capture. The addresses are
+ *     kept per device for the process's life: do not use this entry point on a device after
+ *     cudaDeviceReset.
  *   - Every call shares the arrays (the keys are cleared at the start of each call); calls whose
  *     work overlaps on the GPU race on them.
  *   - Calls no cudaMalloc, cudaFree or allocating library routine. */

@@ -10,10 +10,18 @@
 // Limits and behaviour:
 //   * The key atlas holds at most kStaticKeyTexels = 1,048,576 texels (a 1024 x 1024 atlas,
 //     4 MiB), the pyramid levels a quarter and a sixteenth of that as float4 (5 MiB). Larger
-//     atlases are rejected with MLGI_EINVAL. Every GPU that loads this library keeps those 9 MiB
-//     reserved until the process exits.
-//   * The first call on a device resolves the arrays' device addresses (cudaGetSymbolAddress)
-//     with that device current; make that first call before any stream capture.
+//     atlases are rejected with MLGI_EINVAL, and so is any geometry the allocating entry points
+//     refuse (the same checks, e.g. at most 65535 texels a side).
+//   * When the 9 MiB are reserved: the arrays belong to this file's module. Under the CUDA
+//     runtime's default lazy module loading, a device creates the module -- and reserves the
+//     9 MiB -- at the first call on that device, when the call looks the arrays up
+//     (cudaGetSymbolAddress) with the device current; with CUDA_MODULE_LOADING=EAGER it happens
+//     when the context is created. A caller whose other allocator reserves the device's memory
+//     up front should make its first call before that reservation (or load eagerly); if the
+//     reservation leaves no room, the first call returns MLGI_ENOMEM. From then on the arrays stay
+//     until the process exits. Make the first call before any stream capture.
+//   * The looked-up addresses are kept per device for the life of the process, so the entry
+//     point must not be used on a device after cudaDeviceReset of that device.
 //   * All calls share the one set of arrays. Each call clears it to the empty key (0xFFFFFFFF) before
 //     splatting, so nothing of a previous call leaks into the result, but calls whose work
 //     overlaps on the GPU (different streams, or different host threads) race on it.
@@ -57,7 +65,8 @@ mlgi_status static_addresses(uint32_t** keys, void** pyramid) {
         if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_static_pyramid);
         if (e != cudaSuccess || !p || !q) {
             cudaGetLastError();
-            return MLGI_ECUDA;
+            // loading the module reserves the arrays; no room for them is an allocation failure
+            return e == cudaErrorMemoryAllocation ? MLGI_ENOMEM : MLGI_ECUDA;
         }
         g_static_pyramid_dev[dev] = q;
         g_static_keys_dev[dev] = static_cast<uint32_t*>(p);
@@ -74,13 +83,11 @@ extern "C" mlgi_status mlgi_ism_render_static(const mlgi_points* pts, const mlgi
                                               mlgi_stream stream) {
     if (!pts || !vpls || !p || !depth_out) return MLGI_EINVAL;
     if (depth_format != MLGI_F32 && depth_format != MLGI_F16) return MLGI_EINVAL;
-    if (p->ism_size <= 0 || p->grid_x <= 0 || p->grid_y <= 0 || p->levels < 1 || p->levels > 10 ||
-        p->ism_size % (1 << p->levels) != 0 || !(p->z_far > 0.f))
-        return MLGI_EINVAL;
+    char why[160];
+    if (!mlgi::ism_params_valid(p, why, sizeof(why))) return MLGI_EINVAL;  // the allocating path's checks
     const size_t aw = (size_t)p->grid_x * p->ism_size, ah = (size_t)p->grid_y * p->ism_size;
     if (aw * ah > kStaticKeyTexels) return MLGI_EINVAL;  // beyond the static key atlas
-    if (p->vpl_start < 0 || p->vpl_end <= p->vpl_start || n_vpl <= 0 || n_vpl > vpls->capacity ||
-        p->vpl_end > n_vpl)
+    if (n_vpl <= 0 || n_vpl > vpls->capacity || p->vpl_end > n_vpl)
         return MLGI_EINVAL;
     const int vplCount = p->vpl_end - p->vpl_start;
     if ((p->scale_isms ? vplCount : n_vpl) > p->grid_x * p->grid_y) return MLGI_EINVAL;

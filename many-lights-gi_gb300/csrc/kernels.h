@@ -1,10 +1,17 @@
 // Launch interface between the C ABI (mlgi_api.cu) and the kernel translation units.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "mlgi.h"
+
 namespace mlgi {
+
+// The ISM geometry checks every entry point that takes mlgi_ism_params applies (sizes, level count,
+// atlas at most 65535 texels a side, far plane, VPL range); on failure `why` (n bytes) says why.
+bool ism_params_valid(const mlgi_ism_params* p, char* why, size_t n);
 
 struct VplArgs {
     int n;                 // VPL count (work items)

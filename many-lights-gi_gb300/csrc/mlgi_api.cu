@@ -16,6 +16,39 @@
 #include "kernels.h"
 #include "mlgi.h"
 
+namespace mlgi {
+
+bool ism_params_valid(const mlgi_ism_params* p, char* why, size_t n) {
+    if (!p) {
+        snprintf(why, n, "ism params are NULL");
+        return false;
+    }
+    if (p->ism_size <= 0 || p->grid_x <= 0 || p->grid_y <= 0 || p->levels < 1 || p->levels > 10) {
+        snprintf(why, n, "bad ISM geometry (size %d, grid %dx%d, levels %d)", p->ism_size, p->grid_x, p->grid_y,
+                 p->levels);
+        return false;
+    }
+    if (p->ism_size % (1 << p->levels) != 0) {
+        snprintf(why, n, "ISM size %d is not divisible by 2^%d", p->ism_size, p->levels);
+        return false;
+    }
+    if ((int64_t)p->grid_x * p->ism_size > 65535 || (int64_t)p->grid_y * p->ism_size > 65535) {
+        snprintf(why, n, "atlas larger than 65535 texels on a side");
+        return false;
+    }
+    if (!(p->z_far > 0.f)) {
+        snprintf(why, n, "z_far must be positive");
+        return false;
+    }
+    if (p->vpl_end <= p->vpl_start || p->vpl_start < 0) {
+        snprintf(why, n, "empty VPL range [%d, %d)", p->vpl_start, p->vpl_end);
+        return false;
+    }
+    return true;
+}
+
+}  // namespace mlgi
+
 namespace {
 
 struct DevBuf {
@@ -216,17 +249,8 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 mlgi_status check_ism(mlgi_ctx* ctx, const mlgi_ism_params* p) {
-    if (!p) return fail(ctx, MLGI_EINVAL, "ism params are NULL");
-    if (p->ism_size <= 0 || p->grid_x <= 0 || p->grid_y <= 0 || p->levels < 1 || p->levels > 10)
-        return fail(ctx, MLGI_EINVAL, "bad ISM geometry (size %d, grid %dx%d, levels %d)", p->ism_size, p->grid_x,
-                    p->grid_y, p->levels);
-    if (p->ism_size % (1 << p->levels) != 0)
-        return fail(ctx, MLGI_EINVAL, "ISM size %d is not divisible by 2^%d", p->ism_size, p->levels);
-    if ((int64_t)p->grid_x * p->ism_size > 65535 || (int64_t)p->grid_y * p->ism_size > 65535)
-        return fail(ctx, MLGI_EINVAL, "atlas larger than 65535 texels on a side");
-    if (!(p->z_far > 0.f)) return fail(ctx, MLGI_EINVAL, "z_far must be positive");
-    if (p->vpl_end <= p->vpl_start || p->vpl_start < 0)
-        return fail(ctx, MLGI_EINVAL, "empty VPL range [%d, %d)", p->vpl_start, p->vpl_end);
+    char why[160];
+    if (!mlgi::ism_params_valid(p, why, sizeof(why))) return fail(ctx, MLGI_EINVAL, "%s", why);
     return MLGI_OK;
 }
 

@@ -4,7 +4,7 @@ The reference's hot path is five GLSL 4.3 compute shaders (paths inside the refe
   data/shaders/gi/vpl_processor.comp, data/shaders/ism/ism.comp, data/shaders/ism/pull.comp,
   data/shaders/ism/push.comp, data/shaders/gi/final_gathering.comp
 plus their includes (common/floatpacking.glsl, common/random.glsl, common/reprojection.glsl,
-ism/ism_utils.glsl). This recipe reads them where they lie under /root/reference, applies a fixed
+ism/ism_utils.glsl). This recipe reads them where they lie under the reference root (REF below), applies a fixed
 list of mechanical GLSL -> C++ rewrites (below), and compiles the result together with
 oracle/ref_shim.hpp (GLSL types and built-ins) and oracle/ref_harness.cpp (images, buffers,
 dispatch, work-group fibers) into oracle/_ref/libref.so. No reference source is copied into the
@@ -38,7 +38,11 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+# Root of the reference project: MLGI_REFERENCE_ROOT, or `--reference <dir>` on the command line,
+# else where this build reads it.
+REF = os.environ.get("MLGI_REFERENCE_ROOT", "/root/reference")
+if "--reference" in sys.argv[:-1]:
+    REF = sys.argv[sys.argv.index("--reference") + 1]
 OUT = os.path.join(HERE, "_ref")
 GEN = os.path.join(OUT, "gen")
 LIB = os.path.join(OUT, "libref.so")
