@@ -31,8 +31,16 @@ METRIC = "1080p GI ms/frame"
 UNIT = "ms/frame"
 PASSES = ["vpl_process", "ism_clear", "ism_splat", "pullpush", "final_gather"]
 # kernels of a frame and their slots in Context.last_timings(); the pull-push pass is four launches
-KERNELS = [("vpl_process", 0), ("ism_clear", 1), ("ism_splat", 2), ("pull1", 7), ("pullmid", 8), ("push1", 9),
-           ("push0", 10), ("final_gather", 4)]
+def kernel_slots(cfg):
+    """(kernel, index in mlgi_last_timings) of every kernel of a frame. The pull-push pass is one
+    launch (`pyramid`, reported in the pass's last slot) when each ISM's pyramid runs in one block,
+    else level 1, the middle levels and push level 1 (two or more levels), and push level 0."""
+    import mlgi
+
+    n = mlgi.pullpush_launches(cfg)
+    pp = [("pyramid", 10)] if n == 1 else [("pull1", 7), ("pullmid", 8), ("push1", 9), ("push0", 10)] if n == 4 \
+        else [("pull1", 7), ("push0", 10)]
+    return [("vpl_process", 0), ("ism_clear", 1), ("ism_splat", 2)] + pp + [("final_gather", 4)]
 
 
 def parse():
@@ -55,10 +63,9 @@ def parse():
 
 
 def launches_per_frame(cfg):
-    """Kernels of one mlgi_gi_frame: VPL processing, atlas clear, splat, pull-push (level 1, the
-    per-ISM middle levels and push level 1 when there are two or more levels, push level 0) and
-    final gathering."""
-    return 3 + (4 if cfg.levels >= 2 else 2) + 1
+    """Kernels of one mlgi_gi_frame: VPL processing, atlas clear, splat, the pull-push pass's launches
+    and final gathering."""
+    return len(kernel_slots(cfg))
 
 
 # ---- algorithmic bytes per pass and per kernel (one launch each per frame) ----------------------
@@ -83,6 +90,7 @@ def algorithmic_bytes(cfg, bucket_stride):
         "pullmid": (atlas // 4 * 16 + atlas // 16 * 16) if two else 0,
         "push1": (atlas // 16 * 16 + atlas // 4 * 32) if two else 0,
         "push0": atlas // 4 * 16 + atlas * 4 + atlas * out,
+        "pyramid": atlas * (4 + out),
     }
 
 
@@ -430,8 +438,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
     value = total_ms / frames
     mean_all = passes.mean(axis=0)
     mean_pass = mean_all[:5]
-    kernel_ms = {n: float(mean_all[i]) for n, i in KERNELS if n in ("pull1", "vpl_process", "ism_clear", "ism_splat",
-                                                                     "push0", "final_gather") or cfg.levels >= 2}
+    kernel_ms = {n: float(mean_all[i]) for n, i in kernel_slots(cfg)}
     ab = algorithmic_bytes(cfg, scene.bucket_stride)
     dom_name = max(kernel_ms, key=kernel_ms.get)  # the dominant kernel
     peak, peak_kind = measured_peak_gbs()
@@ -573,7 +580,9 @@ def run_batch(args, rank, world, local_rank):
                        "l2": "inputs larger than L2"},
             "frames_per_s": n / (value * 1e-3), "forms": forms, "plain_ms_per_batch": plain_ms,
             "plain_frames_per_s": n / (plain_ms * 1e-3), "speedup_vs_plain": plain_ms / value,
-            "plain_kernels_ms": {k: float(plain_kernels[i]) for k, i in KERNELS},
+            "plain_kernels_ms": {k: float(plain_kernels[i]) for k, i in
+                                 [("vpl_process", 0), ("ism_clear", 1), ("ism_splat", 2), ("pull1", 7),
+                                  ("pullmid", 8), ("push1", 9), ("push0 or pyramid", 10), ("final_gather", 4)]},
             "gpu_launches": forms[best]["kernel_launches"] * args.steps, "autotune_s": t_tune,
             "clocks": clocks}), flush=True)
     ctx.close()

@@ -164,6 +164,11 @@ mlgi_status mlgi_ism_splat_range(mlgi_ctx* ctx, const mlgi_points* pts, const ml
                                  mlgi_stream stream);
 mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* params, int row0, int row1,
                                mlgi_stream stream);
+/* No counterpart in the reference: the number of kernel launches mlgi_pullpush issues for this
+ * geometry -- 1 when an ISM's whole pyramid runs in one block (ISM edges up to 128 with two or more
+ * levels, far plane in [2^-20, 2^20]), 4 (2 for one level) otherwise -- or -1 for a geometry
+ * mlgi_pullpush refuses. */
+int mlgi_pullpush_launches(const mlgi_ism_params* params);
 
 /* No counterpart in the reference. Allocation-free ISM rendering for callers that cannot
  * allocate device memory (their device memory is reserved up front by another allocator, or

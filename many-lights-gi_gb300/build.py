@@ -34,7 +34,7 @@ CUDA_UNITS = [
 ]
 # The scene fixture must be identical on x86 and Arm hosts: no FMA contraction in its double math.
 HOST_UNITS = [("host/scene.cpp", ["-O3", "-fopenmp", "-fPIC", "-std=c++17", "-ffp-contract=off", f"-I{INCLUDE}"])]
-DEPS = ["csrc/gi_device.cuh", "csrc/kernels.h", "csrc/batch_items.cuh", "host/room.h"]
+DEPS = ["csrc/gi_device.cuh", "csrc/kernels.h", "csrc/batch_items.cuh", "csrc/pyramid.cuh", "host/room.h"]
 
 
 def nvcc() -> str:

@@ -1,11 +1,14 @@
-// VPL processing, ISM point splat and the fused pull-push pyramid.
+// VPL processing, ISM point splat and the pull-push pyramid.
 //
 // This translation unit is compiled with -fmad=false and IEEE division/square root so that its
 // FP32 results are word-for-word those of the reference shaders' arithmetic in GLSL order:
 //   vpl_process_kernel  <- data/shaders/gi/vpl_processor.comp:41-72
 //   ism_splat_kernel    <- data/shaders/ism/ism.comp:54-139
-//   pullpush_kernel     <- data/shaders/ism/pull.comp:20-126 and push.comp:44-165, as driven by
-//                          ImperfectShadowmap::pullpush (ImperfectShadowmap.cpp:121-182)
+//   pyramid_kernel      <- data/shaders/ism/pull.comp:20-126 and push.comp:44-165, as driven by
+//                          ImperfectShadowmap::pullpush (ImperfectShadowmap.cpp:121-182): an
+//                          ISM's whole pyramid in one block (pyramid.cuh); pull1_kernel,
+//                          pullmid_kernel, push1_kernel and push0_kernel run it level by level
+//                          for ISMs too large for that
 #include <cuda_runtime.h>
 
 #include "batch_items.cuh"
@@ -797,6 +800,8 @@ size_t pullmid_smem_bytes(int ism_size, int levels) {
     return b;
 }
 
+#include "pyramid.cuh"
+
 size_t pullpush_scratch_bytes(int atlas_w, int atlas_h, int levels, size_t* lv2_offset) {
     const size_t lv1 = (size_t)(atlas_w >> 1) * (atlas_h >> 1) * 16;
     const size_t lv2 = levels >= 2 ? (size_t)(atlas_w >> 2) * (atlas_h >> 2) * 16 : 0;
@@ -813,6 +818,7 @@ cudaError_t pullpush_prepare(size_t smem) {
     cudaError_t e = cudaFuncSetAttribute(pullmid_kernel<kPullMidThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(pullmid_kernel<kPullMidWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = pyramid_prepare();
     return e;
 }
 
@@ -842,6 +848,10 @@ static PullPushGrids pullpush_grids(const PullPushArgs& a) {
 
 cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
     if (a.row1 <= a.row0) return cudaSuccess;
+    if (pyramid_fused(a.ism_size, a.levels, a.z_far)) {
+        launch_pyramid(a, s);
+        return cudaGetLastError();
+    }
     const PullPushGrids g = pullpush_grids(a);
     pull1_kernel<<<g.g1, kPpTileW * kPpTileH, 0, s>>>(a);
     if (a.levels >= 2) {
@@ -854,6 +864,14 @@ cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
 
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks) {
     if (a.row1 <= a.row0) return cudaSuccess;
+    if (pyramid_fused(a.ism_size, a.levels, a.z_far)) {
+        const cudaError_t e = pyramid_prepare();
+        if (e != cudaSuccess) return e;
+        if (marks)  // one launch: the pass's time lands in the last of the four slots
+            for (int k = 0; k < 3; ++k) cudaEventRecord(marks[k], s);
+        launch_pyramid(a, s);
+        return cudaGetLastError();
+    }
     const PullPushGrids g = pullpush_grids(a);
     pull1_kernel<<<g.g1, kPpTileW * kPpTileH, 0, s>>>(a);
     if (marks) cudaEventRecord(marks[0], s);

@@ -195,6 +195,11 @@ cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s);
 // Shared memory of the per-ISM middle pass (levels 2..L), and the lv1 + lv2 scratch in bytes
 // (lv2 starts at *lv2_offset).
 size_t pullmid_smem_bytes(int ism_size, int levels);
+// Whether launch_pullpush runs an ISM's whole pyramid in one block (pyramid_kernel, no scratch;
+// ISM edges up to 128, far plane in [2^-20, 2^20]) rather than in four launches over the lv1/lv2
+// scratch; its shared memory per block.
+bool pyramid_fused(int ism_size, int levels, float z_far);
+size_t pyramid_smem_bytes(int ism_size, int levels);
 size_t pullpush_scratch_bytes(int atlas_w, int atlas_h, int levels, size_t* lv2_offset);
 int pullpush_batch_items(int pass, int atlas_w, int atlas_h, int ism_count, int levels);
 // Tile rows [tile_row0, tile_row1) of the gathering (tile_row1 < 0: through the last).

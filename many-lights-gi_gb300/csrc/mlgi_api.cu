@@ -263,6 +263,13 @@ mlgi_status check_atlas(mlgi_ctx* ctx, const mlgi_atlas* a, const mlgi_ism_param
     return MLGI_OK;
 }
 
+// Pull-push scratch of a context: the lv1/lv2 levels of the four-launch form, none for ISMs whose
+// pyramid runs in one block (a token allocation, so that the scratch pointer is never NULL).
+size_t pullpush_scratch_need(int atlas_w, int atlas_h, const mlgi_ism_params* p) {
+    if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far)) return 16;
+    return std::max<size_t>(16, mlgi::pullpush_scratch_bytes(atlas_w, atlas_h, p->levels, nullptr));
+}
+
 }  // namespace
 
 extern "C" {
@@ -577,8 +584,9 @@ mlgi_status mlgi_ism_splat(mlgi_ctx* ctx, const mlgi_points* pts, const mlgi_vpl
 mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* p, mlgi_stream stream) {
     if (!ctx) return MLGI_EINVAL;
     if (!atlas || !p) return fail(ctx, MLGI_EINVAL, "NULL argument");
-    mlgi_status st =
-        ensure(ctx, ctx->pp, std::max<size_t>(16, mlgi::pullpush_scratch_bytes(atlas->width, atlas->height, p->levels, nullptr)));
+    mlgi_status st = check_ism(ctx, p);
+    if (st == MLGI_OK) st = check_atlas(ctx, atlas, p);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->pp, pullpush_scratch_need(atlas->width, atlas->height, p));
     if (st != MLGI_OK) return st;
     mlgi::PullPushArgs a;
     if ((st = build_pullpush_args(ctx, atlas, p, ctx->pp.p, a)) != MLGI_OK) return st;
@@ -633,8 +641,9 @@ mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_
     if (!atlas || !p) return fail(ctx, MLGI_EINVAL, "NULL argument");
     if (row0 < 0 || row1 < row0 || row1 > p->grid_y)
         return fail(ctx, MLGI_EINVAL, "ISM rows [%d, %d) outside the grid's %d rows", row0, row1, p->grid_y);
-    mlgi_status st =
-        ensure(ctx, ctx->pp, std::max<size_t>(16, mlgi::pullpush_scratch_bytes(atlas->width, atlas->height, p->levels, nullptr)));
+    mlgi_status st = check_ism(ctx, p);
+    if (st == MLGI_OK) st = check_atlas(ctx, atlas, p);
+    if (st == MLGI_OK) st = ensure(ctx, ctx->pp, pullpush_scratch_need(atlas->width, atlas->height, p));
     if (st != MLGI_OK) return st;
     mlgi::PullPushArgs a;
     if ((st = build_pullpush_args(ctx, atlas, p, ctx->pp.p, a)) != MLGI_OK) return st;
@@ -642,6 +651,13 @@ mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_
     a.row1 = row1;
     MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream)));
     return MLGI_OK;
+}
+
+int mlgi_pullpush_launches(const mlgi_ism_params* p) {
+    char why[160];
+    if (!mlgi::ism_params_valid(p, why, sizeof(why))) return -1;
+    if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far)) return 1;
+    return p->levels >= 2 ? 4 : 2;
 }
 
 mlgi_status mlgi_cluster_lights(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls, int n_vpl,
@@ -922,7 +938,7 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     if (st == MLGI_OK) st = ensure(ctx, ctx->keys, (size_t)aw * ah * 4);
     if (st == MLGI_OK) st = ensure(ctx, ctx->depth, (size_t)aw * ah * (d.atlas_format == MLGI_F16 ? 2 : 4));
     if (st == MLGI_OK)
-        st = ensure(ctx, ctx->pp, std::max<size_t>(16, mlgi::pullpush_scratch_bytes(aw, ah, d.ism.levels, nullptr)));
+        st = ensure(ctx, ctx->pp, pullpush_scratch_need(aw, ah, &d.ism));
     if (st != MLGI_OK) return st;
     mlgi_vpl_buf vb{n, static_cast<float*>(ctx->vpl.p), static_cast<float*>(ctx->packed.p),
                     reduced ? ctx->reduced.p : nullptr};

@@ -177,6 +177,7 @@ _SIGS = {
     "mlgi_ism_splat_range": (C.c_int32, [_p, C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams),
                                          C.POINTER(Atlas), C.c_int, C.c_int, _p]),
     "mlgi_pullpush_rows": (C.c_int32, [_p, C.POINTER(Atlas), C.POINTER(IsmParams), C.c_int, C.c_int, _p]),
+    "mlgi_pullpush_launches": (C.c_int, [C.POINTER(IsmParams)]),
     "mlgi_ism_render_static": (C.c_int32, [C.POINTER(Points), C.POINTER(VplBuf), C.c_int, C.POINTER(IsmParams), _p,
                                            C.c_int, _p]),
     "mlgi_final_gather": (C.c_int32, [_p, C.POINTER(GBufferView), C.POINTER(VplBuf), C.POINTER(Atlas),
@@ -498,6 +499,12 @@ def depth_terms(scene: "Scene") -> tuple[float, float]:
 
 def ism_params(cfg: Config) -> IsmParams:
     return IsmParams(0, cfg.n_vpl, 0, 0, cfg.ism_size, cfg.grid_x, cfg.grid_y, cfg.levels, cfg.z_far)
+
+
+def pullpush_launches(cfg: Config) -> int:
+    """Kernel launches of mlgi_pullpush for the configuration: 1 when each ISM's whole pyramid runs in
+    one block, 4 (2 for a single level) for the per-level form."""
+    return lib().mlgi_pullpush_launches(C.byref(ism_params(cfg)))
 
 
 def vpl_params(cfg: Config, scene: Scene) -> VplParams:

@@ -188,7 +188,7 @@ def test_ism_splat_empty_buckets(ctx):
 @pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2, mlgi.C3B.replace(reduced=False, name="c3b_fp32")],
                          ids=lambda c: c.name)
 def test_pullpush_bit_exact(ctx, cfg):
-    """Fused per-ISM pyramid vs the level-by-level restatement of pull.comp/push.comp."""
+    """The one-block-per-ISM pyramid vs the level-by-level restatement of pull.comp/push.comp."""
     import torch
 
     sc = scene(cfg)
@@ -202,6 +202,32 @@ def test_pullpush_bit_exact(ctx, cfg):
     torch.cuda.synchronize()
     fin = df.atlas_np()
     assert (ofin < 0.99).mean() > (okeys >> 8 < 0.99 * 2 ** 24).mean()  # the pyramid fills holes
+    mism = int((fin.view(np.uint32) != ofin.view(np.uint32)).sum())
+    assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
+
+
+@pytest.mark.parametrize("geom", [(mlgi.C1, 256, 4, 4, 4), (mlgi.C0, 32, 8, 8, 1)],
+                         ids=["c1_keys_as_256px_isms", "c0_one_level"])
+def test_pullpush_per_level_form_bit_exact(ctx, geom):
+    """The four-launch (or, for one level, two-launch) pull-push that serves ISMs whose pyramid does
+    not fit one block's shared memory, against the level-by-level restatement: a splatted atlas read
+    as 4 x 4 ISMs of 256^2 texels with 4 levels, and C0's atlas with a single level."""
+    import torch
+
+    cfg, ism, gx, gy, levels = geom
+    sc = scene(cfg)
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    g = cfg.replace(ism_size=ism, grid_x=gx, grid_y=gy, levels=levels, name="per_level")
+    assert (g.atlas_w, g.atlas_h) == (cfg.atlas_w, cfg.atlas_h)
+    assert mlgi.pullpush_launches(g) == (4 if levels >= 2 else 2)
+    ofin = O.pullpush(okeys, ism, levels, cfg.z_far)
+    df = DeviceFrame(sc)
+    df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
+    ctx.pullpush(mlgi.Atlas(g.atlas_w, g.atlas_h, mlgi.ptr(df.keys), mlgi.ptr(df.atlas), mlgi.F32), mlgi.ism_params(g))
+    torch.cuda.synchronize()
+    fin = df.atlas_np()
     mism = int((fin.view(np.uint32) != ofin.view(np.uint32)).sum())
     assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
 
