@@ -502,6 +502,14 @@ mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n);
 /* Synchronise `stream` and report device-side errors recorded since the last check
  * (MLGI_ETIMEDOUT when a bounded wait inside a kernel gave up). Clears the error word. */
 mlgi_status mlgi_check_device_status(mlgi_ctx* ctx, mlgi_stream stream);
+/* No counterpart in the reference: exercises the bounded device wait. The gathering stages each
+ * VPL slice with a bulk copy completed on an mbarrier, and waits for it at most `wait_cycles` SM
+ * cycles (0 restores the default, about 2^31; else 1000..2^31). A nonzero `extra_tx_bytes` (test
+ * only, at most 4096) makes each block's first staging wait expect that many bytes more than its
+ * copy delivers, so that the wait runs out: the block sets the status word, retires the surplus,
+ * lets its copy land and returns, and mlgi_check_device_status then reports MLGI_ETIMEDOUT. The
+ * settings apply to the context's later mlgi_final_gather calls; set (0, 0) to return to normal. */
+mlgi_status mlgi_set_gather_wait_test(mlgi_ctx* ctx, int64_t wait_cycles, uint32_t extra_tx_bytes);
 
 /* ---- scene fixture (host) ----------------------------------------------------------------- */
 

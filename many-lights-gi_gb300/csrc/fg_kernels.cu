@@ -49,9 +49,13 @@ __device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_
         "l"(src), "r"(bytes), "r"(smem_addr(bar))
         : "memory");
 }
-// Bounded wait on an mbarrier phase: gives up after ~2^31 SM cycles (about a second) and
-// returns false, so a lost transfer can never hang the GPU.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Retires `bytes` of an mbarrier's expected transaction count without a copy.
+__device__ __forceinline__ void mbar_complete_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// Bounded wait on an mbarrier phase: gives up after `limit` SM cycles (by default ~2^31, about a
+// second) and returns false, so a lost transfer can never hang the GPU.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = 1ll << 31) {
     const long long t0 = clock64();
     for (;;) {
         uint32_t done;
@@ -63,7 +67,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
             : "r"(smem_addr(bar)), "r"(parity)
             : "memory");
         if (done) return true;
-        if (clock64() - t0 > (1ll << 31)) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 
@@ -264,7 +268,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     const size_t bytes0 = (size_t)min(kChunk, a.per_class) * kRec;
     const bool early = use_tma && bytes0 % 16 == 0;
     if (early && tid == 0) {
-        mbar_expect_tx(&S.bar, (uint32_t)bytes0);
+        mbar_expect_tx(&S.bar, (uint32_t)bytes0 + a.test_extra_tx);
         tma_bulk_g2s(S.raw, src + (size_t)vbase * kRec, (uint32_t)bytes0, &S.bar);
     }
     const int sw = (a.width + I - 1) / I;
@@ -350,14 +354,18 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         const size_t bytes = (size_t)cnt * kRec;
         if (use_tma && bytes % 16 == 0) {
             if (tid == 0 && !(base == 0 && early)) {  // the first chunk's copy was issued at the start
-                mbar_expect_tx(&S.bar, (uint32_t)bytes);
+                mbar_expect_tx(&S.bar, (uint32_t)bytes + (base == 0 ? a.test_extra_tx : 0u));
                 tma_bulk_g2s(S.raw, src + (size_t)(vbase + base) * kRec, (uint32_t)bytes, &S.bar);
             }
-            const bool ok = __syncthreads_and(mbar_wait(&S.bar, parity));
-            if (!ok) {  // block-uniform: flag the error, give the copy one more bounded wait, leave
+            const long long limit = a.wait_cycles > 0 ? a.wait_cycles : 1ll << 31;
+            const bool ok = __syncthreads_and(mbar_wait(&S.bar, parity, limit));
+            if (!ok) {  // block-uniform: flag the error, let the copy land (one more bounded wait), leave
                 if (tid == 0) {
                     atomicOr(a.status, kStatusTmaTimeout);
-                    mbar_wait(&S.bar, parity);
+                    // a test surplus of expected bytes (never delivered) is retired first, so that
+                    // the phase completes once the real copy has landed
+                    if (base == 0 && a.test_extra_tx) mbar_complete_tx(&S.bar, a.test_extra_tx);
+                    mbar_wait(&S.bar, parity, 1ll << 31);
                 }
                 return false;
             }

@@ -89,6 +89,8 @@ struct FgArgs {
     float influence_cutoff;   // 0: off
     float* out;               // width*height*3
     uint32_t* status;         // device error word (bit 0: VPL staging wait timed out)
+    long long wait_cycles;    // limit of the VPL staging wait in SM cycles (0: about 2^31)
+    uint32_t test_extra_tx;   // test only: bytes the first staging wait expects beyond its copy (0)
     // cull == 2: clustered culling; a pixel keeps the VPLs of its cluster's mask
     const uint32_t* cl_masks;     // (tiles_x * tiles_y * 16) x cl_words
     const uint8_t* cl_slice;      // per pixel

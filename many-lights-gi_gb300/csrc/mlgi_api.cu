@@ -138,6 +138,8 @@ struct mlgi_ctx {
     std::map<int, int32_t*> shuffle_dev;  // per VPL count
     uint32_t* status = nullptr;           // device error word
     uint32_t* status_host = nullptr;      // pinned copy of it, written by host frames
+    long long fg_wait_cycles = 0;         // gathering's staging-wait limit (0: about 2^31 cycles)
+    uint32_t fg_test_extra_tx = 0;        // test only: surplus of expected staging bytes
     // frame-level buffers
     DevBuf vpl, packed, reduced, keys, depth;
     DevBuf pp;  // pull-push pyramid levels 1 and 2
@@ -548,6 +550,8 @@ mlgi_status build_fg_args(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_
     a.influence_cutoff = p->influence_cutoff;
     a.out = out->rgb;
     a.status = ctx->status;
+    a.wait_cycles = ctx->fg_wait_cycles;
+    a.test_extra_tx = ctx->fg_test_extra_tx;
     a.gx = p->grid_x > 0 ? p->grid_x : 1;
     a.gy = p->grid_y > 0 ? p->grid_y : 1;
     a.ism_size = p->ism_size > 0 ? p->ism_size : 1;
@@ -737,6 +741,17 @@ mlgi_status mlgi_final_gather(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const m
     const mlgi_status st = prepare_fg(ctx, g, vpls, atlas, p, out, stream, a);
     if (st != MLGI_OK) return st;
     MLGI_CUDA(ctx, mlgi::launch_final_gather(a, pick(ctx, stream)));
+    return MLGI_OK;
+}
+
+mlgi_status mlgi_set_gather_wait_test(mlgi_ctx* ctx, int64_t wait_cycles, uint32_t extra_tx_bytes) {
+    if (!ctx) return MLGI_EINVAL;
+    if (wait_cycles < 0 || wait_cycles > (int64_t(1) << 31) || (wait_cycles > 0 && wait_cycles < 1000) ||
+        extra_tx_bytes > 4096)
+        return fail(ctx, MLGI_EINVAL, "wait limit %lld cycles / surplus %u bytes out of range", (long long)wait_cycles,
+                    extra_tx_bytes);
+    ctx->fg_wait_cycles = wait_cycles;
+    ctx->fg_test_extra_tx = extra_tx_bytes;
     return MLGI_OK;
 }
 

@@ -212,6 +212,7 @@ _SIGS = {
     "mlgi_set_timing": (C.c_int32, [_p, C.c_int]),
     "mlgi_last_timings": (C.c_int32, [_p, _p, C.c_int]),
     "mlgi_check_device_status": (C.c_int32, [_p, _p]),
+    "mlgi_set_gather_wait_test": (C.c_int32, [_p, C.c_int64, C.c_uint32]),
     "mlgi_scene_generate": (C.c_int32, [C.POINTER(SceneDesc), C.POINTER(SceneInfo), _p, _p, _p, _p, _p, _p, _p, _p]),
     "mlgi_scene_generate_device": (C.c_int32, [C.POINTER(SceneDesc), C.POINTER(SceneInfo), _p, _p, C.c_int, _p, _p, _p,
                                                _p, _p, _p, _p]),
