@@ -59,6 +59,11 @@ def parse():
     ap.add_argument("--seed", type=int, default=5, help="served form: request-stream seed")
     ap.add_argument("--views", type=int, default=32, help="batched form: views per batch")
     ap.add_argument("--batch-streams", type=int, default=4, help="batched form: streams of the concurrent form")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the bounded batched and served measurements")
+    ap.add_argument("--extra-batch-steps", type=int, default=10, help="default workload: timed batches per form")
+    ap.add_argument("--extra-serve-seconds", type=float, default=2.0,
+                    help="default workload: seconds of arrivals per served/plain stream")
     return ap.parse_args()
 
 
@@ -478,6 +483,21 @@ def run_gpu(args, cfg, rank, world, local_rank):
         "wall_s": wall,
         "post": post,
     }
+    if not args.no_extras and world == 1:
+        # the batched and served halves of the metric, bounded: a 32-view batch in both forms and a
+        # few seconds of the served Poisson stream against the plain arm
+        ctx.close()
+        ctx = None
+        b = measure_batch(local_rank, args.views, args.extra_batch_steps, 2, args.batch_streams)
+        line["batched"] = {k: b[k] for k in ("views", "form", "ms_per_batch", "frames_per_s", "forms",
+                                              "plain_ms_per_batch", "plain_frames_per_s", "speedup_vs_plain",
+                                              "kernel_launches_per_batch", "steps", "warmup", "autotune_s")}
+        line["batched"]["workload"] = "c4_batch32: 32 views of 8 rooms, autotuned"
+        sv = measure_serve(local_rank, args.slots, args.rate, args.extra_serve_seconds, args.seed)
+        line["served"] = {k: sv[k] for k in ("served", "plain", "served_at_75pct", "plain_at_75pct",
+                                              "speedup_vs_plain", "single_frame_ms",
+                                              "results_identical_served_vs_plain", "config")}
+        line["served"]["workload"] = "c5_served_poisson (bounded duration)"
     if not args.no_cpu_baseline and world == 1:
         ms, threads, nframes, cpu_passes = time_cpu(cfg, scene, args.cpu_seconds)
         line["cpu_baseline"] = {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
@@ -485,7 +505,8 @@ def run_gpu(args, cfg, rank, world, local_rank):
                                           f"of the reference shaders, OpenMP on {threads} threads",
                                 "passes_ms": cpu_passes}
     print(json.dumps(line), flush=True)
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
 
 
 def c4_views(ctx, n_views=32, n_rooms=8, seed=4):
@@ -512,10 +533,10 @@ def c4_views(ctx, n_views=32, n_rooms=8, seed=4):
     return views
 
 
-def run_batch(args, rank, world, local_rank):
-    """Batched views (32 views of 8 rooms), replayed from CUDA graphs in two forms -- one persistent
-    launch per pass over all views, and each view's kernels spread over several streams -- against
-    one mlgi_gi_frame per view on one stream."""
+def measure_batch(local_rank, n_views, steps, warmup, batch_streams):
+    """Batched views (n_views views of 8 rooms), replayed from CUDA graphs in two forms -- one
+    persistent launch per pass over all views, and each view's kernels spread over several streams --
+    against one mlgi_gi_frame per view on one stream. Returns the measurements as a dict."""
     import numpy as np
     import torch
 
@@ -526,7 +547,7 @@ def run_batch(args, rank, world, local_rank):
     dev = f"cuda:{local_rank}"
     ctx = mlgi.Context(local_rank)
     t_tune = time.perf_counter()
-    cfgs = c4_views(ctx, n_views=args.views)
+    cfgs = c4_views(ctx, n_views=n_views)
     t_tune = time.perf_counter() - t_tune
     frames = [DeviceFrame.generated(c, dev) for c in cfgs]
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
@@ -534,21 +555,21 @@ def run_batch(args, rank, world, local_rank):
 
     def timed(step):
         with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
+            for _ in range(warmup):
                 step()
             torch.cuda.synchronize()
             ev[0].record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 step()
             ev[1].record(stream)
             torch.cuda.synchronize()
-        return ev[0].elapsed_time(ev[1]) / args.steps
+        return ev[0].elapsed_time(ev[1]) / steps
 
     sampler = ClockSampler(local_rank)
     sampler.start()
     forms = {}
     for name, form, streams in (("persistent", mlgi.BATCH_PERSISTENT, 0),
-                                ("concurrent", mlgi.BATCH_CONCURRENT, args.batch_streams)):
+                                ("concurrent", mlgi.BATCH_CONCURRENT, batch_streams)):
         batch = Batch(ctx, frames, form, streams)
         ms = timed(lambda: batch.launch(ctx.stream()))
         forms[name] = {"ms_per_batch": ms, "frames_per_s": len(frames) / (ms * 1e-3),
@@ -565,87 +586,101 @@ def run_batch(args, rank, world, local_rank):
         plain_kernels += ctx.last_timings()
     ctx.set_timing(False)
     ctx.check_device_status()
+    ctx.close()
     best = min(forms, key=lambda k: forms[k]["ms_per_batch"])
-    value = forms[best]["ms_per_batch"]
-    if rank == 0:
-        n = len(frames)
-        print(json.dumps({
-            "metric": f"batched GI ms per {args.views}-view batch", "value": value, "unit": "ms/batch", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "dtype": "f32 / fp16-bf16 mixed",
-            "data": "synthetic (seeded procedural rooms, generated on the GPU)",
-            "config": {"workload": "c4_batch32", "views": n, "rooms": 8, "form": best,
-                       "views_detail": [f"{c.width}x{c.height} N={c.n_vpl} pts=2^{int(np.log2(c.n_points))} "
-                                        f"I={c.interleave} ism={c.ism_size} {'fp16' if c.reduced else 'fp32'}"
-                                        for c in cfgs],
-                       "l2": "inputs larger than L2"},
-            "frames_per_s": n / (value * 1e-3), "forms": forms, "plain_ms_per_batch": plain_ms,
-            "plain_frames_per_s": n / (plain_ms * 1e-3), "speedup_vs_plain": plain_ms / value,
+    n = len(frames)
+    return {"views": n, "form": best, "ms_per_batch": forms[best]["ms_per_batch"],
+            "frames_per_s": n / (forms[best]["ms_per_batch"] * 1e-3), "forms": forms, "plain_ms_per_batch": plain_ms,
+            "plain_frames_per_s": n / (plain_ms * 1e-3), "speedup_vs_plain": plain_ms / forms[best]["ms_per_batch"],
+            "views_detail": [f"{c.width}x{c.height} N={c.n_vpl} pts=2^{int(np.log2(c.n_points))} "
+                             f"I={c.interleave} ism={c.ism_size} {'fp16' if c.reduced else 'fp32'}" for c in cfgs],
             "plain_kernels_ms": {k: float(plain_kernels[i]) for k, i in
                                  [("vpl_process", 0), ("ism_clear", 1), ("ism_splat", 2), ("pull1", 7),
                                   ("pullmid", 8), ("push1", 9), ("push0 or pyramid", 10), ("final_gather", 4)]},
-            "gpu_launches": forms[best]["kernel_launches"] * args.steps, "autotune_s": t_tune,
-            "clocks": clocks}), flush=True)
-    ctx.close()
+            "kernel_launches_per_batch": forms[best]["kernel_launches"], "steps": steps, "warmup": warmup,
+            "autotune_s": t_tune, "clocks": clocks}
 
 
-def run_serve(args, rank, world, local_rank):
+def run_batch(args, rank, world, local_rank):
+    r = measure_batch(local_rank, args.views, args.steps, args.warmup, args.batch_streams)
+    if rank == 0:
+        print(json.dumps({
+            "metric": f"batched GI ms per {args.views}-view batch", "value": r["ms_per_batch"], "unit": "ms/batch",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "dtype": "f32 / fp16-bf16 mixed", "data": "synthetic (seeded procedural rooms, generated on the GPU)",
+            "config": {"workload": "c4_batch32", "views": r["views"], "rooms": 8, "form": r["form"],
+                       "views_detail": r["views_detail"], "l2": "inputs larger than L2"},
+            "frames_per_s": r["frames_per_s"], "forms": r["forms"], "plain_ms_per_batch": r["plain_ms_per_batch"],
+            "plain_frames_per_s": r["plain_frames_per_s"], "speedup_vs_plain": r["speedup_vs_plain"],
+            "plain_kernels_ms": r["plain_kernels_ms"],
+            "gpu_launches": r["kernel_launches_per_batch"] * args.steps, "autotune_s": r["autotune_s"],
+            "clocks": r["clocks"]}), flush=True)
+
+
+def measure_serve(local_rank, slots, rate, duration, seed):
     """Served Poisson stream: open-loop arrivals (seeded) of frames drawn from the batched workload's
     size distribution (4 resolutions x 5 VPL counts x 4 point counts x 2 precisions), 8 rooms,
     light jitter +-5 degrees and a camera orbit step per request; served by the continuous-batching
-    server, then the same request sequence through the plain arm (one frame at a time)."""
+    server, then the same request sequence through the plain arm (one frame at a time). Returns the
+    measurements as a dict."""
     import numpy as np
 
     import mlgi
     from mlgi.serve import Server, shape_set
 
     shapes = shape_set()
-    sv = Server(slots=args.slots, max_width=2560, max_height=1440, hbm_budget=150 << 30, device=local_rank)
+    sv = Server(slots=slots, max_width=2560, max_height=1440, hbm_budget=150 << 30, device=local_rank)
     t = time.perf_counter()
     sv.prepare(shapes)
     t_prep = time.perf_counter() - t
     sampler = ClockSampler(local_rank)
     sampler.start()
     # warm-up: one short stream so that every room state of the run is not generated inside it
-    sv.run_poisson(shapes, rate_hz=args.rate, duration_s=min(1.0, args.duration), seed=args.seed + 1)
-    def stream(rate, seed, plain):
-        c, wall = sv.run_poisson(shapes, rate_hz=rate, duration_s=args.duration, seed=seed, plain=plain)
+    sv.run_poisson(shapes, rate_hz=rate, duration_s=min(1.0, duration), seed=seed + 1)
+
+    def stream(r, sd, plain):
+        c, wall = sv.run_poisson(shapes, rate_hz=r, duration_s=duration, seed=sd, plain=plain)
         ok = c["status"] == mlgi.OK
         lat = c["latency_ms"][ok]
-        return {"rate_hz": rate, "requests": int(len(c)), "ok": int(ok.sum()), "wall_s": wall,
+        return {"rate_hz": r, "requests": int(len(c)), "ok": int(ok.sum()), "wall_s": wall,
                 "frames_per_s": float(ok.sum() / wall), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_queue_ms": float(c["queue_ms"][ok].mean()),
                 "digests": {int(i): int(d) for i, d in zip(c["id"], c["digest"])}}
 
-    runs = {"served": stream(args.rate, args.seed, False), "plain": stream(args.rate, args.seed, True)}
+    runs = {"served": stream(rate, seed, False), "plain": stream(rate, seed, True)}
     # the same kind of stream at 75% of the served capacity just measured: latency below saturation
     rate75 = 0.75 * runs["served"]["frames_per_s"]
-    runs["served_at_75pct"] = stream(rate75, args.seed + 3, False)
-    runs["plain_at_75pct"] = stream(rate75, args.seed + 3, True)
+    runs["served_at_75pct"] = stream(rate75, seed + 3, False)
+    runs["plain_at_75pct"] = stream(rate75, seed + 3, True)
     clocks = sampler.stop()
     st = sv.stats()
     # single-frame latency: the plain arm at a rate it sustains (10% of its throughput)
     light_rate = max(1.0, 0.1 * runs["plain"]["frames_per_s"])
-    c1, _ = sv.run_poisson(shapes, rate_hz=light_rate, duration_s=args.duration, seed=args.seed + 2, plain=True)
+    c1, _ = sv.run_poisson(shapes, rate_hz=light_rate, duration_s=duration, seed=seed + 2, plain=True)
     single = c1["latency_ms"][c1["status"] == mlgi.OK]
     sv.close()
     same = (runs["served"]["digests"] == runs["plain"]["digests"]
             and runs["served_at_75pct"]["digests"] == runs["plain_at_75pct"]["digests"])
     for r in runs.values():
         r.pop("digests")
-    if rank == 0:
-        print(json.dumps({
-            "metric": "served GI frames/s", "value": runs["served"]["frames_per_s"], "unit": "frames/s",
-            "n_gpus": world, "steps": runs["served"]["requests"], "warmup": 1, "higher_is_better": True,
-            "dtype": "f32 / fp16-bf16 mixed", "data": "synthetic (seeded procedural rooms, generated on the GPU)",
-            "config": {"workload": "c5_served_poisson", "rate_hz": args.rate, "duration_s": args.duration,
-                       "seed": args.seed, "rooms": 8, "shapes": len(shapes), "slots": args.slots,
-                       "hbm_budget_gb": 150, "light_jitter_deg": 5, "orbit_step_deg": 0.5},
-            **runs,
-            "speedup_vs_plain": runs["served"]["frames_per_s"] / runs["plain"]["frames_per_s"],
+    return {**runs, "speedup_vs_plain": runs["served"]["frames_per_s"] / runs["plain"]["frames_per_s"],
             "single_frame_ms": {"p50": float(np.percentile(single, 50)), "p99": float(np.percentile(single, 99)),
                                 "rate_hz": light_rate},
             "results_identical_served_vs_plain": same, "prepare_s": t_prep, "server_stats": st,
-            "clocks": clocks}), flush=True)
+            "config": {"rate_hz": rate, "duration_s": duration, "seed": seed, "rooms": 8, "shapes": len(shapes),
+                       "slots": slots, "hbm_budget_gb": 150, "light_jitter_deg": 5, "orbit_step_deg": 0.5},
+            "clocks": clocks}
+
+
+def run_serve(args, rank, world, local_rank):
+    r = measure_serve(local_rank, args.slots, args.rate, args.duration, args.seed)
+    if rank == 0:
+        cfg = r.pop("config")
+        print(json.dumps({
+            "metric": "served GI frames/s", "value": r["served"]["frames_per_s"], "unit": "frames/s",
+            "n_gpus": world, "steps": r["served"]["requests"], "warmup": 1, "higher_is_better": True,
+            "dtype": "f32 / fp16-bf16 mixed", "data": "synthetic (seeded procedural rooms, generated on the GPU)",
+            "config": {"workload": "c5_served_poisson", **cfg}, **r}), flush=True)
 
 
 def main():
