@@ -16,6 +16,8 @@
 // Accumulation order is ascending VPL index for every pixel, so results are deterministic.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "batch_items.cuh"
 #include "gi_device.cuh"
 #include "kernels.h"
@@ -247,12 +249,293 @@ struct FgSmem {
     __align__(8) uint64_t bar;
 };
 
-// One T x T tile of interleave class c with T*T/2 threads. The caller initialises S.bar once and
-// keeps `parity` across calls. Returns false (block-uniform) when the VPL staging wait timed out.
-// kClusters: compile the clustered-culling path (cull == 2), which batched views do not use.
+// Per-VPL data of the gathering from its staged record: the packed rows (see VplPk) and the
+// decoded position, normal and flux. vid is the VPL's index in the VPL buffer.
+template <bool kReduced>
+__device__ __forceinline__ void derive_vpl(const unsigned char* rec, const int vid, const FgArgs& a, const float hs,
+                                           VplPk& R, v3& p, v3& n, v3& f) {
+    decode_vpl<kReduced>(rec, p, n, f);
+    // lookAtRH rows (ism_utils.glsl:5-13) with the fast normalisation
+    const v3 s = normalize_fast(cross(n, mk(0.0f, 1.0f, 0.01f)));
+    const v3 u = cross(s, n);
+    // int(ismIndex / gx) of small non-negative integers equals the integer quotient
+    const int ism = vid - a.ism_index_offset;
+    const int ty = ism / a.gx;
+    const int tx = ism - ty * a.gx;
+    // the lookAtRH rows are scaled by half the ISM size (the texel offset from the ISM centre is
+    // hs * s.d / (1 + a1)); border = 1 marks an ISM on or beyond the atlas border (a scaled layout
+    // gives VPLs outside the range ISM indices off the grid), the only ones whose texel can leave
+    // the atlas: |x| < 1 for every pair that reaches the lookup
+    const bool border = tx <= 0 || ty <= 0 || tx >= a.gx - 1 || ty >= a.gy - 1;
+    R.r[0] = make_ulonglong2(pk(p.x).v, pk(p.y).v);
+    R.r[1] = make_ulonglong2(pk(p.z).v, pk(n.x).v);
+    R.r[2] = make_ulonglong2(pk(n.y).v, pk(n.z).v);
+    R.r[3] = make_ulonglong2(pk(s.x * hs).v, pk(s.y * hs).v);
+    R.r[4] = make_ulonglong2(pk(s.z * hs).v, pk(u.x * hs).v);
+    R.r[5] = make_ulonglong2(pk(u.y * hs).v, pk(u.z * hs).v);
+    R.r[6] = make_ulonglong2(pk(float(tx * a.ism_size) + hs).v, pk(float(ty * a.ism_size) + hs).v);
+    R.r[7] = make_ulonglong2(pk(f.x).v, pk(f.y).v);
+    R.r[8] = make_ulonglong2(pk(f.z).v, pk(border ? 1.0f : 0.0f).v);
+}
+
+// Squared influence radius of a VPL with flux f: every pixel farther than r = (max flux /
+// cutoff)^(1/4) receives flux * cos / d^4 below the cutoff from it (+Inf without a cutoff).
+__device__ __forceinline__ float vpl_influence_r2(const v3 f, const float cutoff) {
+    if (!(cutoff > 0.f)) return __int_as_float(0x7f800000);
+    const float fl = fmaxf(f.x, fmaxf(f.y, f.z));
+    const float r = sqrtf(sqrtf(fl / cutoff));
+    return r * r;
+}
+
+// Per-tile culling of one VPL against the box [bmin, bmax] of the tile's world positions: its
+// front half-space against the box corner farthest along its normal, then the box's squared
+// distance against the influence radius r2 (vpl_influence_r2).
+__device__ __forceinline__ bool vpl_keep(const v3 p, const v3 n, const float r2, const v3 bmin, const v3 bmax) {
+    const v3 sup = mk(n.x > 0.f ? bmax.x : bmin.x, n.y > 0.f ? bmax.y : bmin.y, n.z > 0.f ? bmax.z : bmin.z);
+    if (dot(n, sup - p) < -1e-3f) return false;
+    const v3 q = mk(fminf(fmaxf(p.x, bmin.x), bmax.x), fminf(fmaxf(p.y, bmin.y), bmax.y),
+                    fminf(fmaxf(p.z, bmin.z), bmax.z));
+    const v3 dq = q - p;
+    return !(dot(dq, dq) > r2);
+}
+
+// Pixel (x, y) of the G-buffer: window depth and decoded octahedral normal (a pixel outside the
+// image gets depth 0.5 and normal +z, finite dummies).
+template <bool kNormalF16>
+__device__ __forceinline__ void fg_pixel_setup(const FgArgs& a, const int x, const int y, const bool valid, float& d,
+                                               v3& fn) {
+    d = 0.5f;
+    fn = mk(0.f, 0.f, 1.f);
+    if (!valid) return;
+    const size_t pix = (size_t)y * a.width + x;
+    d = __ldg(a.depth + pix);
+    float ex, ey;
+    if (kNormalF16) {
+        const __half2 h = reinterpret_cast<const __half2*>(a.normal)[pix];
+        ex = __low2float(h);
+        ey = __high2float(h);
+    } else {
+        const float2 e = reinterpret_cast<const float2*>(a.normal)[pix];
+        ex = e.x;
+        ey = e.y;
+    }
+    fn = oct_decode(ex, ey);
+}
+
+// World-space bounding box of a block's pixels (both of each thread's, the valid ones), through
+// `box` (6 x NW floats of shared memory) and one barrier.
+template <int NW>
+__device__ __forceinline__ void fg_tile_box(const v3 w0, const v3 w1, const bool v0, const bool v1,
+                                            float (&box)[6][NW], v3& bmin, v3& bmax) {
+    const float inf = __int_as_float(0x7f800000);
+    float b[6] = {fminf(v0 ? w0.x : inf, v1 ? w1.x : inf),   fminf(v0 ? w0.y : inf, v1 ? w1.y : inf),
+                  fminf(v0 ? w0.z : inf, v1 ? w1.z : inf),   fminf(v0 ? -w0.x : inf, v1 ? -w1.x : inf),
+                  fminf(v0 ? -w0.y : inf, v1 ? -w1.y : inf), fminf(v0 ? -w0.z : inf, v1 ? -w1.z : inf)};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) b[k] = fminf(b[k], __shfl_xor_sync(0xffffffffu, b[k], o));
+    }
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) box[k][threadIdx.x >> 5] = b[k];
+    __syncthreads();
+    float r[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        r[k] = box[k][0];
+        for (int w = 1; w < NW; ++w) r[k] = fminf(r[k], box[k][w]);
+    }
+    bmin = mk(r[0], r[1], r[2]);
+    bmax = mk(-r[3], -r[4], -r[5]);
+}
+
 // VPLs a thread evaluates per gather iteration (for both its pixels): 2 measured best at 1080p,
 // 0.0942 ms against 0.0953 with 1 and 0.1009 with 3 (64 bytes of spill at the 64-register budget)
 constexpr int kVpls = 2;
+
+// One thread's two pixels of a gathering tile: their world positions and normals as packed pairs,
+// the accumulated radiance, and the evaluation of one VPL for both (final_gathering.comp:97-130).
+template <bool kAtlasF16, bool kClusters>
+struct GatherPair {
+    f2 fwx, fwy, fwz, fnx, fny, fnz;
+    f2 accx, accy, accz;
+    bool v0, v1;
+    const uint32_t *cl0, *cl1;
+    const void* atlas;
+    float clampv;
+    bool shadow, clustered;
+    int aw, ah;
+    f2 izf;
+
+    __device__ __forceinline__ void init(const FgArgs& a, const v3 w0, const v3 n0, const v3 w1, const v3 n1,
+                                         const bool pv0, const bool pv1, const uint32_t* c0, const uint32_t* c1) {
+        fwx = pk(w0.x, w1.x);
+        fwy = pk(w0.y, w1.y);
+        fwz = pk(w0.z, w1.z);
+        fnx = pk(n0.x, n1.x);
+        fny = pk(n0.y, n1.y);
+        fnz = pk(n0.z, n1.z);
+        accx = accy = accz = pk(0.f);
+        v0 = pv0;
+        v1 = pv1;
+        cl0 = c0;
+        cl1 = c1;
+        atlas = a.atlas;
+        clampv = a.clamp_value;
+        shadow = a.shadowing != 0;
+        clustered = kClusters && a.cull == 2;
+        aw = a.atlas_w;
+        ah = a.atlas_h;
+        izf = pk(1.0f / a.z_far);
+    }
+
+    // One VPL against both pixels: G the clamped geometry term per pixel (0 for a pixel the pair
+    // does not reach), the ISM texel index per pixel and the normalised distance vz.
+    __device__ __forceinline__ bool prepare(const VplPk& R, const int vid, f2& G, f2& vz, uint32_t& t0, uint32_t& t1,
+                                            bool& ok0, bool& ok1) const {
+        ok0 = v0;
+        ok1 = v1;
+        if (kClusters && clustered) {  // outside the pixel's cluster list
+            if (cl0) ok0 = ok0 && ((__ldg(cl0 + (vid >> 5)) >> (vid & 31)) & 1u);
+            if (cl1) ok1 = ok1 && ((__ldg(cl1 + (vid >> 5)) >> (vid & 31)) & 1u);
+        }
+        const ulonglong2 R0 = R.r[0], R1 = R.r[1], R2 = R.r[2];
+        const f2 dx = fwx - f2{R0.x}, dy = fwy - f2{R0.y}, dz = fwz - f2{R1.x};
+        // the cosine terms have the signs of these dot products with the unnormalised direction:
+        // most pairs end here, before the square root (max(0, a1) * max(0, a2) > 0 needs a1 > 0 and
+        // a2 > 0)
+        const f2 e1 = fma2(f2{R1.y}, dx, fma2(f2{R2.x}, dy, f2{R2.y} * dz));
+        const f2 e2 = fma2(fnx, dx, fma2(fny, dy, fnz * dz));
+        float e1a, e1b, e2a, e2b;
+        split(e1, e1a, e1b);
+        split(e2, e2a, e2b);
+        ok0 = ok0 && e1a > 0.f && e2a < 0.f;
+        ok1 = ok1 && e1b > 0.f && e2b < 0.f;
+        if (!(ok0 || ok1)) return false;
+        const f2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
+        float d2a, d2b;
+        split(d2, d2a, d2b);
+        const f2 inv = pk(rsqrtf(d2a), rsqrtf(d2b));
+        const f2 a1 = e1 * inv, a2n = e2 * inv;  // a2 = -a2n
+        const f2 i2 = inv * inv;
+        float ga, gb;  // -(a1 * a2) / d^4
+        split((a1 * a2n) * (i2 * i2), ga, gb);
+        G = pk(ok0 ? fminf(-ga, clampv) : 0.f, ok1 ? fminf(-gb, clampv) : 0.f);
+        if (shadow) {
+            const ulonglong2 R3 = R.r[3], R4 = R.r[4], R5 = R.r[5], R6 = R.r[6];
+            float qa, qb;
+            split(a1 + pk(1.0f), qa, qb);
+            const f2 rz = inv * pk(rcp_approx(qa), rcp_approx(qb));
+            const f2 sx = fma2(fma2(f2{R3.x}, dx, fma2(f2{R3.y}, dy, f2{R4.x} * dz)), rz, f2{R6.x});
+            const f2 sy = fma2(fma2(f2{R4.y}, dx, fma2(f2{R5.x}, dy, f2{R5.y} * dz)), rz, f2{R6.y});
+            float sxa, sxb, sya, syb;
+            split(sx, sxa, sxb);
+            split(sy, sya, syb);
+            int ix0 = __float2int_rd(sxa), ix1 = __float2int_rd(sxb);
+            int iy0 = __float2int_rd(sya), iy1 = __float2int_rd(syb);
+            float bf, unused;
+            split(f2{R.r[8].y}, bf, unused);
+            if (bf != 0.f) {  // GL_REPEAT, for border ISMs only (uniform over the block)
+                ix0 %= aw;
+                if (ix0 < 0) ix0 += aw;
+                ix1 %= aw;
+                if (ix1 < 0) ix1 += aw;
+                iy0 %= ah;
+                if (iy0 < 0) iy0 += ah;
+                iy1 %= ah;
+                if (iy1 < 0) iy1 += ah;
+            }
+            t0 = ok0 ? (uint32_t)iy0 * (uint32_t)aw + (uint32_t)ix0 : 0u;
+            t1 = ok1 ? (uint32_t)iy1 * (uint32_t)aw + (uint32_t)ix1 : 0u;
+            vz = (d2 * inv) * izf;
+        }
+        return true;
+    }
+
+    __device__ __forceinline__ float occluder(const uint32_t t) const {
+        return kAtlasF16 ? __half2float(__ldg(reinterpret_cast<const __half*>(atlas) + t))
+                         : __ldg(reinterpret_cast<const float*>(atlas) + t);
+    }
+
+    // acc += flux * G * smoothstep(0.98, 1, 1 - (vz - occ)) for both pixels
+    __device__ __forceinline__ void accumulate(const VplPk& R, const f2 G, const f2 vz, const float o0, const float o1) {
+        f2 w = G;
+        if (shadow) {
+            const f2 sv0 = pk(1.0f) - (vz - pk(o0, o1));
+            float sa, sb;
+            split(fma2(sv0, pk(50.0f), pk(-49.0f)), sa, sb);
+            const f2 tt = pk(__saturatef(sa), __saturatef(sb));
+            w = G * ((tt * tt) * fma2(tt, pk(-2.0f), pk(3.0f)));
+        }
+        const ulonglong2 R7 = R.r[7], R8 = R.r[8];
+        accx = fma2(f2{R7.x}, w, accx);
+        accy = fma2(f2{R7.y}, w, accy);
+        accz = fma2(f2{R8.x}, w, accz);
+    }
+
+    // The nk VPLs whose indices into V (ascending) `next()` yields, kVpls per iteration so that
+    // their texel loads are in flight together; each pixel accumulates in ascending order. vid0:
+    // the VPL index of V[0].
+    template <class Next>
+    __device__ __forceinline__ void gather(const VplPk* V, const int vid0, const int nk, Next next) {
+        int q = 0;
+        for (; q + kVpls - 1 < nk; q += kVpls) {
+            int kk[kVpls];
+            f2 G[kVpls], vz[kVpls];
+            uint32_t t[kVpls][2];
+            bool ok[kVpls][2], any[kVpls];
+#pragma unroll
+            for (int j = 0; j < kVpls; ++j) {
+                kk[j] = next();
+                G[j] = pk(0.f);
+                vz[j] = pk(0.f);
+                t[j][0] = t[j][1] = 0u;
+                any[j] = prepare(V[kk[j]], vid0 + kk[j], G[j], vz[j], t[j][0], t[j][1], ok[j][0], ok[j][1]);
+            }
+            float o[kVpls][2];
+#pragma unroll
+            for (int j = 0; j < kVpls; ++j) {
+                o[j][0] = (any[j] && shadow && ok[j][0]) ? occluder(t[j][0]) : 0.f;
+                o[j][1] = (any[j] && shadow && ok[j][1]) ? occluder(t[j][1]) : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < kVpls; ++j)
+                if (any[j]) accumulate(V[kk[j]], G[j], vz[j], o[j][0], o[j][1]);
+        }
+        for (; q < nk; ++q) {
+            const int k = next();
+            f2 G = pk(0.f), vz = pk(0.f);
+            uint32_t t0 = 0u, t1 = 0u;
+            bool ok0, ok1;
+            if (prepare(V[k], vid0 + k, G, vz, t0, t1, ok0, ok1))
+                accumulate(V[k], G, vz, (shadow && ok0) ? occluder(t0) : 0.f, (shadow && ok1) ? occluder(t1) : 0.f);
+        }
+    }
+
+    __device__ __forceinline__ void store(const FgArgs& a, const int y, const int x0, const int x1) const {
+        float ax0, ax1, ay0, ay1, az0, az1;
+        split(accx, ax0, ax1);
+        split(accy, ay0, ay1);
+        split(accz, az0, az1);
+        if (v0) {
+            const size_t pix = (size_t)y * a.width + x0;
+            a.out[3 * pix + 0] = ax0 * a.gi_scale;
+            a.out[3 * pix + 1] = ay0 * a.gi_scale;
+            a.out[3 * pix + 2] = az0 * a.gi_scale;
+        }
+        if (v1) {
+            const size_t pix = (size_t)y * a.width + x1;
+            a.out[3 * pix + 0] = ax1 * a.gi_scale;
+            a.out[3 * pix + 1] = ay1 * a.gi_scale;
+            a.out[3 * pix + 2] = az1 * a.gi_scale;
+        }
+    }
+};
+
+// One T x T tile of interleave class c with T*T/2 threads. The caller initialises S.bar once and
+// keeps `parity` across calls. Returns false (block-uniform) when the VPL staging wait timed out.
+// kClusters: compile the clustered-culling path (cull == 2), which batched views do not use.
 
 template <int T, bool kReduced, bool kAtlasF16, bool kNormalF16, bool kClusters = true>
 __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const int c, FgSmem<T>& S,
@@ -283,24 +566,10 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     // ---- pixel setup: world position from depth (final_gathering.comp:70-76, evaluated with
     // compensated arithmetic) and the octahedral normal ----
     auto setup = [&](int x, bool valid, float& d, v3& fn, const uint32_t*& cl_row) {
-        d = 0.5f;
-        fn = mk(0.f, 0.f, 1.f);
+        fg_pixel_setup<kNormalF16>(a, x, y, valid, d, fn);
         cl_row = nullptr;
-        if (!valid) return;
-        const size_t pix = (size_t)y * a.width + x;
-        d = __ldg(a.depth + pix);
-        float ex, ey;
-        if (kNormalF16) {
-            const __half2 h = reinterpret_cast<const __half2*>(a.normal)[pix];
-            ex = __low2float(h);
-            ey = __high2float(h);
-        } else {
-            const float2 e = reinterpret_cast<const float2*>(a.normal)[pix];
-            ex = e.x;
-            ey = e.y;
-        }
-        fn = oct_decode(ex, ey);
-        if (kClusters && a.cull == 2) {
+        if (valid && kClusters && a.cull == 2) {
+            const size_t pix = (size_t)y * a.width + x;
             const int cluster = ((y / kClusterPixels) * a.cl_tiles_x + x / kClusterPixels) * kClusterSlices + a.cl_slice[pix];
             cl_row = a.cl_masks + (size_t)cluster * a.cl_words;
         }
@@ -317,37 +586,13 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
 
     // ---- per-tile bounds for culling ----
     v3 bmin = mk(0.f, 0.f, 0.f), bmax = mk(0.f, 0.f, 0.f);
-    if (a.cull == 1) {
-        const float inf = __int_as_float(0x7f800000);
-        float b[6] = {fminf(v0 ? w0.x : inf, v1 ? w1.x : inf),   fminf(v0 ? w0.y : inf, v1 ? w1.y : inf),
-                      fminf(v0 ? w0.z : inf, v1 ? w1.z : inf),   fminf(v0 ? -w0.x : inf, v1 ? -w1.x : inf),
-                      fminf(v0 ? -w0.y : inf, v1 ? -w1.y : inf), fminf(v0 ? -w0.z : inf, v1 ? -w1.z : inf)};
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) b[k] = fminf(b[k], __shfl_xor_sync(0xffffffffu, b[k], o));
-        }
-        if ((tid & 31) == 0)
-#pragma unroll
-            for (int k = 0; k < 6; ++k) S.box[k][tid >> 5] = b[k];
-        __syncthreads();
-        float r[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            r[k] = S.box[k][0];
-            for (int w = 1; w < NW; ++w) r[k] = fminf(r[k], S.box[k][w]);
-        }
-        bmin = mk(r[0], r[1], r[2]);
-        bmax = mk(-r[3], -r[4], -r[5]);
-    }
+    if (a.cull == 1) fg_tile_box<NW>(w0, w1, v0, v1, S.box, bmin, bmax);
 
     __syncthreads();  // the previous tile's use of S is over
 
     const float hs = float(a.ism_size) * 0.5f;
-    const float inv_zfar = 1.0f / a.z_far;
-    const f2 fwx = pk(w0.x, w1.x), fwy = pk(w0.y, w1.y), fwz = pk(w0.z, w1.z);
-    const f2 fnx = pk(n0.x, n1.x), fny = pk(n0.y, n1.y), fnz = pk(n0.z, n1.z);
-    f2 accx = pk(0.f), accy = pk(0.f), accz = pk(0.f);
+    GatherPair<kAtlasF16, kClusters> gp;
+    gp.init(a, w0, n0, w1, n1, v0, v1, cl0, cl1);
 
     for (int base = 0; base < a.per_class; base += kChunk) {
         const int cnt = min(kChunk, a.per_class - base);
@@ -379,44 +624,8 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         // derive per-VPL data (every value stored twice) and the cull flag
         for (int k = tid; k < cnt; k += NT) {
             v3 p, n, f;
-            decode_vpl<kReduced>(S.raw + (size_t)k * kRec, p, n, f);
-            // lookAtRH rows (ism_utils.glsl:5-13) with the fast normalisation
-            const v3 s = normalize_fast(cross(n, mk(0.0f, 1.0f, 0.01f)));
-            const v3 u = cross(s, n);
-            const int vid = vbase + base + k;
-            // int(ismIndex / gx) of small non-negative integers equals the integer quotient
-            const int ism = vid - a.ism_index_offset;
-            const int ty = ism / a.gx;
-            const int tx = ism - ty * a.gx;
-            // the lookAtRH rows are scaled by half the ISM size (the texel offset from the ISM
-            // centre is hs * s.d / (1 + a1)); border = 1 marks an ISM on or beyond the atlas border
-            // (a scaled layout gives VPLs outside the range ISM indices off the grid), the only
-            // ones whose texel can leave the atlas: |x| < 1 for every pair that reaches the lookup
-            const bool border = tx <= 0 || ty <= 0 || tx >= a.gx - 1 || ty >= a.gy - 1;
-            VplPk& R = S.v[k];
-            R.r[0] = make_ulonglong2(pk(p.x).v, pk(p.y).v);
-            R.r[1] = make_ulonglong2(pk(p.z).v, pk(n.x).v);
-            R.r[2] = make_ulonglong2(pk(n.y).v, pk(n.z).v);
-            R.r[3] = make_ulonglong2(pk(s.x * hs).v, pk(s.y * hs).v);
-            R.r[4] = make_ulonglong2(pk(s.z * hs).v, pk(u.x * hs).v);
-            R.r[5] = make_ulonglong2(pk(u.y * hs).v, pk(u.z * hs).v);
-            R.r[6] = make_ulonglong2(pk(float(tx * a.ism_size) + hs).v, pk(float(ty * a.ism_size) + hs).v);
-            R.r[7] = make_ulonglong2(pk(f.x).v, pk(f.y).v);
-            R.r[8] = make_ulonglong2(pk(f.z).v, pk(border ? 1.0f : 0.0f).v);
-            bool keep = true;
-            if (a.cull == 1) {
-                // front half-space of the VPL against the box corner farthest along its normal
-                const v3 sup = mk(n.x > 0.f ? bmax.x : bmin.x, n.y > 0.f ? bmax.y : bmin.y, n.z > 0.f ? bmax.z : bmin.z);
-                if (dot(n, sup - p) < -1e-3f) keep = false;
-                if (keep && a.influence_cutoff > 0.f) {
-                    const float fl = fmaxf(f.x, fmaxf(f.y, f.z));
-                    const float r = sqrtf(sqrtf(fl / a.influence_cutoff));
-                    const v3 q = mk(fminf(fmaxf(p.x, bmin.x), bmax.x), fminf(fmaxf(p.y, bmin.y), bmax.y),
-                                    fminf(fmaxf(p.z, bmin.z), bmax.z));
-                    const v3 dq = q - p;
-                    if (dot(dq, dq) > r * r) keep = false;
-                }
-            }
+            derive_vpl<kReduced>(S.raw + (size_t)k * kRec, vbase + base + k, a, hs, S.v[k], p, n, f);
+            const bool keep = a.cull != 1 || vpl_keep(p, n, vpl_influence_r2(f, a.influence_cutoff), bmin, bmax);
             S.flag[k] = keep ? 1 : 0;
         }
         __syncthreads();
@@ -435,148 +644,13 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         __syncthreads();
 
         // ---- gather over the kept list (final_gathering.comp:97-130), two pixels per thread ----
-        const int nk = S.n;
         if (v0 || v1) {
-            const float* atlas32 = reinterpret_cast<const float*>(a.atlas);
-            const __half* atlas16 = reinterpret_cast<const __half*>(a.atlas);
-            const float clampv = a.clamp_value;
-            const bool shadow = a.shadowing != 0;
-            const int aw = a.atlas_w, ah = a.atlas_h;
-            const f2 one = pk(1.0f), izf = pk(inv_zfar);
-            // One VPL against both pixels: G the clamped geometry term per pixel (0 for a pixel the
-            // pair does not reach), the ISM texel index per pixel and the normalised distance vz.
-            auto prepare = [&](int k, f2& G, f2& vz, uint32_t& t0, uint32_t& t1, bool& ok0, bool& ok1) -> bool {
-                ok0 = v0;
-                ok1 = v1;
-                if (kClusters && a.cull == 2) {  // outside the pixel's cluster list
-                    const int vid = vbase + base + k;
-                    if (cl0) ok0 = ok0 && ((__ldg(cl0 + (vid >> 5)) >> (vid & 31)) & 1u);
-                    if (cl1) ok1 = ok1 && ((__ldg(cl1 + (vid >> 5)) >> (vid & 31)) & 1u);
-                }
-                const VplPk& R = S.v[k];
-                const ulonglong2 R0 = R.r[0], R1 = R.r[1], R2 = R.r[2];
-                const f2 dx = fwx - f2{R0.x}, dy = fwy - f2{R0.y}, dz = fwz - f2{R1.x};
-                // the cosine terms have the signs of these dot products with the unnormalised
-                // direction: most pairs end here, before the square root (max(0, a1) *
-                // max(0, a2) > 0 needs a1 > 0 and a2 > 0)
-                const f2 e1 = fma2(f2{R1.y}, dx, fma2(f2{R2.x}, dy, f2{R2.y} * dz));
-                const f2 e2 = fma2(fnx, dx, fma2(fny, dy, fnz * dz));
-                float e1a, e1b, e2a, e2b;
-                split(e1, e1a, e1b);
-                split(e2, e2a, e2b);
-                ok0 = ok0 && e1a > 0.f && e2a < 0.f;
-                ok1 = ok1 && e1b > 0.f && e2b < 0.f;
-                if (!(ok0 || ok1)) return false;
-                const f2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
-                float d2a, d2b;
-                split(d2, d2a, d2b);
-                const f2 inv = pk(rsqrtf(d2a), rsqrtf(d2b));
-                const f2 a1 = e1 * inv, a2n = e2 * inv;  // a2 = -a2n
-                const f2 i2 = inv * inv;
-                float ga, gb;  // -(a1 * a2) / d^4
-                split((a1 * a2n) * (i2 * i2), ga, gb);
-                G = pk(ok0 ? fminf(-ga, clampv) : 0.f, ok1 ? fminf(-gb, clampv) : 0.f);
-                if (shadow) {
-                    const ulonglong2 R3 = R.r[3], R4 = R.r[4], R5 = R.r[5], R6 = R.r[6];
-                    float qa, qb;
-                    split(a1 + one, qa, qb);
-                    const f2 rz = inv * pk(rcp_approx(qa), rcp_approx(qb));
-                    const f2 sx = fma2(fma2(f2{R3.x}, dx, fma2(f2{R3.y}, dy, f2{R4.x} * dz)), rz, f2{R6.x});
-                    const f2 sy = fma2(fma2(f2{R4.y}, dx, fma2(f2{R5.x}, dy, f2{R5.y} * dz)), rz, f2{R6.y});
-                    float sxa, sxb, sya, syb;
-                    split(sx, sxa, sxb);
-                    split(sy, sya, syb);
-                    int ix0 = __float2int_rd(sxa), ix1 = __float2int_rd(sxb);
-                    int iy0 = __float2int_rd(sya), iy1 = __float2int_rd(syb);
-                    float bf, unused;
-                    split(f2{R.r[8].y}, bf, unused);
-                    if (bf != 0.f) {  // GL_REPEAT, for border ISMs only (uniform over the block)
-                        ix0 %= aw;
-                        if (ix0 < 0) ix0 += aw;
-                        ix1 %= aw;
-                        if (ix1 < 0) ix1 += aw;
-                        iy0 %= ah;
-                        if (iy0 < 0) iy0 += ah;
-                        iy1 %= ah;
-                        if (iy1 < 0) iy1 += ah;
-                    }
-                    t0 = ok0 ? (uint32_t)iy0 * (uint32_t)aw + (uint32_t)ix0 : 0u;
-                    t1 = ok1 ? (uint32_t)iy1 * (uint32_t)aw + (uint32_t)ix1 : 0u;
-                    vz = (d2 * inv) * izf;
-                }
-                return true;
-            };
-            auto occluder = [&](uint32_t t) -> float {
-                return kAtlasF16 ? __half2float(__ldg(atlas16 + t)) : __ldg(atlas32 + t);
-            };
-            // acc += flux * G * smoothstep(0.98, 1, 1 - (vz - occ)) for both pixels
-            auto accumulate = [&](int k, f2 G, f2 vz, float o0, float o1) {
-                f2 w = G;
-                if (shadow) {
-                    const f2 sv0 = one - (vz - pk(o0, o1));
-                    float sa, sb;
-                    split(fma2(sv0, pk(50.0f), pk(-49.0f)), sa, sb);
-                    const f2 tt = pk(__saturatef(sa), __saturatef(sb));
-                    w = G * ((tt * tt) * fma2(tt, pk(-2.0f), pk(3.0f)));
-                }
-                const ulonglong2 R7 = S.v[k].r[7], R8 = S.v[k].r[8];
-                accx = fma2(f2{R7.x}, w, accx);
-                accy = fma2(f2{R7.y}, w, accy);
-                accz = fma2(f2{R8.x}, w, accz);
-            };
-            // kVpls VPLs per iteration, so that their 2 kVpls texel loads are in flight together;
-            // each pixel still accumulates in ascending list order
             int q = 0;
-            for (; q + kVpls - 1 < nk; q += kVpls) {
-                int kk[kVpls];
-                f2 G[kVpls], vz[kVpls];
-                uint32_t t[kVpls][2];
-                bool ok[kVpls][2], any[kVpls];
-#pragma unroll
-                for (int j = 0; j < kVpls; ++j) {
-                    kk[j] = S.list[q + j];
-                    G[j] = pk(0.f);
-                    vz[j] = pk(0.f);
-                    t[j][0] = t[j][1] = 0u;
-                    any[j] = prepare(kk[j], G[j], vz[j], t[j][0], t[j][1], ok[j][0], ok[j][1]);
-                }
-                float o[kVpls][2];
-#pragma unroll
-                for (int j = 0; j < kVpls; ++j) {
-                    o[j][0] = (any[j] && shadow && ok[j][0]) ? occluder(t[j][0]) : 0.f;
-                    o[j][1] = (any[j] && shadow && ok[j][1]) ? occluder(t[j][1]) : 0.f;
-                }
-#pragma unroll
-                for (int j = 0; j < kVpls; ++j)
-                    if (any[j]) accumulate(kk[j], G[j], vz[j], o[j][0], o[j][1]);
-            }
-            for (; q < nk; ++q) {
-                const int k = S.list[q];
-                f2 G = pk(0.f), vz = pk(0.f);
-                uint32_t t0 = 0u, t1 = 0u;
-                bool ok0, ok1;
-                if (prepare(k, G, vz, t0, t1, ok0, ok1))
-                    accumulate(k, G, vz, (shadow && ok0) ? occluder(t0) : 0.f, (shadow && ok1) ? occluder(t1) : 0.f);
-            }
+            gp.gather(S.v, vbase + base, S.n, [&]() { return S.list[q++]; });
         }
         __syncthreads();
     }
-    float ax0, ax1, ay0, ay1, az0, az1;
-    split(accx, ax0, ax1);
-    split(accy, ay0, ay1);
-    split(accz, az0, az1);
-    if (v0) {
-        const size_t pix = (size_t)y * a.width + x0;
-        a.out[3 * pix + 0] = ax0 * a.gi_scale;
-        a.out[3 * pix + 1] = ay0 * a.gi_scale;
-        a.out[3 * pix + 2] = az0 * a.gi_scale;
-    }
-    if (v1) {
-        const size_t pix = (size_t)y * a.width + x1;
-        a.out[3 * pix + 0] = ax1 * a.gi_scale;
-        a.out[3 * pix + 1] = ay1 * a.gi_scale;
-        a.out[3 * pix + 2] = az1 * a.gi_scale;
-    }
+    gp.store(a, y, x0, x1);
     return true;
 }
 
@@ -589,14 +663,155 @@ __global__ void __launch_bounds__(T* T / 2, T == 16 ? 8 : 32) fg_kernel(FgArgs a
     fg_tile<T, kReduced, kAtlasF16, kNormalF16>(a, a.tile0 + blockIdx.x, blockIdx.y, S, parity);
 }
 
+// ---- class-persistent gathering ----------------------------------------------------------------
+// Block (b, c) stages and derives interleave class c's VPL slice once (one bulk copy, one bounded
+// wait), then gathers tiles b, b + gridDim.x, ... of the launch's tile range for that class. Per
+// tile it reduces the tile's world-space box (one barrier: the box slots alternate between tiles),
+// and every warp culls the whole slice against it itself, one VPL a lane, keeping the survivors
+// as ballot masks: no per-tile staging, derivation or list compaction. Used for 16 x 16 tiles when
+// a class slice fits one staging chunk (N / I^2 <= 64) and culling is off or per tile; the tile
+// arithmetic (derive_vpl, vpl_keep, GatherPair) is fg_tile's, so results are the same bit for bit.
+constexpr int kClassMaxVpls = 64;
+constexpr int kFgClassBlocksPerSm = 32;  // C2: 0.0844 ms; 8: 0.0923, 16: 0.0891; per-tile kernel 0.0918
+
+struct FgClassSmem {
+    __align__(128) unsigned char raw[kClassMaxVpls * 48];
+    VplPk v[kClassMaxVpls];
+    float4 cp[kClassMaxVpls], cn[kClassMaxVpls];  // (position, squared influence radius), normal
+    float box[2][6][4];
+    __align__(8) uint64_t bar;
+};
+
+template <bool kReduced, bool kAtlasF16, bool kNormalF16>
+__global__ void __launch_bounds__(128, 8) fg_class_kernel(FgArgs a, int tile_begin, int n_tiles) {
+    constexpr int T = 16, NT = 128, HT = 8, NW = 4, kRec = kReduced ? 24 : 48;
+    __shared__ FgClassSmem S;
+    const int tid = threadIdx.x;
+    const int c = blockIdx.y;
+    const int I = a.interleave, cx = c % I, cy = c / I;
+    const int vbase = c * a.per_class, cnt = a.per_class;
+    const float hs = float(a.ism_size) * 0.5f;
+    const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
+    const size_t bytes = (size_t)cnt * kRec;
+    const bool use_tma = ((size_t)vbase * kRec) % 16 == 0 && bytes % 16 == 0;
+    if (tid == 0) {
+        mbar_init(&S.bar, 1);
+        if (use_tma) {
+            mbar_expect_tx(&S.bar, (uint32_t)bytes + a.test_extra_tx);
+            tma_bulk_g2s(S.raw, src + (size_t)vbase * kRec, (uint32_t)bytes, &S.bar);
+        }
+    }
+    if (!use_tma)
+        for (size_t k = tid * 4; k < bytes; k += NT * 4)
+            *reinterpret_cast<uint32_t*>(S.raw + k) = __ldg(reinterpret_cast<const uint32_t*>(src + (size_t)vbase * kRec + k));
+    __syncthreads();
+    if (use_tma) {
+        const long long limit = a.wait_cycles > 0 ? a.wait_cycles : 1ll << 31;
+        if (!__syncthreads_and(mbar_wait(&S.bar, 0, limit))) {  // block-uniform: flag, let the copy land, leave
+            if (tid == 0) {
+                atomicOr(a.status, kStatusTmaTimeout);
+                if (a.test_extra_tx) mbar_complete_tx(&S.bar, a.test_extra_tx);
+                mbar_wait(&S.bar, 0, 1ll << 31);
+            }
+            return;
+        }
+    }
+    for (int k = tid; k < cnt; k += NT) {
+        v3 p, n, f;
+        derive_vpl<kReduced>(S.raw + (size_t)k * kRec, vbase + k, a, hs, S.v[k], p, n, f);
+        S.cp[k] = make_float4(p.x, p.y, p.z, vpl_influence_r2(f, a.influence_cutoff));
+        S.cn[k] = make_float4(n.x, n.y, n.z, 0.f);
+    }
+    __syncthreads();
+
+    const int sw = (a.width + I - 1) / I, ntx = (sw + T - 1) / T;
+    const int lane = tid & 31;
+    int it = 0;
+    for (int tile = tile_begin + blockIdx.x; tile < tile_begin + n_tiles; tile += gridDim.x, ++it) {
+        const int tix = tile % ntx, tiy = tile / ntx;
+        const int y = (tiy * T + tid / HT) * I + cy;
+        const int x0 = (tix * T + 2 * (tid % HT)) * I + cx, x1 = x0 + I;
+        const bool v0 = x0 < a.width && y < a.height, v1 = x1 < a.width && y < a.height;
+        v3 w0, n0, w1, n1;
+        float d0, d1;
+        fg_pixel_setup<kNormalF16>(a, x0, y, v0, d0, n0);
+        fg_pixel_setup<kNormalF16>(a, x1, y, v1, d1, n1);
+        reconstruct_world2(a.inv_vp, x0, x1, y, a.width, a.height, a.inv_w, a.inv_h, d0, d1, pk(a.z_far * 0.0f), w0, w1);
+        if (!v0) w0 = mk(0.f, 0.f, 0.f);
+        if (!v1) w1 = mk(0.f, 0.f, 0.f);
+        unsigned m0 = 0xFFFFFFFFu, m1 = 0xFFFFFFFFu;
+        if (a.cull == 1) {
+            v3 bmin, bmax;
+            fg_tile_box<NW>(w0, w1, v0, v1, S.box[it & 1], bmin, bmax);
+            auto keep = [&](const int k) {
+                if (k >= cnt) return false;
+                const float4 cp = S.cp[k], cn = S.cn[k];
+                return vpl_keep(mk(cp.x, cp.y, cp.z), mk(cn.x, cn.y, cn.z), cp.w, bmin, bmax);
+            };
+            m0 = __ballot_sync(0xffffffffu, keep(lane));
+            m1 = cnt > 32 ? __ballot_sync(0xffffffffu, keep(32 + lane)) : 0u;
+        }
+        m0 &= cnt >= 32 ? 0xFFFFFFFFu : (1u << cnt) - 1u;
+        m1 &= cnt >= 64 ? 0xFFFFFFFFu : cnt > 32 ? (1u << (cnt - 32)) - 1u : 0u;
+        GatherPair<kAtlasF16, false> gp;
+        gp.init(a, w0, n0, w1, n1, v0, v1, nullptr, nullptr);
+        if (v0 || v1) {
+            unsigned r0 = m0, r1 = m1;
+            gp.gather(S.v, vbase, __popc(m0) + __popc(m1), [&]() {
+                int k;
+                if (r0) {
+                    k = __ffs(r0) - 1;
+                    r0 &= r0 - 1u;
+                } else {
+                    k = 32 + __ffs(r1) - 1;
+                    r1 &= r1 - 1u;
+                }
+                return k;
+            });
+        }
+        gp.store(a, y, x0, x1);
+    }
+}
+
 // Tile rows [tr0, tr1): tiles are numbered row by row, so a band of tile rows is a contiguous
 // range of tile indices starting at tile0.
+static int sm_count() {
+    static int n[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!n[dev]) cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev);
+    return n[dev] > 0 ? n[dev] : 152;
+}
+
+static cudaError_t launch_fg_class(const FgArgs& a, cudaStream_t s, int tr0, int tr1) {
+    const int I = a.interleave;
+    const int ntx = ((a.width + I - 1) / I + 15) / 16;
+    const int tile_begin = tr0 * ntx, n_tiles = (tr1 - tr0) * ntx;
+    // kFgClassBlocksPerSm 128-thread blocks per SM, spread evenly over the classes
+    const int per_class = std::max(1, std::min(n_tiles, (kFgClassBlocksPerSm * sm_count() + I * I - 1) / (I * I)));
+    const dim3 grid(per_class, I * I);
+    const int sel = (a.reduced ? 4 : 0) | (a.atlas_f16 ? 2 : 0) | (a.normal_f16 ? 1 : 0);
+    switch (sel) {
+        case 0: fg_class_kernel<false, false, false><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+        case 1: fg_class_kernel<false, false, true><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+        case 2: fg_class_kernel<false, true, false><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+        case 3: fg_class_kernel<false, true, true><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+        case 4: fg_class_kernel<true, false, false><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+        case 5: fg_class_kernel<true, false, true><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+        case 6: fg_class_kernel<true, true, false><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+        default: fg_class_kernel<true, true, true><<<grid, 128, 0, s>>>(a, tile_begin, n_tiles); break;
+    }
+    return cudaGetLastError();
+}
+
 template <int T>
 static cudaError_t launch_fg_t(const FgArgs& args, cudaStream_t s, int tr0, int tr1) {
     const int I = args.interleave;
     const int sw = (args.width + I - 1) / I;
     const int ntx = (sw + T - 1) / T;
     if (tr1 <= tr0) return cudaSuccess;
+    if (T == 16 && args.cull != 2 && args.per_class >= 1 && args.per_class <= kClassMaxVpls)
+        return launch_fg_class(args, s, tr0, tr1);
     FgArgs a = args;
     a.tile0 = tr0 * ntx;
     const dim3 grid(ntx * (tr1 - tr0), I * I);
