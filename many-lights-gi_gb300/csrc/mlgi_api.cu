@@ -1224,7 +1224,8 @@ struct mlgi_batch {
     mlgi::BatchView* d_views = nullptr;
     int* d_prefix = nullptr;
     int grid[mlgi::kBpCount] = {};
-    size_t pp_smem = 0;
+    size_t pp_smem = 0;   // shared memory of the per-ISM middle-level pass
+    size_t pyr_smem = 0;  // shared memory of the one-block-per-ISM pyramid pass
     int form = MLGI_BATCH_PERSISTENT;
     int launches = 0;                  // kernels per mlgi_batch_launch
     std::vector<cudaStream_t> side;    // concurrent form: the views' streams (used during capture)
@@ -1283,8 +1284,10 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     counts[mlgi::kBpClear] = (int)((texels + mlgi::kBatchClearTexels - 1) / mlgi::kBatchClearTexels);
     counts[mlgi::kBpVpl] = (int)((n + mlgi::kBatchVplPerItem - 1) / mlgi::kBatchVplPerItem);
     counts[mlgi::kBpSplat] = f.points.n_buckets * v.splat.chunks;
+    const bool fused = mlgi::pyramid_fused(f.ism.ism_size, f.ism.levels, f.ism.z_far);
     for (int pass : {mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1, mlgi::kBpPush0})
-        counts[pass] = mlgi::pullpush_batch_items(pass, aw, ah, f.ism.grid_x * f.ism.grid_y, f.ism.levels);
+        counts[pass] = fused ? 0 : mlgi::pullpush_batch_items(pass, aw, ah, f.ism.grid_x * f.ism.grid_y, f.ism.levels);
+    counts[mlgi::kBpPyramid] = fused ? f.ism.grid_x * f.ism.grid_y : 0;
     counts[mlgi::kBpFg] = red ? 0 : v.fg_tiles_per_class * I * I;
     counts[mlgi::kBpFg16] = red ? v.fg_tiles_per_class * I * I : 0;
     return MLGI_OK;
@@ -1303,12 +1306,20 @@ mlgi_status capture_batch(mlgi_batch* b) {
             e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(mlgi::BatchView) * n_views, cudaMemcpyHostToDevice,
                                 b->stream);
         for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1,
-                      mlgi::kBpPush0})
-            if (e == cudaSuccess)
-                e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullMid ? b->pp_smem : 0, b->stream);
-        for (int p : {mlgi::kBpFg, mlgi::kBpFg16})
-            if (e == cudaSuccess) e = mlgi::launch_batch_fg(t, p, b->grid[p], b->stream);
-        b->launches = 9;
+                      mlgi::kBpPush0, mlgi::kBpPyramid}) {
+            if (e == cudaSuccess && b->grid[p] > 0) {
+                e = mlgi::launch_batch_ism(t, p, b->grid[p],
+                                           p == mlgi::kBpPullMid ? b->pp_smem : p == mlgi::kBpPyramid ? b->pyr_smem : 0,
+                                           b->stream);
+                ++b->launches;
+            }
+        }
+        for (int p : {mlgi::kBpFg, mlgi::kBpFg16}) {
+            if (e == cudaSuccess && b->grid[p] > 0) {
+                e = mlgi::launch_batch_fg(t, p, b->grid[p], b->stream);
+                ++b->launches;
+            }
+        }
     } else {
         // views to streams, costliest first onto the least-loaded stream (estimated from the work
         // measured per unit at 1080p: gathered pairs, splatted points, atlas texels)
@@ -1341,7 +1352,9 @@ mlgi_status capture_batch(mlgi_batch* b) {
                 if (e == cudaSuccess) e = mlgi::launch_ism_splat(v.splat, s);
                 if (e == cudaSuccess) e = mlgi::launch_pullpush_captured(v.pp, s);
                 if (e == cudaSuccess) e = mlgi::launch_final_gather(v.fg, s);
-                b->launches += 3 + (v.pp.levels >= 2 ? 4 : 2) + 1;
+                b->launches += 3 + (mlgi::pyramid_fused(v.pp.ism_size, v.pp.levels, v.pp.z_far) ? 1
+                                    : v.pp.levels >= 2                                          ? 4
+                                                                                                : 2) + 1;
             }
             if (e == cudaSuccess) e = cudaEventRecord(b->events[j], b->side[j]);  // join
             if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->events[j], 0);
@@ -1423,6 +1436,8 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
         if (st != MLGI_OK) return bail(st);
         for (int p = 0; p < mlgi::kBpCount; ++p) prefix[p * (n_views + 1) + i + 1] = prefix[p * (n_views + 1) + i] + counts[p];
         b->pp_smem = std::max(b->pp_smem, mlgi::pullmid_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
+        if (mlgi::pyramid_fused(views[i].ism.ism_size, views[i].ism.levels, views[i].ism.z_far))
+            b->pyr_smem = std::max(b->pyr_smem, mlgi::pyramid_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -1430,7 +1445,9 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
         const int items = prefix[p * (n_views + 1) + n_views];
         const int per_sm = p == mlgi::kBpFg || p == mlgi::kBpFg16
                                ? 8
-                               : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
+                               : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid   ? b->pp_smem
+                                                              : p == mlgi::kBpPyramid ? b->pyr_smem
+                                                                                      : 0);
         b->grid[p] = std::min(items, std::max(1, sms) * per_sm);
     }
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1463,7 +1480,9 @@ mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_des
     if (view_arena_bytes(*desc) != view_arena_bytes(old) || desc->points.n_buckets != old.points.n_buckets ||
         desc->gbuffer.width != old.gbuffer.width || desc->gbuffer.height != old.gbuffer.height ||
         desc->fg.interleave != old.fg.interleave || desc->ism.grid_x != old.ism.grid_x ||
-        desc->ism.ism_size != old.ism.ism_size || desc->ism.levels != old.ism.levels)
+        desc->ism.ism_size != old.ism.ism_size || desc->ism.levels != old.ism.levels ||
+        mlgi::pyramid_fused(desc->ism.ism_size, desc->ism.levels, desc->ism.z_far) !=
+            mlgi::pyramid_fused(old.ism.ism_size, old.ism.levels, old.ism.z_far))
         return fail(ctx, MLGI_EINVAL, "a view update must keep its sizes and layout");
     MLGI_CUDA(ctx, cudaStreamSynchronize(b->stream));
     int counts[mlgi::kBpCount];
