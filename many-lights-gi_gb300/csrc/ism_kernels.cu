@@ -99,12 +99,15 @@ cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s) {
 // identical). Each point keeps the first <= 4 VPLs that pass the two-sided hemisphere cull and
 // atomicMin's its key into their paraboloid ISMs.
 constexpr int kSplatThreads = 256;
+constexpr int kSplatTaskCap = 31 + 4 * 32;
 
 struct SplatSmem {
     // per VPL, 16-byte rows: (position, ISM tile x), (normal, ISM tile y), (lookAtRH s, 0),
     // (lookAtRH u, 0); the tile offsets are float(x) and float(y) of ism_utils.glsl:35-37
     float4 pos[16], n[16], s[16], u[16];
-    float4 tasks[kSplatThreads / 32][128];  // per warp: (point xyz, VPL slot << 8 | radius byte)
+    // per warp: (point xyz, VPL slot << 8 | radius byte); up to 31 carried over from the previous
+    // group of points plus 4 for each of 32 new points
+    float4 tasks[kSplatThreads / 32][kSplatTaskCap];
     // per byte value b of a point's packed word, computed with the shader's own operations:
     float unorm[256];       // float(b) / 255 * 2 - 1, a normal component (ism.comp:81-85)
     uint8_t rbyte[256];     // uint(float(b) / 255 * 25 * 10 / 2), the key's radius byte (ism.comp:87, 131-136)
@@ -176,7 +179,49 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
     float4* tasks = S.tasks[threadIdx.x >> 5];
     unsigned issued = 0;  // kCount: this thread's in-range projections
     // Each warp takes 32 points at a time; a point's projections into its <= 4 VPLs become tasks
-    // that the whole warp then runs, so lanes do not idle on points with fewer VPLs.
+    // in the warp's list, and the warp runs them 32 at a time with all lanes. Fewer than 32 left
+    // over wait for the next group's tasks, so that only the warp's last round runs partly empty.
+    // atomicMin is order-independent, so the keys do not depend on when a task runs.
+    int pending = 0;  // tasks in the list (warp-uniform)
+    auto run_task = [&](const float4 task) {
+        const uint32_t tw = __float_as_uint(task.w);
+        const int i = (int)(tw >> 8);
+        const uint32_t rbyte = tw & 0xFFu;
+        const float4 vp = S.pos[i], vn = S.n[i];
+        const v3 rel = mk(task.x, task.y, task.z) - mk(vp.x, vp.y, vp.z);
+        // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
+        const float dist = length(rel);
+        const v3 n = mk(vn.x, vn.y, vn.z);
+        const float4 vs = S.s[i], vu = S.u[i];
+        float vx = dot(mk(vs.x, vs.y, vs.z), rel);
+        float vy = dot(mk(vu.x, vu.y, vu.z), rel);
+        float vz = ((-n.x) * rel.x + (-n.y) * rel.y) + (-n.z) * rel.z;
+        const float signOfV = gsign(vz);
+        vx = vx / dist;
+        vy = vy / dist;
+        vz = vz / dist;
+        vz = 1.0f - vz;
+        vx = vx / vz;
+        vy = vy / vz;
+        vz = dist / z_far;
+        vz = vz * -signOfV;
+        vx = (vx + 1.0f) / 2.0f;
+        vy = (vy + 1.0f) / 2.0f;
+        vx = vx + vp.w;  // ISM tile x
+        vy = vy + vn.w;  // ISM tile y
+        vx = rgx != 0.f ? vx * rgx : vx / fgx;
+        vy = rgy != 0.f ? vy * rgy : vy / fgy;
+        vx = vx * fw;
+        vy = vy * fh;
+        vz = vz * 16777216.0f;
+        const uint32_t key = (f2u(vz) << 8) | rbyte;
+        const int px = f2i(vx), py = f2i(vy);
+        if (px < 0 || py < 0 || px >= atlas_w || py >= atlas_h) return;  // image op out of range: no-op
+        if (kCount)
+            ++issued;
+        else
+            atomicMin(keys + (size_t)py * atlas_w + px, key);
+    };
     for (uint32_t base = first + threadIdx.x - lane; base < cnt; base += kSplatThreads) {
         const uint32_t j = base + lane;
         float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -212,52 +257,24 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         if (found > 0) {
             const uint32_t rbyte = S.rbyte[__float_as_uint(pt.w) >> 24];
             for (int k = 0; k < found; ++k)
-                tasks[pre + k] = make_float4(pt.x, pt.y, pt.z, __uint_as_float((((used >> (4 * k)) & 15u) << 8) | rbyte));
+                tasks[pending + pre + k] =
+                    make_float4(pt.x, pt.y, pt.z, __uint_as_float((((used >> (4 * k)) & 15u) << 8) | rbyte));
         }
+        pending += total;
         __syncwarp();
-        // for each task, project and atomicMin (ism.comp:112-137)
-        for (int t = lane; t < total; t += 32) {
-            const float4 task = tasks[t];
-            const uint32_t tw = __float_as_uint(task.w);
-            const int i = (int)(tw >> 8);
-            const uint32_t rbyte = tw & 0xFFu;
-            const float4 vp = S.pos[i], vn = S.n[i];
-            const v3 rel = mk(task.x, task.y, task.z) - mk(vp.x, vp.y, vp.z);
-            // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
-            const float dist = length(rel);
-            const v3 n = mk(vn.x, vn.y, vn.z);
-            const float4 vs = S.s[i], vu = S.u[i];
-            float vx = dot(mk(vs.x, vs.y, vs.z), rel);
-            float vy = dot(mk(vu.x, vu.y, vu.z), rel);
-            float vz = ((-n.x) * rel.x + (-n.y) * rel.y) + (-n.z) * rel.z;
-            const float signOfV = gsign(vz);
-            vx = vx / dist;
-            vy = vy / dist;
-            vz = vz / dist;
-            vz = 1.0f - vz;
-            vx = vx / vz;
-            vy = vy / vz;
-            vz = dist / z_far;
-            vz = vz * -signOfV;
-            vx = (vx + 1.0f) / 2.0f;
-            vy = (vy + 1.0f) / 2.0f;
-            vx = vx + vp.w;  // ISM tile x
-            vy = vy + vn.w;  // ISM tile y
-            vx = rgx != 0.f ? vx * rgx : vx / fgx;
-            vy = rgy != 0.f ? vy * rgy : vy / fgy;
-            vx = vx * fw;
-            vy = vy * fh;
-            vz = vz * 16777216.0f;
-            const uint32_t key = (f2u(vz) << 8) | rbyte;
-            const int px = f2i(vx), py = f2i(vy);
-            if (px < 0 || py < 0 || px >= atlas_w || py >= atlas_h) continue;  // image op out of range: no-op
-            if (kCount)
-                ++issued;
-            else
-                atomicMin(keys + (size_t)py * atlas_w + px, key);
-        }
-        __syncwarp();  // the warp's tasks are consumed before the next points overwrite them
+        // full rounds of 32 tasks (ism.comp:112-137 for each)
+        const int full = pending & ~31;
+        for (int t = lane; t < full; t += 32) run_task(tasks[t]);
+        // the remainder (< 32) moves to the front of the list
+        const int rem = pending - full;
+        float4 keep = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane < rem) keep = tasks[full + lane];
+        __syncwarp();
+        if (lane < rem) tasks[lane] = keep;
+        pending = rem;
+        __syncwarp();
     }
+    if (lane < pending) run_task(tasks[lane]);  // the last, partly empty round
     if (kCount) {
         for (int o = 16; o > 0; o >>= 1) issued += __shfl_xor_sync(0xffffffffu, issued, o);
         if (lane == 0 && issued) atomicAdd(atomics, (unsigned long long)issued);

@@ -40,8 +40,10 @@ def test_batch_equals_single_frames_and_replays(ctx, form, streams):
         f.rgb.zero_()
     torch.cuda.synchronize()  # the batch runs on its own stream
     b = Batch(ctx, frames, form, streams)
+    # persistent: clear, VPLs, splat, the four pull-push levels' passes and one gathering pass per
+    # precision; concurrent: each view's own kernels
     assert b.kernel_launches() == (9 if form == mlgi.BATCH_PERSISTENT
-                                   else sum(3 + (4 if f.cfg.levels >= 2 else 2) + 1 for f in frames))
+                                   else sum(3 + mlgi.pullpush_launches(f.cfg) + 1 for f in frames))
     for _ in range(2):  # the graph replays
         b.launch()
         torch.cuda.synchronize()
