@@ -1036,22 +1036,6 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH, 5) batch_push0_kernel(Bat
     }
 }
 
-// The fused pyramid over the view table: an item is one ISM of a view.
-__global__ void __launch_bounds__(kPyrBigThreads, 2) batch_pyramid_kernel(BatchTable t) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ PullPushArgs args;
-    __shared__ int s_pre[kBatchPrefixCache + 1];
-    ItemWalk w;
-    w.init(t.prefix + kBpPyramid * (t.n_views + 1), t.n_views, s_pre);
-    int cur = -1;
-    for (int item = blockIdx.x; item < w.total; item += gridDim.x) {
-        const int v = w.view(item);
-        stage_pp_args(t, v, cur, args);
-        __syncthreads();  // the previous item's use of the shared memory is over
-        pyramid_ism<kPyrBigThreads>(args, w.local(item), smem);
-    }
-}
-
 int pullpush_batch_items(int pass, int atlas_w, int atlas_h, int ism_count, int levels) {
     const int w1 = atlas_w >> 1, h1 = atlas_h >> 1;
     switch (pass) {
@@ -1075,7 +1059,6 @@ cudaError_t launch_batch_ism(const BatchTable& t, int pass, int grid, size_t sme
             break;
         case kBpPush1: batch_push1_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(t); break;
         case kBpPush0: batch_push0_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(t); break;
-        case kBpPyramid: batch_pyramid_kernel<<<grid, kPyrBigThreads, smem, s>>>(t); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -1095,10 +1078,6 @@ int batch_blocks_per_sm(int pass, size_t smem) {
             break;
         case kBpPush1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_push1_kernel, tt, 0); break;
         case kBpPush0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_push0_kernel, tt, 0); break;
-        case kBpPyramid:
-            cudaFuncSetAttribute(batch_pyramid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pyramid_kernel, kPyrBigThreads, smem);
-            break;
         default: break;
     }
     return n > 0 ? n : 1;

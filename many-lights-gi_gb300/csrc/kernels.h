@@ -164,10 +164,7 @@ struct BatchView {
     int fg_mode;  // 0: FP32 records/atlas/normals, 1: reduced (24-byte records, FP16 atlas and normals)
 };
 
-// kBpPyramid: the whole pull-push of one ISM per work item (views whose pyramid fits one block);
-// the four passes before it serve the other views.
-enum BatchPass { kBpClear = 0, kBpVpl, kBpSplat, kBpPull1, kBpPullMid, kBpPush1, kBpPush0, kBpFg, kBpFg16, kBpPyramid,
-                 kBpCount };
+enum BatchPass { kBpClear = 0, kBpVpl, kBpSplat, kBpPull1, kBpPullMid, kBpPush1, kBpPush0, kBpFg, kBpFg16, kBpCount };
 
 struct BatchTable {
     const BatchView* views;  // device

@@ -1224,8 +1224,7 @@ struct mlgi_batch {
     mlgi::BatchView* d_views = nullptr;
     int* d_prefix = nullptr;
     int grid[mlgi::kBpCount] = {};
-    size_t pp_smem = 0;   // shared memory of the per-ISM middle-level pass
-    size_t pyr_smem = 0;  // shared memory of the one-block-per-ISM pyramid pass
+    size_t pp_smem = 0;  // shared memory of the per-ISM middle-level pass
     int form = MLGI_BATCH_PERSISTENT;
     int launches = 0;                  // kernels per mlgi_batch_launch
     std::vector<cudaStream_t> side;    // concurrent form: the views' streams (used during capture)
@@ -1284,12 +1283,11 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     counts[mlgi::kBpClear] = (int)((texels + mlgi::kBatchClearTexels - 1) / mlgi::kBatchClearTexels);
     counts[mlgi::kBpVpl] = (int)((n + mlgi::kBatchVplPerItem - 1) / mlgi::kBatchVplPerItem);
     counts[mlgi::kBpSplat] = f.points.n_buckets * v.splat.chunks;
-    // the persistent form runs the pull-push level by level for every view: one pass of the
-    // one-block-per-ISM pyramid over all views (kBpPyramid) measured 13.6 ms against 12.5 ms per
-    // 32-view batch, its block shape and shared memory being the largest view's for every view
+    // the persistent form runs the pull-push level by level for every view (one pass of the
+    // one-block-per-ISM pyramid over all views' ISMs measured 13.6 ms against 12.5 ms per 32-view
+    // batch: its block shape and shared memory were the largest view's for every view)
     for (int pass : {mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1, mlgi::kBpPush0})
         counts[pass] = mlgi::pullpush_batch_items(pass, aw, ah, f.ism.grid_x * f.ism.grid_y, f.ism.levels);
-    counts[mlgi::kBpPyramid] = 0;
     counts[mlgi::kBpFg] = red ? 0 : v.fg_tiles_per_class * I * I;
     counts[mlgi::kBpFg16] = red ? v.fg_tiles_per_class * I * I : 0;
     return MLGI_OK;
@@ -1308,11 +1306,9 @@ mlgi_status capture_batch(mlgi_batch* b) {
             e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(mlgi::BatchView) * n_views, cudaMemcpyHostToDevice,
                                 b->stream);
         for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1,
-                      mlgi::kBpPush0, mlgi::kBpPyramid}) {
+                      mlgi::kBpPush0}) {
             if (e == cudaSuccess && b->grid[p] > 0) {
-                e = mlgi::launch_batch_ism(t, p, b->grid[p],
-                                           p == mlgi::kBpPullMid ? b->pp_smem : p == mlgi::kBpPyramid ? b->pyr_smem : 0,
-                                           b->stream);
+                e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullMid ? b->pp_smem : 0, b->stream);
                 ++b->launches;
             }
         }
@@ -1438,8 +1434,6 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
         if (st != MLGI_OK) return bail(st);
         for (int p = 0; p < mlgi::kBpCount; ++p) prefix[p * (n_views + 1) + i + 1] = prefix[p * (n_views + 1) + i] + counts[p];
         b->pp_smem = std::max(b->pp_smem, mlgi::pullmid_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
-        if (mlgi::pyramid_fused(views[i].ism.ism_size, views[i].ism.levels, views[i].ism.z_far))
-            b->pyr_smem = std::max(b->pyr_smem, mlgi::pyramid_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -1447,9 +1441,7 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
         const int items = prefix[p * (n_views + 1) + n_views];
         const int per_sm = p == mlgi::kBpFg || p == mlgi::kBpFg16
                                ? 8
-                               : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid   ? b->pp_smem
-                                                              : p == mlgi::kBpPyramid ? b->pyr_smem
-                                                                                      : 0);
+                               : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
         b->grid[p] = std::min(items, std::max(1, sms) * per_sm);
     }
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
