@@ -3,6 +3,8 @@
 The reference's hot path is five GLSL 4.3 compute shaders (paths inside the reference project):
   data/shaders/gi/vpl_processor.comp, data/shaders/ism/ism.comp, data/shaders/ism/pull.comp,
   data/shaders/ism/push.comp, data/shaders/gi/final_gathering.comp
+and its clustered culling two more: data/shaders/clustered_shading/clustering.comp and
+  data/shaders/clustered_shading/light_lists.comp
 plus their includes (common/floatpacking.glsl, common/random.glsl, common/reprojection.glsl,
 ism/ism_utils.glsl). This recipe reads them where they lie under the reference root (REF below), applies a fixed
 list of mechanical GLSL -> C++ rewrites (below), and compiles the result together with
@@ -22,6 +24,9 @@ Rewrites (nothing else is changed):
   7. parameter qualifier `in` dropped; memory qualifiers (restrict, readonly, writeonly, coherent)
      dropped;
   8. `uniform T name [= v];` -> a member read from the harness's bindings (default v);
+     (and for the fragment shader gi_blur.frag: `inout` parameters -> references, stage `in`/`out`
+     variables -> members the harness sets and reads; the X and Y programs are the reference's own
+     DIRECTION replacements, GIStage.cpp:444-449)
      interface blocks `layout(...) uniform|buffer Name { T member[...]; };` -> members bound to
      harness arrays; `shared T name[N];` -> a view of the work group's shared arena.
 The shaders are wrapped as C++ structs (globals -> members, main() -> member function).
@@ -56,6 +61,11 @@ SHADERS = {
     "Ref_push_L0": ("data/shaders/ism/push.comp", []),
     "Ref_push": ("data/shaders/ism/push.comp", [("#define LEVEL_ZERO", "#undef LEVEL_ZERO")]),
     "Ref_final_gathering": ("data/shaders/gi/final_gathering.comp", []),
+    "Ref_clustering": ("data/shaders/clustered_shading/clustering.comp", []),
+    # the X and Y programs GIStage.cpp:444-449 builds from the fragment shader by global replacement
+    "Ref_gi_blur_x": ("data/shaders/gi/gi_blur.frag", [("#define DIRECTION ivec2(0,0)", "#define DIRECTION ivec2(1,0)")]),
+    "Ref_gi_blur_y": ("data/shaders/gi/gi_blur.frag", [("#define DIRECTION ivec2(0,0)", "#define DIRECTION ivec2(0,1)")]),
+    "Ref_light_lists": ("data/shaders/clustered_shading/light_lists.comp", []),
 }
 
 GLSL_TYPES = ("float", "int", "uint", "bool", "vec2", "vec3", "vec4", "ivec2", "ivec3", "ivec4", "uvec2",
@@ -134,8 +144,11 @@ def rewrite(src: str) -> str:
     src = re.sub(r"\.g\b", ".y", src)
     src = re.sub(r"\.b\b", ".z", src)
     src = re.sub(r"\.a\b", ".w", src)
-    # 7. parameter qualifier `in`
+    # 7. parameter qualifier `in`; `inout` parameters become references
     src = re.sub(r"\b(const\s+)?in\s+(\w+\s+\w+\s*[,)])", r"\1\2", src)
+    src = re.sub(r"\binout\s+(\w+)\s+(\w+)", r"\1& \2", src)
+    # 9. a fragment shader's stage inputs and outputs become members the harness sets and reads
+    src = re.sub(r"^\s*(?:in|out)\s+(\w+)\s+(\w+)\s*;", r"\1 \2{};", src, flags=re.M)
     return src
 
 

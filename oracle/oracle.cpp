@@ -639,8 +639,10 @@ V3<float> unpack_r11_ref(uint32_t w) {
 // gi_blur.frag:24-72 as GIStage::blur runs it (GIStage.cpp:308-344): the X pass over the whole
 // image into a temporary buffer, then the Y pass; with `packed`, every buffer is R11G11B10F.
 // Samples outside the image are skipped.
+// nrm_rgb (optional, in place of nrm_oct): normals stored as n*0.5+0.5 RGB, decoded as gi_blur.frag
+// decodes its faceNormalSampler texels (rgb * 2 - 1) -- the reference G-buffer's format, for pinning
 void gi_blur_ref(int w, int h, const float* depth, const float* nrm_oct, const void* gi_in, int packed, float A,
-                 float B, void* gi_out, int threads) {
+                 float B, void* gi_out, int threads, const float* nrm_rgb = nullptr) {
     const size_t n = (size_t)w * h;
     std::vector<float> lin(n);
     std::vector<V3<float>> nrm(n), src(n), tmp(n);
@@ -648,7 +650,9 @@ void gi_blur_ref(int w, int h, const float* depth, const float* nrm_oct, const v
         const float z_b = depth[p];
         const float z_n = 2.0f * z_b - 1.0f;
         lin[p] = -B / (A + z_n);  // reprojection.glsl:6-14
-        nrm[p] = oct_decode<float>(nrm_oct[2 * p], nrm_oct[2 * p + 1]);
+        nrm[p] = nrm_rgb ? V3<float>(nrm_rgb[3 * p] * 2.0f - 1.0f, nrm_rgb[3 * p + 1] * 2.0f - 1.0f,
+                                     nrm_rgb[3 * p + 2] * 2.0f - 1.0f)
+                         : oct_decode<float>(nrm_oct[2 * p], nrm_oct[2 * p + 1]);
         src[p] = packed ? unpack_r11_ref(static_cast<const uint32_t*>(gi_in)[p])
                         : V3<float>(static_cast<const float*>(gi_in)[3 * p], static_cast<const float*>(gi_in)[3 * p + 1],
                                     static_cast<const float*>(gi_in)[3 * p + 2]);
@@ -909,6 +913,10 @@ void oracle_unpack_r11g11b10f(const uint32_t* words, float* rgb, int64_t n) {
 void oracle_gi_blur(int w, int h, const float* depth, const float* nrm_oct, const void* gi_in, int packed, float A,
                     float B, void* gi_out, int threads) {
     gi_blur_ref(w, h, depth, nrm_oct, gi_in, packed, A, B, gi_out, threads);
+}
+void oracle_gi_blur_rgb_normals(int w, int h, const float* depth, const float* nrm_rgb, const float* gi_in, float A,
+                                float B, float* gi_out, int threads) {
+    gi_blur_ref(w, h, depth, nullptr, gi_in, 0, A, B, gi_out, threads, nrm_rgb);
 }
 void oracle_cluster_lights(int w, int h, const float* depth, const float* inv_vp, float A, float B, float zfar,
                            const float* vpos, const uint32_t* vpn_bits, int n_vpl, uint32_t* used, uint32_t* masks,

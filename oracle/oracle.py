@@ -196,6 +196,18 @@ def gi_blur(depth, normal_oct, gi, proj_a, proj_b, packed=False, threads=0):
     return out
 
 
+def gi_blur_rgb_normals(depth, normal_rgb, gi, proj_a, proj_b, threads=0):
+    """gi_blur with the normals given as n*0.5+0.5 RGB [H, W, 3] (the reference G-buffer's format,
+    decoded rgb * 2 - 1 as gi_blur.frag does); FP32 RGB in and out."""
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    g = np.ascontiguousarray(gi, np.float32)
+    out = np.zeros_like(g)
+    lib().oracle_gi_blur_rgb_normals(w, h, _p(depth), _p(np.ascontiguousarray(normal_rgb, np.float32)), _p(g),
+                                     C.c_float(proj_a), C.c_float(proj_b), _p(out), threads)
+    return out
+
+
 def composite(gi, albedo, exposure, occlusion=None, direct=None, packed=False):
     """deferredshading.frag's GI ambient term, Reinhard and toSRGB. Returns (rgb float32 [H, W, 3],
     rgba8 uint32 [H, W])."""

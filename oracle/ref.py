@@ -83,3 +83,33 @@ def final_gather(depth, normal_rgb, inv_vp, proj, vpl9, n_vpl, vpl_start, vpl_en
                            _p(np.ascontiguousarray(atlas, np.float32)), aw, ah, C.c_float(z_far), C.c_float(z_near),
                            C.c_float(gi), C.c_float(clampv), per_class, _p(out), threads)
     return out
+
+
+def cluster_lights(depth, inv_vp, proj_a, proj_b, z_far, packed_vpls):
+    """clustering.comp + light_lists.comp as ClusteredShading::process drives them (1024 VPLs).
+    Returns, per used cluster in the atomic counter's order, (x, y, slice) and its 1024-entry
+    light-list column (entry 64 s: sub-list s's count + 1; its VPL ids follow)."""
+    h, w = depth.shape
+    nclusters = ((w + 127) // 128) * ((h + 127) // 128) * 16
+    n_used = C.c_int(0)
+    words = np.zeros(nclusters, np.uint32)
+    lists = np.zeros((nclusters, 1024), np.uint32)
+    pk = np.ascontiguousarray(packed_vpls, np.float32)
+    lib().ref_cluster_lights(w, h, _p(np.ascontiguousarray(depth, np.float32)),
+                             _p(np.ascontiguousarray(inv_vp, np.float32).reshape(16)), C.c_float(proj_a),
+                             C.c_float(proj_b), C.c_float(z_far), _p(pk), pk.shape[0], C.byref(n_used), _p(words),
+                             _p(lists))
+    n = n_used.value
+    xyz = [(int(wd & 0xFF), int((wd >> 8) & 0xFF), int((wd >> 16) & 0xFF)) for wd in words[:n]]
+    return xyz, lists[:n]
+
+
+def gi_blur(depth, normal_rgb, gi, proj_a, proj_b, threads=0):
+    """gi_blur.frag's X program then its Y program (GIStage::blur) on float RGB buffers; normal_rgb
+    is n*0.5+0.5. Returns [H, W, 3] float32."""
+    h, w = depth.shape
+    out = np.zeros((h, w, 3), np.float32)
+    lib().ref_gi_blur(w, h, _p(np.ascontiguousarray(depth, np.float32)),
+                      _p(np.ascontiguousarray(normal_rgb, np.float32)), _p(np.ascontiguousarray(gi, np.float32)),
+                      C.c_float(proj_a), C.c_float(proj_b), _p(out), threads)
+    return out

@@ -64,6 +64,18 @@ MLGI_REF_SHADER_END
 MLGI_REF_SHADER(Ref_final_gathering)
 #include "Ref_final_gathering.inc"
 MLGI_REF_SHADER_END
+MLGI_REF_SHADER(Ref_gi_blur_x)
+#include "Ref_gi_blur_x.inc"
+MLGI_REF_SHADER_END
+MLGI_REF_SHADER(Ref_gi_blur_y)
+#include "Ref_gi_blur_y.inc"
+MLGI_REF_SHADER_END
+MLGI_REF_SHADER(Ref_clustering)
+#include "Ref_clustering.inc"
+MLGI_REF_SHADER_END
+MLGI_REF_SHADER(Ref_light_lists)
+#include "Ref_light_lists.inc"
+MLGI_REF_SHADER_END
 
 // ---- dispatch -----------------------------------------------------------------------------------
 namespace {
@@ -310,6 +322,108 @@ void ref_final_gather(int w, int h, const float* depth, const float* normal_rgb,
     dispatch<Ref_final_gathering>(B, uvec3((uint)gx, (uint)gy, 1), uvec3(8, 8, 1), false, threads);
     for (size_t t = 0; t < (size_t)w * h; ++t)
         for (int k = 0; k < 3; ++k) out_rgb[3 * t + k] = outv[4 * t + k];
+}
+
+// ClusteredShading::process (ClusteredShading.cpp:70-112): clustering.comp over
+// ceil(w/128) x ceil(h/128) groups of 128, then light_lists.comp over (clusters, 16) groups of 64.
+// The projection matrix has only [2][2] = proj_a and [3][2] = proj_b set (the shaders read no
+// other entry). Outputs: *n_used, and per used cluster (in the order the atomic counter gave):
+// cluster_word[i] = x | y << 8 | slice << 16, and lists[i * 1024 .. +1024), the light-list column
+// (entry 64 s is sub-list s's count + 1, its VPL ids follow). Runs work groups in dispatch order
+// on one thread, so that a sub-list's count slot is written after the previous sub-list's entries.
+void ref_cluster_lights(int w, int h, const float* depth, const float* inv_vp, float proj_a, float proj_b, float zfar,
+                        const float* packed_vpls, int n_vpl, int* n_used, uint32_t* cluster_word, uint32_t* lists) {
+    const int ncx = (w + 127) / 128, ncy = (h + 127) / 128, nclusters = ncx * ncy * 16;
+    std::vector<float> dep((size_t)w * h * 4, 0.f);
+    for (size_t t = 0; t < (size_t)w * h; ++t) dep[4 * t] = depth[t];
+    mat4 P;
+    for (int c = 0; c < 4; ++c) P.c[c] = vec4(0.f, 0.f, 0.f, 0.f);
+    P.c[2].z = proj_a;
+    P.c[3].z = proj_b;
+    std::vector<uint32_t> compact((size_t)nclusters, 0u), list_ids((size_t)nclusters, 0u);
+    std::vector<uint32_t> counter(4, 0u);
+    {
+        Bindings B;
+        B.set("compactUsedIDs", UImage2D{compact.data(), nclusters, 1, 1});
+        B.set("lightListIds", Image3D{list_ids.data(), ncx, ncy, 16});
+        B.set("depthSampler", Sampler2D{dep.data(), nullptr, w, h, true});
+        B.buffers["atomicCounter"] = counter.data();
+        B.set("projectionMatrix", P);
+        B.set("zFar", zfar);
+        dispatch<Ref_clustering>(B, uvec3((uint)ncx, (uint)ncy, 1), uvec3(128, 1, 1), true, 1);
+    }
+    const int used = (int)counter[0];
+    std::vector<vec4> pk(1024);
+    std::memcpy(pk.data(), packed_vpls, sizeof(float) * 4 * (size_t)std::min(n_vpl, 1024));
+    std::vector<uint32_t> ll((size_t)std::max(used, 1) * 1024, 0u);
+    {
+        Bindings B;
+        B.set("compactUsedClusterIDs", UImage2D{compact.data(), nclusters, 1, 1});
+        B.set("lightLists", UImage2D{ll.data(), std::max(used, 1), 1024, 1});
+        B.set("clusterCorners", Image2D{nullptr, nullptr, 0, 0, 4});
+        B.buffers["vplPositionNormalBuffer"] = pk.data();
+        B.buffers["numUsedClusters"] = counter.data();
+        B.set("viewport", ivec2(w, h));
+        B.set("projectionMatrix", P);
+        B.set("viewProjectionInverseMatrix", to_mat4(inv_vp));
+        B.set("zFar", zfar);
+        B.set("vplStartIndex", 0);
+        B.set("vplEndIndex", 1024);
+        dispatch<Ref_light_lists>(B, uvec3((uint)nclusters, 16, 1), uvec3(64, 1, 1), true, 1);
+    }
+    *n_used = used;
+    for (int i = 0; i < used; ++i) {
+        cluster_word[i] = compact[i];
+        for (int r = 0; r < 1024; ++r) lists[(size_t)i * 1024 + r] = ll[(size_t)r * used + i];
+    }
+}
+
+// GIStage::blur (GIStage.cpp:308-344): gi_blur.frag's X program over the screen-aligned quad into a
+// temporary buffer, then its Y program; every buffer is float RGB here. normal_rgb: n*0.5+0.5.
+void ref_gi_blur(int w, int h, const float* depth, const float* normal_rgb, const float* gi_rgb, float proj_a,
+                 float proj_b, float* out_rgb, int threads) {
+    std::vector<float> dep((size_t)w * h * 4, 0.f), nrm((size_t)w * h * 4, 0.f), gi((size_t)w * h * 4, 0.f),
+        tmp((size_t)w * h * 4, 0.f);
+    for (size_t t = 0; t < (size_t)w * h; ++t) {
+        dep[4 * t] = depth[t];
+        for (int k = 0; k < 3; ++k) {
+            nrm[4 * t + k] = normal_rgb[3 * t + k];
+            gi[4 * t + k] = gi_rgb[3 * t + k];
+        }
+    }
+    mat4 P;
+    for (int c = 0; c < 4; ++c) P.c[c] = vec4(0.f, 0.f, 0.f, 0.f);
+    P.c[2].z = proj_a;
+    P.c[3].z = proj_b;
+    auto pass = [&](auto tag, const std::vector<float>& src, std::vector<float>& dst) {
+        using S = typename decltype(tag)::type;
+        Bindings B;
+        B.set("giSampler", Sampler2D{src.data(), nullptr, w, h, true});
+        B.set("faceNormalSampler", Sampler2D{nrm.data(), nullptr, w, h, true});
+        B.set("depthSampler", Sampler2D{dep.data(), nullptr, w, h, true});
+        B.set("projectionMatrix", P);
+        B.set("projectionInverseMatrix", P);
+#pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : omp_get_max_threads())
+        for (int y = 0; y < h; ++y) {
+            S sh(&B);
+            for (int x = 0; x < w; ++x) {
+                sh.gl_FragCoord = vec4(float(x) + 0.5f, float(y) + 0.5f, 0.f, 1.f);
+                sh.v_uv = vec2((float(x) + 0.5f) / float(w), (float(y) + 0.5f) / float(h));
+                sh.main();
+                float* o = dst.data() + 4 * ((size_t)y * w + x);
+                o[0] = sh.outColor.x;
+                o[1] = sh.outColor.y;
+                o[2] = sh.outColor.z;
+            }
+        }
+    };
+    struct X { using type = Ref_gi_blur_x; };
+    struct Y { using type = Ref_gi_blur_y; };
+    pass(X{}, gi, tmp);
+    std::vector<float> res((size_t)w * h * 4, 0.f);
+    pass(Y{}, tmp, res);
+    for (size_t t = 0; t < (size_t)w * h; ++t)
+        for (int k = 0; k < 3; ++k) out_rgb[3 * t + k] = res[4 * t + k];
 }
 
 }  // extern "C"

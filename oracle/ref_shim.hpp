@@ -205,6 +205,10 @@ auto operator&(const Swz<T, N, A, B, C>& s, S k) { return s.get() & k; }
 
 template <class T> V2<T>& operator+=(V2<T>& a, const V2<T>& b) { a = a + b; return a; }
 template <class T> V3<T>& operator+=(V3<T>& a, const V3<T>& b) { a = a + b; return a; }
+template <class T, int A, int B, int C> V3<T>& operator+=(V3<T>& a, const Swz<T, 3, A, B, C>& b) {
+    a = a + b.get();
+    return a;
+}
 template <class T> V4<T>& operator+=(V4<T>& a, const V4<T>& b) { a = a + b; return a; }
 template <class T, class S> V3<T>& operator*=(V3<T>& a, S s) { a = V3<T>(a * s); return a; }
 
@@ -229,6 +233,7 @@ inline float mod(float x, float y) { return x - y * std::floor(x / y); }
 inline float min(float x, float y) { return y < x ? y : x; }
 inline float max(float x, float y) { return x < y ? y : x; }
 inline float max(float x, int y) { return max(x, float(y)); }
+inline float max(int x, float y) { return max(float(x), y); }
 inline float min(float x, int y) { return min(x, float(y)); }
 inline int min(int x, int y) { return y < x ? y : x; }
 inline float clamp(float x, float a, float b) { return min(max(x, a), b); }
@@ -379,6 +384,25 @@ inline uint imageAtomicMin(UImage2D& im, ivec2 p, uint v) {
     }
     return cur;
 }
+// 1-D images (uimage1D shares UImage2D's storage, one row) and 3-D integer images
+inline uvec4 imageLoad(const UImage2D& im, int i) { return imageLoad(im, ivec2(i, 0)); }
+inline void imageStore(UImage2D& im, int i, uvec4 v) { imageStore(im, ivec2(i, 0), v); }
+inline void imageStore(Image3D& im, ivec3 p, uvec4 v) {
+    if (p.x < 0 || p.y < 0 || p.z < 0 || p.x >= im.w || p.y >= im.h || p.z >= im.d) return;
+    im.u[((size_t)p.z * im.h + p.y) * im.w + p.x] = v.x;
+}
+// atomicAdd on shared variables (a work group's invocations run as fibers on one thread) and on
+// buffer members (work groups run on several threads)
+inline int32_t atomicAdd(int32_t& m, int32_t v) { return __atomic_fetch_add(&m, v, __ATOMIC_RELAXED); }
+inline uint atomicAdd(uint& m, uint v) { return __atomic_fetch_add(&m, v, __ATOMIC_RELAXED); }
+inline uint atomicAdd(uint& m, int32_t v) { return atomicAdd(m, (uint)v); }
+template <class A, class B> bvec2 lessThan(const A& a, const B& b) {
+    const auto x = val(a);
+    const auto y = val(b);
+    return bvec2(x.x < y.x, x.y < y.y);
+}
+inline bool all(bvec2 b) { return b.x && b.y; }
+
 inline ivec2 imageSize(const Image2D& im) { return ivec2(im.w, im.h); }
 inline ivec2 imageSize(const UImage2D& im) { return ivec2(im.w, im.h); }
 inline IntScalar imageSize(const ImageBuffer& im) { return IntScalar{im.n}; }
@@ -428,6 +452,7 @@ extern thread_local std::map<std::string, std::vector<unsigned char>>* tl_shared
 struct RefShaderBase {
     Bindings* B;
     uvec3 gl_WorkGroupID, gl_LocalInvocationID, gl_NumWorkGroups, gl_WorkGroupSize;
+    vec4 gl_FragCoord;  // fragment shaders: the pixel centre the harness runs
     explicit RefShaderBase(Bindings* b) : B(b), gl_NumWorkGroups(b->num_groups), gl_WorkGroupSize(b->local_size) {}
     template <class T> T uni(const char* n) const {
         T v{};
@@ -445,8 +470,10 @@ struct RefShaderBase {
         return static_cast<T*>(it->second);
     }
     template <class T> T* shared_mem(const char* n, size_t count) const {
+        // 64 bytes beyond the declared size: clustering.comp's slice index reaches 16 at the far
+        // plane and writes one past its 16-entry array (the pin's scenes stay in front of it)
         auto& v = (*tl_shared_arena)[n];
-        if (v.size() < count * sizeof(T)) v.resize(count * sizeof(T));
+        if (v.size() < count * sizeof(T) + 64) v.resize(count * sizeof(T) + 64);
         return reinterpret_cast<T*>(v.data());
     }
 };

@@ -94,3 +94,51 @@ def test_final_gathering(case):
                          cfg.interleave)
     assert np.abs(orr).max() > 0
     assert (rr.view(np.uint32) == orr.view(np.uint32)).all()
+
+
+def test_clustered_culling_lists(case):
+    """clustering.comp + light_lists.comp against the restatement (O.cluster_lights) on CREF: the
+    same used clusters, and in each cluster's sub-list s the same VPLs of [64 s, 64 s + 64), as
+    sets (the reference's list order is atomic order). A sub-list that keeps all 64 VPLs loses its
+    last entry to the next sub-list's count slot (light_lists.comp:117-126), so for such lists the
+    reference's 63 entries must be a subset of the restatement's 64."""
+    cfg, sc, perm = case
+    op, _, _, opn = O.vpl_process(sc.rsm_depth, sc.rsm_normal, sc.rsm_diffuse, cfg.n_vpl,
+                                  sc.mat("inv_biased_light_vp"), cfg.light_intensity, 1, perm)
+    a, b = mlgi.depth_terms(sc)
+    packed = np.concatenate([op, opn.view(np.float32)[:, None]], 1)
+    xyz, lists = R.cluster_lights(sc.gbuf_depth, sc.mat("inv_view_proj"), a, b, cfg.z_far, packed)
+    used, masks, _ = O.cluster_lights(sc.gbuf_depth, sc.mat("inv_view_proj"), a, b, cfg.z_far, op, opn, cfg.n_vpl)
+    ncx = (cfg.width + 127) // 128
+    ours = {(t % ncx, t // ncx, s) for t in range(len(used)) for s in range(16) if (int(used[t]) >> s) & 1}
+    assert set(xyz) == ours and len(xyz) == len(ours) > 0
+    full = partial = 0
+    for (x, y, s_), col in zip(xyz, lists):
+        row = masks[(y * ncx + x) * 16 + s_]
+        for sub in range(16):
+            mine = {k for k in range(64 * sub, 64 * sub + 64) if (int(row[k // 32]) >> (k % 32)) & 1}
+            n = int(col[64 * sub]) - 1
+            ref = {int(v) for v in col[64 * sub + 1: 64 * sub + 1 + min(n, 63)]}
+            assert n == len(mine), (x, y, s_, sub)
+            if n <= 63:
+                assert ref == mine, (x, y, s_, sub)
+                partial += 1
+            else:
+                assert ref <= mine and len(ref) == 63, (x, y, s_, sub)
+                full += 1
+    assert partial > 0
+
+
+def test_gi_blur(case):
+    """gi_blur.frag's X and Y programs against the restatement, with the normals in the reference's
+    RGB G-buffer format on both sides; bit for bit away from the image border, where the shader's
+    texelFetch outside the image is undefined and the restatement skips the sample."""
+    cfg, sc, perm = case
+    a, b = mlgi.depth_terms(sc)
+    rgb = octahedral_to_rgb(sc.gbuf_normal)
+    gi = np.random.default_rng(3).random((cfg.height, cfg.width, 3)).astype(np.float32)
+    rr = R.gi_blur(sc.gbuf_depth, rgb, gi, a, b)
+    orr = O.gi_blur_rgb_normals(sc.gbuf_depth, rgb, gi, a, b)
+    inner = (slice(3, cfg.height - 3), slice(3, cfg.width - 3))
+    assert (rr[inner].view(np.uint32) == orr[inner].view(np.uint32)).all()
+    assert np.abs(rr[inner] - gi[inner]).max() > 1e-3  # the filter did change the image
