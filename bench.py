@@ -130,7 +130,7 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
@@ -167,8 +167,10 @@ class ClockSampler:
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower().startswith("active")})
+        busy = [float(r[9]) for r in rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows),
+                "gpu_busy_pct": statistics.median(busy) if busy else None}
 
 
 # ---- CPU implementation of the path (the oracle's FP32 restatement, all host threads) -----------
@@ -639,12 +641,18 @@ def measure_serve(local_rank, slots, rate, duration, seed):
     sv.run_poisson(shapes, rate_hz=rate, duration_s=min(1.0, duration), seed=seed + 1)
 
     def stream(r, sd, plain):
+        # nvidia-smi's utilization.gpu during the stream: the share of each sample period in which a
+        # kernel ran (how busy the plain arm alone keeps the GPU)
+        busy = ClockSampler(local_rank)
+        busy.start()
         c, wall = sv.run_poisson(shapes, rate_hz=r, duration_s=duration, seed=sd, plain=plain)
+        b = busy.stop()
         ok = c["status"] == mlgi.OK
         lat = c["latency_ms"][ok]
         return {"rate_hz": r, "requests": int(len(c)), "ok": int(ok.sum()), "wall_s": wall,
                 "frames_per_s": float(ok.sum() / wall), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_queue_ms": float(c["queue_ms"][ok].mean()),
+                "gpu_busy_pct": b.get("gpu_busy_pct") if b else None,
                 "digests": {int(i): int(d) for i, d in zip(c["id"], c["digest"])}}
 
     runs = {"served": stream(rate, seed, False), "plain": stream(rate, seed, True)}
