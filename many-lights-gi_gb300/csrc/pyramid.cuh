@@ -432,7 +432,9 @@ __device__ __forceinline__ void pyramid_ism(const PullPushArgs& a, const int ism
 
 // Threads per block: kPyrBigThreads for ISM edges above 64 (two blocks per SM, as their shared
 // memory allows; 384 threads leave 80 registers a thread, measured at C2: 0.256 ms against 0.274 ms
-// with 512 threads at 64 registers and 0.276 ms with 256), kPyrSmallThreads for smaller ones.
+// with 512 threads at 64 registers and 0.276 ms with 256), kPyrSmallThreads for smaller ones with
+// at least three blocks per SM (85 registers: 64^2 ISMs in 0.0945 ms against 0.0955 with four
+// blocks at 64 registers and 0.108 with two).
 constexpr int kPyrBigThreads = 384, kPyrSmallThreads = 256;
 
 template <int NT, int kMinBlocks>
@@ -450,7 +452,7 @@ static cudaError_t pyramid_prepare() {
     cudaError_t e = cudaFuncSetAttribute(pyramid_kernel<kPyrBigThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kPyramidSmemMax);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(pyramid_kernel<kPyrSmallThreads, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(pyramid_kernel<kPyrSmallThreads, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kPyramidSmemMax);
     if (e == cudaSuccess && dev >= 0 && dev < kMaxDevices) done[dev] = true;
     return e;
@@ -462,5 +464,5 @@ static void launch_pyramid(const PullPushArgs& a, cudaStream_t s) {
     if (a.ism_size > 64)
         pyramid_kernel<kPyrBigThreads, 2><<<isms, kPyrBigThreads, smem, s>>>(a);
     else
-        pyramid_kernel<kPyrSmallThreads, 4><<<isms, kPyrSmallThreads, smem, s>>>(a);
+        pyramid_kernel<kPyrSmallThreads, 3><<<isms, kPyrSmallThreads, smem, s>>>(a);
 }
