@@ -174,8 +174,8 @@ int mlgi_pullpush_launches(const mlgi_ism_params* params);
  * allocate device memory (their device memory is reserved up front by another allocator, or
  * they run in a plugin or callback that is only handed pre-allocated buffers): clears, splats
  * and pull-pushes like mlgi_ism_splat + mlgi_pullpush, but keeps its intermediates (the key
- * atlas and pull-push pyramid levels 1 and 2) in fixed device arrays inside the library instead
- * of allocating them. Needs no context; runs on
+ * atlas and pull-push pyramid levels 1 and 2, the latter used only when an ISM's pyramid does not
+ * run in one block) in fixed device arrays inside the library instead of allocating them. Needs no context; runs on
  * the current device and on `stream` (NULL = the legacy default stream).
  *   - Atlas limit: grid_x*ism_size * grid_y*ism_size <= 1,048,576 texels (e.g. 1024 x 1024);
  *     larger atlases, and any geometry mlgi_ism_splat refuses, return MLGI_EINVAL.

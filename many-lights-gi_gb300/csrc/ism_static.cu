@@ -5,7 +5,9 @@
 // process whose device memory is fully reserved up front by another allocator, a plugin that is
 // only handed pre-allocated buffers, or a callback that runs while the CUDA allocator is locked.
 // Such callers still pass their own input (points, VPLs) and output (final depth atlas) buffers;
-// only the intermediates -- the key atlas and pull-push pyramid levels 1 and 2 -- live here.
+// only the intermediates -- the key atlas and pull-push pyramid levels 1 and 2 -- live here. (The
+// pyramid levels are used only by the per-level pull-push form; where an ISM's pyramid runs in
+// one block, its levels stay in that block's shared memory.)
 //
 // Limits and behaviour:
 //   * The key atlas holds at most kStaticKeyTexels = 1,048,576 texels (a 1024 x 1024 atlas,
