@@ -287,16 +287,23 @@ __device__ __forceinline__ float vpl_influence_r2(const v3 f, const float cutoff
     return r * r;
 }
 
-// Per-tile culling of one VPL against the box [bmin, bmax] of the tile's world positions: its
-// front half-space against the box corner farthest along its normal, then the box's squared
-// distance against the influence radius r2 (vpl_influence_r2).
-__device__ __forceinline__ bool vpl_keep(const v3 p, const v3 n, const float r2, const v3 bmin, const v3 bmax) {
+// Culling of one VPL against a box [bmin, bmax] of world positions. vpl_front: the VPL's front
+// half-space reaches the box corner farthest along its normal (with a -1e-3 margin, so a VPL it
+// drops has a negative cosine at every position in the box: it adds exactly nothing there).
+// vpl_near: the box's squared distance is within the influence radius r2 (vpl_influence_r2).
+__device__ __forceinline__ bool vpl_front(const v3 p, const v3 n, const v3 bmin, const v3 bmax) {
     const v3 sup = mk(n.x > 0.f ? bmax.x : bmin.x, n.y > 0.f ? bmax.y : bmin.y, n.z > 0.f ? bmax.z : bmin.z);
-    if (dot(n, sup - p) < -1e-3f) return false;
+    return !(dot(n, sup - p) < -1e-3f);
+}
+__device__ __forceinline__ bool vpl_near(const v3 p, const float r2, const v3 bmin, const v3 bmax) {
     const v3 q = mk(fminf(fmaxf(p.x, bmin.x), bmax.x), fminf(fmaxf(p.y, bmin.y), bmax.y),
                     fminf(fmaxf(p.z, bmin.z), bmax.z));
     const v3 dq = q - p;
     return !(dot(dq, dq) > r2);
+}
+// Per-tile culling: both tests against the tile's box.
+__device__ __forceinline__ bool vpl_keep(const v3 p, const v3 n, const float r2, const v3 bmin, const v3 bmax) {
+    return vpl_front(p, n, bmin, bmax) && vpl_near(p, r2, bmin, bmax);
 }
 
 // Pixel (x, y) of the G-buffer: window depth and decoded octahedral normal (a pixel outside the
@@ -322,19 +329,34 @@ __device__ __forceinline__ void fg_pixel_setup(const FgArgs& a, const int x, con
     fn = oct_decode(ex, ey);
 }
 
-// World-space bounding box of a block's pixels (both of each thread's, the valid ones), through
-// `box` (6 x NW floats of shared memory) and one barrier.
-template <int NW>
-__device__ __forceinline__ void fg_tile_box(const v3 w0, const v3 w1, const bool v0, const bool v1,
-                                            float (&box)[6][NW], v3& bmin, v3& bmax) {
+// World-space bounding box of a warp's pixels (both of each thread's, the valid ones) as six
+// minima (x, y, z, -x, -y, -z), in every lane.
+__device__ __forceinline__ void fg_warp_box(const v3 w0, const v3 w1, const bool v0, const bool v1, float (&b)[6]) {
     const float inf = __int_as_float(0x7f800000);
-    float b[6] = {fminf(v0 ? w0.x : inf, v1 ? w1.x : inf),   fminf(v0 ? w0.y : inf, v1 ? w1.y : inf),
-                  fminf(v0 ? w0.z : inf, v1 ? w1.z : inf),   fminf(v0 ? -w0.x : inf, v1 ? -w1.x : inf),
-                  fminf(v0 ? -w0.y : inf, v1 ? -w1.y : inf), fminf(v0 ? -w0.z : inf, v1 ? -w1.z : inf)};
+    b[0] = fminf(v0 ? w0.x : inf, v1 ? w1.x : inf);
+    b[1] = fminf(v0 ? w0.y : inf, v1 ? w1.y : inf);
+    b[2] = fminf(v0 ? w0.z : inf, v1 ? w1.z : inf);
+    b[3] = fminf(v0 ? -w0.x : inf, v1 ? -w1.x : inf);
+    b[4] = fminf(v0 ? -w0.y : inf, v1 ? -w1.y : inf);
+    b[5] = fminf(v0 ? -w0.z : inf, v1 ? -w1.z : inf);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) b[k] = fminf(b[k], __shfl_xor_sync(0xffffffffu, b[k], o));
+    }
+}
+
+// World-space bounding box of a block's pixels, through `box` (6 x NW floats of shared memory)
+// and one barrier; wmin/wmax (optional) receive the calling warp's own box.
+template <int NW>
+__device__ __forceinline__ void fg_tile_box(const v3 w0, const v3 w1, const bool v0, const bool v1,
+                                            float (&box)[6][NW], v3& bmin, v3& bmax, v3* wmin = nullptr,
+                                            v3* wmax = nullptr) {
+    float b[6];
+    fg_warp_box(w0, w1, v0, v1, b);
+    if (wmin) {
+        *wmin = mk(b[0], b[1], b[2]);
+        *wmax = mk(-b[3], -b[4], -b[5]);
     }
     if ((threadIdx.x & 31) == 0)
 #pragma unroll
@@ -741,12 +763,16 @@ __global__ void __launch_bounds__(128, 8) fg_class_kernel(FgArgs a, int tile_beg
         if (!v1) w1 = mk(0.f, 0.f, 0.f);
         unsigned m0 = 0xFFFFFFFFu, m1 = 0xFFFFFFFFu;
         if (a.cull == 1) {
-            v3 bmin, bmax;
-            fg_tile_box<NW>(w0, w1, v0, v1, S.box[it & 1], bmin, bmax);
+            // the half-space test against the warp's own box (a VPL it drops adds exactly nothing
+            // to any of the warp's pixels, so the radiance is the per-tile cull's bit for bit), the
+            // influence test against the tile's box (the culling rule the oracle restates)
+            v3 bmin, bmax, wmin, wmax;
+            fg_tile_box<NW>(w0, w1, v0, v1, S.box[it & 1], bmin, bmax, &wmin, &wmax);
             auto keep = [&](const int k) {
                 if (k >= cnt) return false;
                 const float4 cp = S.cp[k], cn = S.cn[k];
-                return vpl_keep(mk(cp.x, cp.y, cp.z), mk(cn.x, cn.y, cn.z), cp.w, bmin, bmax);
+                const v3 p = mk(cp.x, cp.y, cp.z);
+                return vpl_front(p, mk(cn.x, cn.y, cn.z), wmin, wmax) && vpl_near(p, cp.w, bmin, bmax);
             };
             m0 = __ballot_sync(0xffffffffu, keep(lane));
             m1 = cnt > 32 ? __ballot_sync(0xffffffffu, keep(32 + lane)) : 0u;
