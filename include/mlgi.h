@@ -40,6 +40,7 @@ typedef int32_t mlgi_status;
 #define MLGI_ETIMEDOUT 3   /* a bounded device-side wait gave up */
 #define MLGI_ECUDA 4       /* a CUDA runtime call failed */
 #define MLGI_ECANCELED 5   /* a queued request was cancelled */
+#define MLGI_EBOUNDS 6     /* bounds-checked library only: a kernel computed an index outside its buffer */
 
 typedef struct mlgi_ctx mlgi_ctx;
 typedef void* mlgi_stream; /* a cudaStream_t; NULL selects the context's stream */
@@ -500,8 +501,30 @@ mlgi_status mlgi_set_timing(mlgi_ctx* ctx, int enabled);
 mlgi_status mlgi_last_timings(mlgi_ctx* ctx, float* ms, int n);
 
 /* Synchronise `stream` and report device-side errors recorded since the last check
- * (MLGI_ETIMEDOUT when a bounded wait inside a kernel gave up). Clears the error word. */
+ * (MLGI_ETIMEDOUT when a bounded wait inside a kernel gave up). Clears the error word. In the
+ * bounds-checked library it first synchronises the device and reports MLGI_EBOUNDS when any
+ * kernel of the process met an index outside its buffer since the last check (mlgi_last_error
+ * names the source line and the index); those records are cleared too. */
 mlgi_status mlgi_check_device_status(mlgi_ctx* ctx, mlgi_stream stream);
+
+/* No counterpart in the reference (its only error handling is ModelLoadingStage.cpp:92-97): the
+ * allocation-failure hook. With after >= 0 the library's next `after` device or pinned host
+ * allocations succeed and every later one fails as out of memory, without asking CUDA, until the
+ * hook is reset with -1 (the default). Calls whose allocation fails return MLGI_ENOMEM and leave
+ * their context usable; a server request whose room cannot be allocated completes with
+ * MLGI_ENOMEM. Process-wide; for tests. */
+mlgi_status mlgi_set_alloc_fault(int64_t after);
+
+/* The bounds-checked library, libmlgi_checked.so, is this library built with -DMLGI_CHECKS: its
+ * kernels check the indices they compute against the extents of the buffers they address, record
+ * the first one outside (its source line and value, per translation unit), and use index 0 in its
+ * place, so that the access stays inside the buffer. 1 in that library, 0 in the normal one. */
+int mlgi_checks_enabled(void);
+/* Test of the checks themselves: reads element `index` of a device array of `extent` >= 1 floats
+ * through a checked index. In the checked library an index outside [0, extent) is recorded (the
+ * read goes to element 0) and mlgi_check_device_status then reports MLGI_EBOUNDS; the normal
+ * library, whose index is unchecked, refuses it with MLGI_EINVAL and launches nothing. */
+mlgi_status mlgi_check_index_selftest(mlgi_ctx* ctx, int64_t index, int64_t extent);
 /* No counterpart in the reference: exercises the bounded device wait. The gathering stages each
  * VPL slice with a bulk copy completed on an mbarrier, and waits for it at most `wait_cycles` SM
  * cycles (0 restores the default, about 2^31; else 1000..2^31). A nonzero `extra_tx_bytes` (test

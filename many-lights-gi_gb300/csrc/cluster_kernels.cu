@@ -18,6 +18,7 @@
 // shaders' FP32 operation order word for word.
 #include <cuda_runtime.h>
 
+#include "checks.cuh"
 #include "gi_device.cuh"
 #include "kernels.h"
 
@@ -52,7 +53,7 @@ __global__ void __launch_bounds__(kClusterPixels) cluster_mark_kernel(ClusterArg
     for (int r = 0; r < kMarkRows; ++r) {
         const int y = blockIdx.y * kMarkRows + r;
         if (x < a.width && y < a.height) {
-            const size_t p = (size_t)y * a.width + x;
+            const size_t p = MLGI_IX((size_t)y * a.width + x, (size_t)a.width * a.height);
             const int slice = depth_slice(linear_depth(__ldg(a.depth + p), a.proj_a, a.proj_b), a.scale);
             a.pixel_slice[p] = (uint8_t)slice;
             bits |= 1u << slice;
@@ -65,7 +66,7 @@ __global__ void __launch_bounds__(kClusterPixels) cluster_mark_kernel(ClusterArg
     if (threadIdx.x == 0) {
         uint32_t v = 0;
         for (int w = 0; w < kClusterPixels / 32; ++w) v |= s_bits[w];
-        if (v) atomicOr(a.used + (blockIdx.y * kMarkRows / kClusterPixels) * a.tiles_x + blockIdx.x, v);
+        if (v) atomicOr(a.used + MLGI_IX((blockIdx.y * kMarkRows / kClusterPixels) * a.tiles_x + blockIdx.x, a.tiles_x * a.tiles_y), v);
     }
 }
 
@@ -78,7 +79,7 @@ __device__ __forceinline__ float slice_to_z(int slice, float scale) {
 // One block per cluster (tile-major, 16 slices per tile); each warp takes 32 consecutive VPLs and
 // writes their keep bits as one mask word.
 __global__ void __launch_bounds__(128) cluster_lists_kernel(ClusterArgs a) {
-    const int cl = blockIdx.x;
+    const int cl = MLGI_IX((int)blockIdx.x, a.tiles_x * a.tiles_y * kClusterSlices);
     const int tile = cl / kClusterSlices, slice = cl - tile * kClusterSlices;
     if (!((__ldg(a.used + tile) >> slice) & 1u)) return;  // unused: never read
     const int cx = tile % a.tiles_x, cy = tile / a.tiles_x;
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(128) cluster_lists_kernel(ClusterArgs a) {
         const int v = base + (threadIdx.x & 31);
         bool found = false;
         if (v < a.n_vpl) {
-            const float4 pk = __ldg(a.packed + v);
+            const float4 pk = __ldg(a.packed + MLGI_IX(v, a.n_vpl));
             const v3 n = unpack3SN(__float_as_uint(pk.w));
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(128) cluster_lists_kernel(ClusterArgs a) {
             }
         }
         const unsigned bits = __ballot_sync(0xffffffffu, found);
-        if ((threadIdx.x & 31) == 0) mask[base >> 5] = bits;
+        if ((threadIdx.x & 31) == 0) mask[MLGI_IX(base >> 5, a.mask_words)] = bits;
     }
 }
 
@@ -133,3 +134,5 @@ cudaError_t launch_cluster_lights(const ClusterArgs& a, cudaStream_t s) {
 }
 
 }  // namespace mlgi
+
+MLGI_CHECK_UNIT(cluster_kernels)

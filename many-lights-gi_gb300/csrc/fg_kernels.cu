@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "batch_items.cuh"
+#include "checks.cuh"
 #include "gi_device.cuh"
 #include "kernels.h"
 
@@ -314,7 +315,7 @@ __device__ __forceinline__ void fg_pixel_setup(const FgArgs& a, const int x, con
     d = 0.5f;
     fn = mk(0.f, 0.f, 1.f);
     if (!valid) return;
-    const size_t pix = (size_t)y * a.width + x;
+    const size_t pix = MLGI_IX((size_t)y * a.width + x, (size_t)a.width * a.height);
     d = __ldg(a.depth + pix);
     float ex, ey;
     if (kNormalF16) {
@@ -476,8 +477,9 @@ struct GatherPair {
     }
 
     __device__ __forceinline__ float occluder(const uint32_t t) const {
-        return kAtlasF16 ? __half2float(__ldg(reinterpret_cast<const __half*>(atlas) + t))
-                         : __ldg(reinterpret_cast<const float*>(atlas) + t);
+        const uint32_t i = MLGI_IX(t, (uint32_t)aw * (uint32_t)ah);
+        return kAtlasF16 ? __half2float(__ldg(reinterpret_cast<const __half*>(atlas) + i))
+                         : __ldg(reinterpret_cast<const float*>(atlas) + i);
     }
 
     // acc += flux * G * smoothstep(0.98, 1, 1 - (vz - occ)) for both pixels
@@ -541,13 +543,13 @@ struct GatherPair {
         split(accy, ay0, ay1);
         split(accz, az0, az1);
         if (v0) {
-            const size_t pix = (size_t)y * a.width + x0;
+            const size_t pix = MLGI_IX((size_t)y * a.width + x0, (size_t)a.width * a.height);
             a.out[3 * pix + 0] = ax0 * a.gi_scale;
             a.out[3 * pix + 1] = ay0 * a.gi_scale;
             a.out[3 * pix + 2] = az0 * a.gi_scale;
         }
         if (v1) {
-            const size_t pix = (size_t)y * a.width + x1;
+            const size_t pix = MLGI_IX((size_t)y * a.width + x1, (size_t)a.width * a.height);
             a.out[3 * pix + 0] = ax1 * a.gi_scale;
             a.out[3 * pix + 1] = ay1 * a.gi_scale;
             a.out[3 * pix + 2] = az1 * a.gi_scale;
@@ -568,6 +570,10 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
     const int I = a.interleave;
     const int cx = c % I, cy = c / I;
     const int vbase = c * a.per_class;
+    // checked build: a class slice outside the VPL buffer or a chunk larger than the staging
+    // buffer skips the tile (block-uniform, before any copy is issued)
+    if (!MLGI_RANGE_OK(vbase, a.per_class, a.n_vpl) || !MLGI_RANGE_OK(0, (size_t)min(kChunk, a.per_class) * kRec, sizeof(S.raw)))
+        return true;
     const bool use_tma = ((size_t)vbase * kRec) % 16 == 0;
     const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
     const size_t bytes0 = (size_t)min(kChunk, a.per_class) * kRec;
@@ -591,7 +597,7 @@ __device__ __forceinline__ bool fg_tile(const FgArgs& a, const int tile, const i
         fg_pixel_setup<kNormalF16>(a, x, y, valid, d, fn);
         cl_row = nullptr;
         if (valid && kClusters && a.cull == 2) {
-            const size_t pix = (size_t)y * a.width + x;
+            const size_t pix = MLGI_IX((size_t)y * a.width + x, (size_t)a.width * a.height);
             const int cluster = ((y / kClusterPixels) * a.cl_tiles_x + x / kClusterPixels) * kClusterSlices + a.cl_slice[pix];
             cl_row = a.cl_masks + (size_t)cluster * a.cl_words;
         }
@@ -715,6 +721,9 @@ __global__ void __launch_bounds__(128, 8) fg_class_kernel(FgArgs a, int tile_beg
     const float hs = float(a.ism_size) * 0.5f;
     const unsigned char* src = kReduced ? a.reduced : reinterpret_cast<const unsigned char*>(a.vpl);
     const size_t bytes = (size_t)cnt * kRec;
+    // checked build: a class slice outside the VPL buffer or larger than the staging buffer skips
+    // the block (block-uniform, before any copy is issued)
+    if (!MLGI_RANGE_OK(vbase, cnt, a.n_vpl) || !MLGI_RANGE_OK(0, bytes, sizeof(S.raw))) return;
     const bool use_tma = ((size_t)vbase * kRec) % 16 == 0 && bytes % 16 == 0;
     if (tid == 0) {
         mbar_init(&S.bar, 1);
@@ -905,3 +914,5 @@ cudaError_t launch_batch_fg(const BatchTable& t, int pass, int grid, cudaStream_
 }
 
 }  // namespace mlgi
+
+MLGI_CHECK_UNIT(fg_kernels)

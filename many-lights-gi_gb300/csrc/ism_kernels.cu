@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "batch_items.cuh"
+#include "checks.cuh"
 #include "gi_device.cuh"
 #include "kernels.h"
 
@@ -30,7 +31,7 @@ __device__ __forceinline__ void vpl_one(const VplArgs& a, const uint32_t idx) {
     uint32_t nb = 0;
     float d = 0.f;
     if (tcx < (uint32_t)a.rsm_w && tcy < (uint32_t)a.rsm_h) {  // texelFetch out of range reads zero
-        const size_t t = (size_t)tcy * a.rsm_w + tcx;
+        const size_t t = MLGI_IX((size_t)tcy * a.rsm_w + tcx, (size_t)a.rsm_w * a.rsm_h);
         const uint32_t dw = __ldg(a.diffuse + t);
         diffuse = mk(float(dw & 0xFFu) / 255.0f, float((dw >> 8) & 0xFFu) / 255.0f, float((dw >> 16) & 0xFFu) / 255.0f);
         nb = __ldg(a.normal + t);
@@ -45,7 +46,7 @@ __device__ __forceinline__ void vpl_one(const VplArgs& a, const uint32_t idx) {
     for (int r = 0; r < 4; ++r) w4[r] = ((m[r] * tfx + m[4 + r] * tfy) + m[8 + r] * d) + m[12 + r] * 1.0f;
     const v3 pos = mk(w4[0] / w4[3], w4[1] / w4[3], w4[2] / w4[3]);
     const v3 color = diffuse * a.intensity;
-    const uint32_t ri = a.perm ? (uint32_t)__ldg(a.perm + idx) : idx;
+    const uint32_t ri = MLGI_IX(a.perm ? (uint32_t)__ldg(a.perm + idx) : idx, (uint32_t)a.n);
     const uint32_t pn = pack3SN(normal);
     const v3 un = unpack3SN(pn);
     a.vpl[3 * ri + 0] = make_float4(pos.x, pos.y, pos.z, 0.f);
@@ -139,7 +140,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             index %= vplCount;
             index += a.vpl_start;
         }
-        const float4 pk = a.packed[index];
+        const float4 pk = a.packed[MLGI_IX(index, a.n_vpl)];
         const v3 n = unpack3SN(__float_as_uint(pk.w));
         v3 s, u;
         look_at_rows(n, s, u);
@@ -165,10 +166,10 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
     // the count stops one past the buffer's entries; that also bounds the block's work.
     const int64_t in_buffer = max((int64_t)0, a.n_entries - (int64_t)wg * a.bucket_stride);
     const uint32_t avail = (uint32_t)min(in_buffer, (int64_t)0xFFFFFFFE);
-    uint32_t count = __ldg(a.counts + wg);  // the last chunk takes any points beyond the stride
+    // the last chunk takes any points beyond the stride (the counts hold at least the launch's buckets)
+    uint32_t count = __ldg(a.counts + MLGI_IX(wg, a.bucket0 + a.n_groups));
     if (count > avail) count = avail + 1;
     const uint32_t cnt = chunk == a.chunks - 1 ? count : min(count, first + kSplatChunk);
-    const float4* bucket = a.points + (int64_t)wg * a.bucket_stride;
     const float fw = float(a.atlas_w), fh = float(a.atlas_h), fgx = float(a.gx), fgy = float(a.gy);
     const float rgx = pow2_recip(a.gx), rgy = pow2_recip(a.gy);
     // per-task parameters in registers (a may live in shared memory in the batched form)
@@ -187,12 +188,12 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         const uint32_t tw = __float_as_uint(task.w);
         const int i = (int)(tw >> 8);
         const uint32_t rbyte = tw & 0xFFu;
-        const float4 vp = S.pos[i], vn = S.n[i];
+        const float4 vp = S.pos[MLGI_IX(i, 16)], vn = S.n[MLGI_IX(i, 16)];
         const v3 rel = mk(task.x, task.y, task.z) - mk(vp.x, vp.y, vp.z);
         // paraboloid_project(rel, length(rel), n, zFar, ismIndex, grid, preserveSign = true)
         const float dist = length(rel);
         const v3 n = mk(vn.x, vn.y, vn.z);
-        const float4 vs = S.s[i], vu = S.u[i];
+        const float4 vs = S.s[MLGI_IX(i, 16)], vu = S.u[MLGI_IX(i, 16)];
         float vx = dot(mk(vs.x, vs.y, vs.z), rel);
         float vy = dot(mk(vu.x, vu.y, vu.z), rel);
         float vz = ((-n.x) * rel.x + (-n.y) * rel.y) + (-n.z) * rel.z;
@@ -220,7 +221,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         if (kCount)
             ++issued;
         else
-            atomicMin(keys + (size_t)py * atlas_w + px, key);
+            atomicMin(keys + MLGI_IX((size_t)py * atlas_w + px, (size_t)atlas_w * atlas_h), key);
     };
     for (uint32_t base = first + threadIdx.x - lane; base < cnt; base += kSplatThreads) {
         const uint32_t j = base + lane;
@@ -228,7 +229,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         int found = 0;
         uint32_t used = 0;
         if (j < cnt) {
-            if (j < avail) pt = __ldg(bucket + j);  // else the zero point
+            if (j < avail) pt = __ldg(a.points + MLGI_IX((int64_t)wg * a.bucket_stride + j, a.n_entries));  // else the zero point
             const v3 position = mk(pt.x, pt.y, pt.z);
             const uint32_t nr = __float_as_uint(pt.w);
             const v3 pn = mk(S.unorm[nr & 0xFFu], S.unorm[(nr >> 8) & 0xFFu], S.unorm[(nr >> 16) & 0xFFu]);
@@ -257,7 +258,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         if (found > 0) {
             const uint32_t rbyte = S.rbyte[__float_as_uint(pt.w) >> 24];
             for (int k = 0; k < found; ++k)
-                tasks[pending + pre + k] =
+                tasks[MLGI_IX(pending + pre + k, kSplatTaskCap)] =
                     make_float4(pt.x, pt.y, pt.z, __uint_as_float((((used >> (4 * k)) & 15u) << 8) | rbyte));
         }
         pending += total;
@@ -438,8 +439,9 @@ __device__ constexpr int kPullOff[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};
 // of a key sample is exactly (+-0.25, +-0.25) (dx = dy = 0 at level 0).
 __device__ __forceinline__ float4 pull1_texel(const PullPushArgs& a, const float* s_rad, const float* s_mdo,
                                               const int gox, const int goy) {
-    const uint2 r0 = __ldg(reinterpret_cast<const uint2*>(a.keys + (size_t)(2 * goy) * a.atlas_w + 2 * gox));
-    const uint2 r1 = __ldg(reinterpret_cast<const uint2*>(a.keys + (size_t)(2 * goy + 1) * a.atlas_w + 2 * gox));
+    const size_t nk = (size_t)a.atlas_w * a.atlas_h - 1;  // a pair's first key
+    const uint2 r0 = __ldg(reinterpret_cast<const uint2*>(a.keys + MLGI_IX((size_t)(2 * goy) * a.atlas_w + 2 * gox, nk)));
+    const uint2 r1 = __ldg(reinterpret_cast<const uint2*>(a.keys + MLGI_IX((size_t)(2 * goy + 1) * a.atlas_w + 2 * gox, nk)));
     const uint32_t key[4] = {r0.x, r1.x, r0.y, r1.y};  // (0,0), (0,1), (1,0), (1,1)
     const float fs = float(a.ism_size);
     PullSample q[4];
@@ -459,15 +461,15 @@ __device__ __forceinline__ float4 pull1_texel(const PullPushArgs& a, const float
     return pull_combine(q, 0.5f, sqrtf(0.125f));
 }
 
-// Pull level l >= 2 at global level-l texel (gox, goy); `in` is level l-1 with row pitch `pin`
-// and origin (ix0, iy0) in global level-(l-1) coordinates.
-__device__ __forceinline__ float4 pull_texel(const float4* in, const int pin, const int ix0, const int iy0,
-                                             const int gox, const int goy, const float scale) {
+// Pull level l >= 2 at global level-l texel (gox, goy); `in` is level l-1 (n texels) with row
+// pitch `pin` and origin (ix0, iy0) in global level-(l-1) coordinates.
+__device__ __forceinline__ float4 pull_texel(const float4* in, const size_t n, const int pin, const int ix0,
+                                             const int iy0, const int gox, const int goy, const float scale) {
     PullSample q[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int gix = 2 * gox + kPullOff[k][0], giy = 2 * goy + kPullOff[k][1];
-        const float4 t = in[(giy - iy0) * pin + (gix - ix0)];
+        const float4 t = in[MLGI_IX((giy - iy0) * pin + (gix - ix0), n)];
         const float2 d = unpack_half2(__float_as_uint(t.w));
         q[k].depth = t.x;
         q[k].maxDepth = t.y;
@@ -577,7 +579,7 @@ __device__ __forceinline__ void push_coarse(const float4* c, const int pc, const
         // coordinates off the level are clamped: such texels are never inside an output's ISM
         const int cx = min(max(gx - 1 + kPushOff[k][0], 0), cw - 1);
         const int cy = min(max(gy - 1 + kPushOff[k][1], 0), ch - 1);
-        const float4 t = c[(uint32_t)cy * (uint32_t)pc + (uint32_t)cx];
+        const float4 t = c[MLGI_IX((uint32_t)cy * (uint32_t)pc + (uint32_t)cx, (uint32_t)pc * (uint32_t)ch)];
         const float2 d = unpack_half2(__float_as_uint(t.w));
         C.depth[k] = t.x;
         C.maxDepth[k] = t.y;
@@ -667,7 +669,8 @@ __device__ __forceinline__ void pull1_tile(const PullPushArgs& a, const int tx, 
     const int s1 = a.ism_size >> 1;
     const int x = tx * kPpTileW + (threadIdx.x % kPpTileW), y = a.row0 * s1 + ty * kPpTileH + (threadIdx.x / kPpTileW);
     const int w1 = a.atlas_w >> 1;
-    if (x < w1 && y < a.row1 * s1) a.lv1[(uint32_t)y * w1 + x] = pull1_texel(a, s_rad, s_mdo, x, y);
+    if (x < w1 && y < a.row1 * s1)
+        a.lv1[MLGI_IX((uint32_t)y * w1 + x, (uint32_t)w1 * (a.atlas_h >> 1))] = pull1_texel(a, s_rad, s_mdo, x, y);
 }
 
 // Quad passes on a kPpTileW x kPpTileH tile (tx, ty) of quads: level l has (w_l / 2 + 1) x
@@ -686,15 +689,17 @@ __device__ __forceinline__ void push1_quads(const PullPushArgs& a, const int tx,
     const bool bx = multiple_of(gx, sc, a.m_c1), by = multiple_of(gy, sc, a.m_c1);
     const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
     const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w1, oky0 = y0 >= Y0, oky1 = y0 + 1 < Y1;
-    float4* row0 = a.lv1 + (uint32_t)max(y0, 0) * w1;  // only used when oky0
-    float4* row1 = a.lv1 + (uint32_t)min(y0 + 1, h1 - 1) * w1;  // only used when oky1
-    if (oky0 && okx0) row0[x0] = push_output<true, 0, 0>(C, bx, by, row0[x0]);
-    if (oky0 && okx1) row0[x0 + 1] = push_output<true, 1, 0>(C, bx, by, row0[x0 + 1]);
-    if (oky1 && okx0) row1[x0] = push_output<true, 0, 1>(C, bx, by, row1[x0]);
-    if (oky1 && okx1) row1[x0 + 1] = push_output<true, 1, 1>(C, bx, by, row1[x0 + 1]);
+    const uint32_t n1 = (uint32_t)w1 * h1;
+    const uint32_t o0 = (uint32_t)max(y0, 0) * w1 + x0, o1 = (uint32_t)min(y0 + 1, h1 - 1) * w1 + x0;  // x0 < 0: unused
+    float4* lv1 = a.lv1;
+    if (oky0 && okx0) lv1[MLGI_IX(o0, n1)] = push_output<true, 0, 0>(C, bx, by, lv1[MLGI_IX(o0, n1)]);
+    if (oky0 && okx1) lv1[MLGI_IX(o0 + 1, n1)] = push_output<true, 1, 0>(C, bx, by, lv1[MLGI_IX(o0 + 1, n1)]);
+    if (oky1 && okx0) lv1[MLGI_IX(o1, n1)] = push_output<true, 0, 1>(C, bx, by, lv1[MLGI_IX(o1, n1)]);
+    if (oky1 && okx1) lv1[MLGI_IX(o1 + 1, n1)] = push_output<true, 1, 1>(C, bx, by, lv1[MLGI_IX(o1 + 1, n1)]);
 }
 
-__device__ __forceinline__ void store_depth(const PullPushArgs& a, const uint32_t o, const float d) {
+__device__ __forceinline__ void store_depth(const PullPushArgs& a, uint32_t o, const float d) {
+    o = MLGI_IX(o, (uint32_t)a.atlas_w * (uint32_t)a.atlas_h);
     if (a.out_f16)
         reinterpret_cast<__half*>(a.out)[o] = __float2half_rn(d);
     else
@@ -702,7 +707,7 @@ __device__ __forceinline__ void store_depth(const PullPushArgs& a, const uint32_
 }
 
 __device__ __forceinline__ float key_depth(const PullPushArgs& a, const uint32_t o) {
-    return float(__ldg(a.keys + o) >> 8) / 16777216.0f;
+    return float(__ldg(a.keys + MLGI_IX(o, (uint32_t)a.atlas_w * (uint32_t)a.atlas_h)) >> 8) / 16777216.0f;
 }
 
 __device__ __forceinline__ void push0_quads(const PullPushArgs& a, const int tx, const int ty) {
@@ -740,7 +745,14 @@ __device__ __forceinline__ void pullmid_ism(const PullPushArgs& a, const int ism
         for (int k = 2; k < l; ++k) off += (size_t)(s >> k) * (s >> k);
         return lvl_base + off;
     };
-    const int ix = ism % a.grid_x, iy = ism / a.grid_x;
+#ifdef MLGI_CHECKS
+    {  // levels 2..L inside the block's shared memory: their last texel
+        uint32_t dyn;
+        asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+        (void)MLGI_IX((lvl(L + 1) - lvl_base) - 1, dyn > kPullPushTableBytes ? (dyn - kPullPushTableBytes) / 16 : 0);
+    }
+#endif
+    const int im = MLGI_IX(ism, a.grid_x * a.grid_y), ix = im % a.grid_x, iy = im / a.grid_x;
     const int nt = blockDim.x, tid = threadIdx.x;
     for (int l = 2; l <= L; ++l) {  // pull
         const int sl = s >> l;
@@ -749,8 +761,9 @@ __device__ __forceinline__ void pullmid_ism(const PullPushArgs& a, const int ism
         const float scale = pow2neg(l);
         for (int i = tid; i < sl * sl; i += nt) {
             const int gox = ox0 + i % sl, goy = oy0 + i / sl;
-            out[i] = l == 2 ? pull_texel(a.lv1, a.atlas_w >> 1, 0, 0, gox, goy, scale)
-                            : pull_texel(lvl(l - 1), 2 * sl, 2 * ox0, 2 * oy0, gox, goy, scale);
+            out[i] = l == 2 ? pull_texel(a.lv1, (size_t)(a.atlas_w >> 1) * (a.atlas_h >> 1), a.atlas_w >> 1, 0, 0, gox,
+                                         goy, scale)
+                            : pull_texel(lvl(l - 1), (size_t)4 * sl * sl, 2 * sl, 2 * ox0, 2 * oy0, gox, goy, scale);
         }
         __syncthreads();
     }
@@ -771,7 +784,7 @@ __device__ __forceinline__ void pullmid_ism(const PullPushArgs& a, const int ism
             for (int k = 0; k < 4; ++k) {
                 const int cx = gidx - 1 + kPushOff[k][0] - ix * sc, cy = gidy - 1 + kPushOff[k][1] - iy * sc;
                 inside[k] = cx >= 0 && cy >= 0 && cx < sc && cy < sc;
-                coarse[k] = inside[k] ? coarse_lvl[cy * sc + cx] : make_float4(0.f, 0.f, 0.f, 0.f);
+                coarse[k] = inside[k] ? coarse_lvl[MLGI_IX(cy * sc + cx, sc * sc)] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
             same[i] = push_texel<true>(coarse, inside, (px + 1) & 1, (py + 1) & 1, same[i], scale);
         }
@@ -780,7 +793,7 @@ __device__ __forceinline__ void pullmid_ism(const PullPushArgs& a, const int ism
     const int s2 = s >> 2, w2 = a.atlas_w >> 2;
     const float4* l2 = lvl(2);
     for (int i = tid; i < s2 * s2; i += nt)
-        a.lv2[(size_t)(iy * s2 + i / s2) * w2 + ix * s2 + i % s2] = l2[i];
+        a.lv2[MLGI_IX((size_t)(iy * s2 + i / s2) * w2 + ix * s2 + i % s2, (size_t)w2 * (a.atlas_h >> 2))] = l2[i];
 }
 
 // kPull1Rows tile rows per block, so that the key tables are filled once for several tiles.
@@ -1084,3 +1097,5 @@ int batch_blocks_per_sm(int pass, size_t smem) {
 }
 
 }  // namespace mlgi
+
+MLGI_CHECK_UNIT(ism_kernels)

@@ -13,6 +13,24 @@ namespace mlgi {
 // atlas at most 65535 texels a side, far plane, VPL range); on failure `why` (n bytes) says why.
 bool ism_params_valid(const mlgi_ism_params* p, char* why, size_t n);
 
+// Every device and pinned host allocation of the library goes through these. Once the allocations
+// that mlgi_set_alloc_fault allows are used up they fail with cudaErrorMemoryAllocation without
+// asking CUDA (the simulated out-of-memory of the allocation-failure tests).
+cudaError_t dev_alloc(void** p, size_t bytes);
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t s);
+cudaError_t pinned_alloc(void** p, size_t bytes);
+
+#ifdef MLGI_CHECKS
+// The bounds-checked build: each kernel translation unit's first index violation since the last
+// call, read and cleared (checks.cuh).
+cudaError_t checks_take_ism_kernels(unsigned long long* rec);
+cudaError_t checks_take_fg_kernels(unsigned long long* rec);
+cudaError_t checks_take_scene_kernels(unsigned long long* rec);
+cudaError_t checks_take_post_kernels(unsigned long long* rec);
+cudaError_t checks_take_cluster_kernels(unsigned long long* rec);
+cudaError_t checks_take_mlgi_api(unsigned long long* rec);
+#endif
+
 struct VplArgs {
     int n;                 // VPL count (work items)
     uint32_t ax, ay;       // lightsOnAxis

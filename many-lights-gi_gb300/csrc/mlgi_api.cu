@@ -1,6 +1,7 @@
 // C ABI of the GI hot path: argument checking, context-owned buffers, per-pass timing and the
 // frame-level chain (GIStage::process's GI part, GIStage.cpp:346-418).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -13,6 +14,7 @@
 
 #include <cuda_runtime.h>
 
+#include "checks.cuh"
 #include "kernels.h"
 #include "mlgi.h"
 
@@ -47,7 +49,42 @@ bool ism_params_valid(const mlgi_ism_params* p, char* why, size_t n) {
     return true;
 }
 
+namespace {
+// Allocations left before the simulated failures begin; -1: none simulated.
+std::atomic<long long> g_allocs_left{-1};
+
+bool simulated_failure() {
+    long long v = g_allocs_left.load();
+    while (v >= 0) {
+        if (v == 0) return true;
+        if (g_allocs_left.compare_exchange_weak(v, v - 1)) return false;
+    }
+    return false;
+}
+}  // namespace
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    return simulated_failure() ? cudaErrorMemoryAllocation : cudaMalloc(p, bytes);
+}
+
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t s) {
+    *p = nullptr;
+    return simulated_failure() ? cudaErrorMemoryAllocation : cudaMallocAsync(p, bytes, s);
+}
+
+cudaError_t pinned_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    return simulated_failure() ? cudaErrorMemoryAllocation : cudaMallocHost(p, bytes);
+}
+
 }  // namespace mlgi
+
+extern "C" mlgi_status mlgi_set_alloc_fault(int64_t after) {
+    if (after < -1) return MLGI_EINVAL;
+    mlgi::g_allocs_left.store(after);
+    return MLGI_OK;
+}
 
 namespace {
 
@@ -168,7 +205,7 @@ struct mlgi_ctx {
     // cannot do).
     struct {
         std::vector<unsigned char> key;
-        int calls = 0;           // calls with this key
+        int calls = 0;           // calls with this key that went through
         bool failed = false;     // the capture did not succeed: this key runs directly
         cudaGraphExec_t exec = nullptr;
     } hgraph;
@@ -204,10 +241,11 @@ mlgi_status ensure(mlgi_ctx* ctx, DevBuf& b, size_t bytes) {
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.bytes = 0;
-    cudaError_t e = cudaMalloc(&b.p, bytes);
+    cudaError_t e = mlgi::dev_alloc(&b.p, bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return fail(ctx, MLGI_ENOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        return fail(ctx, e == cudaErrorMemoryAllocation ? MLGI_ENOMEM : MLGI_ECUDA, "cudaMalloc(%zu bytes) failed: %s",
+                    bytes, cudaGetErrorString(e));
     }
     b.bytes = bytes;
     return MLGI_OK;
@@ -233,7 +271,7 @@ mlgi_status get_shuffle(mlgi_ctx* ctx, int n, const int32_t** out) {
     std::vector<int32_t> h(n);
     shuffle_host(n, h.data());
     int32_t* d = nullptr;
-    if (cudaMalloc(&d, sizeof(int32_t) * n) != cudaSuccess) {
+    if (mlgi::dev_alloc((void**)&d, sizeof(int32_t) * n) != cudaSuccess) {
         cudaGetLastError();
         return fail(ctx, MLGI_ENOMEM, "shuffle table allocation failed");
     }
@@ -284,6 +322,7 @@ const char* mlgi_status_string(mlgi_status s) {
         case MLGI_ETIMEDOUT: return "device wait timed out";
         case MLGI_ECUDA: return "CUDA error";
         case MLGI_ECANCELED: return "cancelled";
+        case MLGI_EBOUNDS: return "index out of bounds";
         default: return "unknown status";
     }
 }
@@ -295,9 +334,9 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
     ctx->device = desc ? desc->device : 0;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->status, sizeof(uint32_t));
+    if (e == cudaSuccess) e = mlgi::dev_alloc((void**)&ctx->status, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(ctx->status, 0, sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->status_host, sizeof(uint32_t), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = mlgi::pinned_alloc((void**)&ctx->status_host, sizeof(uint32_t));
     for (int i = 0; e == cudaSuccess && i < kNumEvents; ++i) e = cudaEventCreate(&ctx->ev[i]);
     for (int i = 0; e == cudaSuccess && i < 3; ++i) e = cudaEventCreate(&ctx->ev_pp[i]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking);
@@ -317,7 +356,7 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
     if (e != cudaSuccess) {
         cudaGetLastError();
         mlgi_destroy(ctx);
-        return MLGI_ECUDA;
+        return e == cudaErrorMemoryAllocation ? MLGI_ENOMEM : MLGI_ECUDA;
     }
     *out = ctx;
     return MLGI_OK;
@@ -755,8 +794,74 @@ mlgi_status mlgi_set_gather_wait_test(mlgi_ctx* ctx, int64_t wait_cycles, uint32
     return MLGI_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Reads element `index` of `buf` (`extent` floats) through a checked index (the test of the checks).
+__global__ void check_index_selftest_kernel(const float* buf, long long index, long long extent, float* out) {
+    *out = buf[MLGI_IX(index, extent)];
+}
+
+#ifdef MLGI_CHECKS
+// The first recorded index violation of any unit (then every unit's record is cleared), as an
+// MLGI_EBOUNDS failure of ctx; MLGI_OK when there is none.
+mlgi_status take_index_violations(mlgi_ctx* ctx) {
+    MLGI_CUDA(ctx, cudaDeviceSynchronize());
+    struct Unit {
+        const char* name;
+        cudaError_t (*take)(unsigned long long*);
+    };
+    const Unit units[] = {{"ism_kernels", mlgi::checks_take_ism_kernels},   {"fg_kernels", mlgi::checks_take_fg_kernels},
+                          {"scene_kernels", mlgi::checks_take_scene_kernels}, {"post_kernels", mlgi::checks_take_post_kernels},
+                          {"cluster_kernels", mlgi::checks_take_cluster_kernels}, {"mlgi_api", mlgi::checks_take_mlgi_api}};
+    mlgi_status st = MLGI_OK;
+    for (const Unit& u : units) {
+        unsigned long long rec = 0;
+        MLGI_CUDA(ctx, u.take(&rec));
+        if (rec && st == MLGI_OK)
+            st = fail(ctx, MLGI_EBOUNDS, "index %llu out of range at line %llu of the %s unit",
+                      rec & ((1ull << 44) - 1), rec >> 44, u.name);
+    }
+    return st;
+}
+#endif
+}  // namespace
+
+extern "C" {
+
+int mlgi_checks_enabled(void) {
+#ifdef MLGI_CHECKS
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+mlgi_status mlgi_check_index_selftest(mlgi_ctx* ctx, int64_t index, int64_t extent) {
+    if (!ctx) return MLGI_EINVAL;
+    if (extent < 1 || extent > (int64_t(1) << 24)) return fail(ctx, MLGI_EINVAL, "extent %lld out of range", (long long)extent);
+    if (!mlgi_checks_enabled() && (index < 0 || index >= extent))
+        return fail(ctx, MLGI_EINVAL, "index %lld outside [0, %lld) needs the bounds-checked library", (long long)index,
+                    (long long)extent);
+    cudaStream_t s = ctx->stream;
+    float* buf = nullptr;
+    if (mlgi::dev_alloc_async((void**)&buf, (size_t)(extent + 1) * sizeof(float), s) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, MLGI_ENOMEM, "self-test buffer");
+    }
+    MLGI_CUDA(ctx, cudaMemsetAsync(buf, 0, (size_t)(extent + 1) * sizeof(float), s));
+    check_index_selftest_kernel<<<1, 1, 0, s>>>(buf, index, extent, buf + extent);
+    const cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(buf, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "check_index_selftest_kernel");
+    return MLGI_OK;
+}
+
 mlgi_status mlgi_check_device_status(mlgi_ctx* ctx, mlgi_stream stream) {
     if (!ctx) return MLGI_EINVAL;
+#ifdef MLGI_CHECKS
+    if (const mlgi_status st = take_index_violations(ctx)) return st;
+#endif
     cudaStream_t s = pick(ctx, stream);
     uint32_t word = 0;
     MLGI_CUDA(ctx, cudaMemcpyAsync(&word, ctx->status, sizeof(word), cudaMemcpyDeviceToHost, s));
@@ -1200,7 +1305,9 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     } else {
         st = host_frame(ctx, f, rgb_host);
     }
-    ++g.calls;
+    // a key is captured only after a call with it went through: that call made every allocation
+    // the frame needs, which a capture could not make
+    if (st == MLGI_OK) ++g.calls;
     // nothing may still read the caller's buffers when the call returns, also after an error
     const cudaError_t e1 = cudaStreamSynchronize(ctx->copy);
     const cudaError_t e2 = cudaStreamSynchronize(ctx->side);
@@ -1419,13 +1526,13 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
         mlgi_batch_destroy(b);
         return st;
     };
-    if (cudaMalloc(&b->arena, std::max<size_t>(total, 256)) != cudaSuccess) {
+    if (mlgi::dev_alloc(&b->arena, std::max<size_t>(total, 256)) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(ctx, MLGI_ENOMEM, "batch arena of %zu bytes", total));
     }
-    if (cudaMallocHost(&b->h_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
-        cudaMalloc(&b->d_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
-        cudaMalloc(&b->d_prefix, sizeof(int) * mlgi::kBpCount * (n_views + 1)) != cudaSuccess) {
+    if (mlgi::pinned_alloc((void**)&b->h_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
+        mlgi::dev_alloc((void**)&b->d_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
+        mlgi::dev_alloc((void**)&b->d_prefix, sizeof(int) * mlgi::kBpCount * (n_views + 1)) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(ctx, MLGI_ENOMEM, "batch tables"));
     }
@@ -1514,3 +1621,5 @@ mlgi_status mlgi_batch_launch(mlgi_batch* b, mlgi_stream stream) {
 }
 
 }  // extern "C"
+
+MLGI_CHECK_UNIT(mlgi_api)

@@ -13,6 +13,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "checks.cuh"
 #include "gi_device.cuh"
 #include "kernels.h"
 
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(kBlurThreads) gi_blur_kernel(BlurArgs a) {
             S.gi[ry][rx] = make_float4(0.f, 0.f, 0.f, 0.f);
             continue;
         }
-        const size_t p = (size_t)gy * a.width + gx;
+        const size_t p = MLGI_IX((size_t)gy * a.width + gx, (size_t)a.width * a.height);
         // linearDepth (reprojection.glsl:6-14)
         const float z_n = 2.0f * __ldg(a.depth + p) - 1.0f;
         const float lin = __fdividef(-a.proj_b, a.proj_a + z_n);
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kBlurThreads) gi_blur_kernel(BlurArgs a) {
                 if (S.gi[cy + side * i][cx].w != 0.f)
                     blur_sample(c, S.nl[cy + side * i][cx], S.tx[cy + side * i][tx], float(i), acc, factorAcc);
         const v3 o = acc * __fdividef(1.0f, factorAcc);
-        const size_t p = (size_t)gy * a.width + gx;
+        const size_t p = MLGI_IX((size_t)gy * a.width + gx, (size_t)a.width * a.height);
         if (a.packed) {
             reinterpret_cast<uint32_t*>(a.gi_out)[p] = pack_r11g11b10f(o);
         } else {
@@ -306,3 +307,5 @@ cudaError_t launch_composite(const CompositeArgs& a, cudaStream_t s) {
 }
 
 }  // namespace mlgi
+
+MLGI_CHECK_UNIT(post_kernels)

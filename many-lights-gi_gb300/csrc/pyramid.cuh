@@ -269,11 +269,12 @@ __device__ __noinline__ void push_quad_exact_smem(float4* same, const float4* co
     push_coarse(coarse, sc, sc, sc, gx, gy, scale, C);
     const bool bx = gx == 0 || gx == sc, by = gy == 0 || gy == sc;
     const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
-    if (y0 >= 0 && x0 >= 0) same[y0 * el + x0] = push_output<true, 0, 0>(C, bx, by, same[y0 * el + x0]);
-    if (y0 >= 0 && x0 + 1 < el) same[y0 * el + x0 + 1] = push_output<true, 1, 0>(C, bx, by, same[y0 * el + x0 + 1]);
-    if (y0 + 1 < el && x0 >= 0) same[(y0 + 1) * el + x0] = push_output<true, 0, 1>(C, bx, by, same[(y0 + 1) * el + x0]);
+    const int n = el * el, i0 = y0 * el + x0, i1 = (y0 + 1) * el + x0;  // used only where inside
+    if (y0 >= 0 && x0 >= 0) same[MLGI_IX(i0, n)] = push_output<true, 0, 0>(C, bx, by, same[MLGI_IX(i0, n)]);
+    if (y0 >= 0 && x0 + 1 < el) same[MLGI_IX(i0 + 1, n)] = push_output<true, 1, 0>(C, bx, by, same[MLGI_IX(i0 + 1, n)]);
+    if (y0 + 1 < el && x0 >= 0) same[MLGI_IX(i1, n)] = push_output<true, 0, 1>(C, bx, by, same[MLGI_IX(i1, n)]);
     if (y0 + 1 < el && x0 + 1 < el)
-        same[(y0 + 1) * el + x0 + 1] = push_output<true, 1, 1>(C, bx, by, same[(y0 + 1) * el + x0 + 1]);
+        same[MLGI_IX(i1 + 1, n)] = push_output<true, 1, 1>(C, bx, by, same[MLGI_IX(i1 + 1, n)]);
 }
 
 __device__ __noinline__ float4 push_quad_exact_l0(const float4* lv1, const int e1, const int gx, const int gy,
@@ -297,7 +298,7 @@ __device__ __forceinline__ void push_quad_smem(float4* same, const float4* coars
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int cx = min(max(gx - 1 + kPushOff[k][0], 0), sc - 1), cy = min(max(gy - 1 + kPushOff[k][1], 0), sc - 1);
-        c[k] = push_term(coarse[cy * sc + cx], scale);
+        c[k] = push_term(coarse[MLGI_IX(cy * sc + cx, sc * sc)], scale);
     }
     const bool bx = gx == 0 || gx == sc, by = gy == 0 || gy == sc;
     const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
@@ -306,7 +307,9 @@ __device__ __forceinline__ void push_quad_smem(float4* same, const float4* coars
     // clamped indices: an output outside the ISM is neither stored nor lets its value matter
     const int i00 = max(y0, 0) * el + max(x0, 0), i10 = max(y0, 0) * el + min(x0 + 1, el - 1),
               i01 = min(y0 + 1, el - 1) * el + max(x0, 0), i11 = min(y0 + 1, el - 1) * el + min(x0 + 1, el - 1);
-    const float4 o00 = same[i00], o10 = same[i10], o01 = same[i01], o11 = same[i11];
+    const int n = el * el;
+    const float4 o00 = same[MLGI_IX(i00, n)], o10 = same[MLGI_IX(i10, n)], o01 = same[MLGI_IX(i01, n)],
+                 o11 = same[MLGI_IX(i11, n)];
     bool band = false;
     const float4 r00 = push_out_lean<true, 0, 0>(c, bx, by, o00, band, T);
     const float4 r10 = push_out_lean<true, 1, 0>(c, bx, by, o10, band, T);
@@ -316,10 +319,10 @@ __device__ __forceinline__ void push_quad_smem(float4* same, const float4* coars
         push_quad_exact_smem(same, coarse, el, gx, gy, scale);
         return;
     }
-    if (ok00) same[i00] = r00;
-    if (ok10) same[i10] = r10;
-    if (ok01) same[i01] = r01;
-    if (ok11) same[i11] = r11;
+    if (ok00) same[MLGI_IX(i00, n)] = r00;
+    if (ok10) same[MLGI_IX(i10, n)] = r10;
+    if (ok01) same[MLGI_IX(i01, n)] = r01;
+    if (ok11) same[MLGI_IX(i11, n)] = r11;
 }
 
 template <int NT>
@@ -327,7 +330,7 @@ __device__ __forceinline__ void pyramid_ism(const PullPushArgs& a, const int ism
     PyramidTables& T = *reinterpret_cast<PyramidTables*>(smem);
     float4* pyr = reinterpret_cast<float4*>(smem + kPyramidTableBytes);
     const int s = a.ism_size, L = a.levels, e1 = s >> 1, e2 = s >> 2;
-    const int ix = ism % a.grid_x, iy = ism / a.grid_x;
+    const int im = MLGI_IX(ism, a.grid_x * a.grid_y), ix = im % a.grid_x, iy = im / a.grid_x;
     const int tid = threadIdx.x;
     fill_pyramid_tables(T, a.z_far);
     __syncthreads();
@@ -335,14 +338,22 @@ __device__ __forceinline__ void pyramid_ism(const PullPushArgs& a, const int ism
     float4* const lv2 = pyr + e1 * e1;
     const float fs = float(s), z_far = a.z_far;
     const int aw = a.atlas_w;
+#ifdef MLGI_CHECKS
+    {  // the whole pyramid inside the block's shared memory: its last texel
+        uint32_t dyn;
+        asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+        (void)MLGI_IX(pyramid_offset(s, L + 1) - 1, dyn > kPyramidTableBytes ? (dyn - kPyramidTableBytes) / 16 : 0);
+    }
+#endif
+    const size_t nk = (size_t)aw * a.atlas_h - 3;  // a row of four keys: its first
 
     // phase 1: a thread per level-2 texel, in row-major order
     for (int uy = tid / e2, ux = tid - (tid / e2) * e2; uy < e2;) {
         const int gx2 = ix * e2 + ux, gy2 = iy * e2 + uy;  // global level-2 texel
-        const uint32_t* kr = a.keys + (size_t)(4 * gy2) * aw + 4 * gx2;
+        const size_t kr = (size_t)(4 * gy2) * aw + 4 * gx2;
         uint4 r[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) r[j] = __ldg(reinterpret_cast<const uint4*>(kr + (size_t)j * aw));
+        for (int j = 0; j < 4; ++j) r[j] = __ldg(reinterpret_cast<const uint4*>(a.keys + MLGI_IX(kr + (size_t)j * aw, nk)));
         float4 t[4];  // level-1 texels (2 gx2, 2 gy2) + kPullOff[k]
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -350,9 +361,9 @@ __device__ __forceinline__ void pyramid_ism(const PullPushArgs& a, const int ism
             const uint4 ra = r[2 * ky], rb = r[2 * ky + 1];
             const uint32_t key[4] = {kx ? ra.z : ra.x, kx ? rb.z : rb.x, kx ? ra.w : ra.y, kx ? rb.w : rb.y};
             t[k] = pull1_lean(key, T, z_far, fs);
-            lv1[(2 * uy + ky) * e1 + 2 * ux + kx] = t[k];
+            lv1[MLGI_IX((2 * uy + ky) * e1 + 2 * ux + kx, e1 * e1)] = t[k];
         }
-        lv2[uy * e2 + ux] = pull_lean(t, gx2, gy2, 0.25f, T);
+        lv2[MLGI_IX(uy * e2 + ux, e2 * e2)] = pull_lean(t, gx2, gy2, 0.25f, T);
         ux += NT;  // the texel NT further in row-major order (NT may exceed e2)
         while (ux >= e2) {
             ux -= e2;
@@ -371,7 +382,8 @@ __device__ __forceinline__ void pyramid_ism(const PullPushArgs& a, const int ism
             const int ly = i / el, lx = i - ly * el;
             float4 t4[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) t4[k] = in[(2 * ly + kPullOff[k][1]) * 2 * el + 2 * lx + kPullOff[k][0]];
+            for (int k = 0; k < 4; ++k)
+                t4[k] = in[MLGI_IX((2 * ly + kPullOff[k][1]) * 2 * el + 2 * lx + kPullOff[k][0], 4 * el * el)];
             out[i] = pull_lean(t4, el * ix + lx, el * iy + ly, scale, T);
         }
         __syncthreads();
@@ -395,7 +407,7 @@ __device__ __forceinline__ void pyramid_ism(const PullPushArgs& a, const int ism
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int cx = min(max(gx - 1 + kPushOff[k][0], 0), e1 - 1), cy = min(max(gy - 1 + kPushOff[k][1], 0), e1 - 1);
-            c[k] = push_term(lv1[cy * e1 + cx], 1.0f);
+            c[k] = push_term(lv1[MLGI_IX(cy * e1 + cx, e1 * e1)], 1.0f);
         }
         const bool bx = gx == 0 || gx == e1, by = gy == 0 || gy == e1;
         const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;  // ISM-local

@@ -9,6 +9,7 @@
 #include <cuda_fp16.h>
 
 #include "../host/room.h"
+#include "checks.cuh"
 #include "kernels.h"
 #include "mlgi.h"
 
@@ -147,7 +148,7 @@ __global__ void raster_camera_kernel(const RoomGPU R, int w, int h, float* depth
                                      uint32_t* albedo) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
-    const size_t i = (size_t)y * w + x;
+    const size_t i = MLGI_IX((size_t)y * w + x, (size_t)w * h);
     const Ray ray = pixel_ray(R.inv_vp, x, y, w, h);
     Hit hit;
     float d = 1.f, ex = 0.f, ey = 0.f;
@@ -179,7 +180,7 @@ __global__ void raster_camera_kernel(const RoomGPU R, int w, int h, float* depth
 __global__ void raster_light_kernel(const RoomGPU R, int w, int h, float* depth, uint32_t* normal, uint32_t* diffuse) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
-    const size_t i = (size_t)y * w + x;
+    const size_t i = MLGI_IX((size_t)y * w + x, (size_t)w * h);
     const Ray ray = pixel_ray(R.inv_lvp, x, y, w, h);
     Hit hit;
     float d = 1.f;
@@ -222,6 +223,7 @@ __global__ void points_kernel(const RoomGPU R, int64_t n_points, int n_buckets, 
         if (R.cdf[mid] < u0) lo = mid + 1; else hi = mid;
     }
     float px, py, pz, nx, ny, nz;
+    lo = MLGI_IX(lo, R.n_patches < kRoomMaxPatches ? R.n_patches : kRoomMaxPatches);
     if (R.patch_kind[lo] == 0) {
         px = R.patch_o[lo][0] + R.patch_a[lo][0] * u1 + R.patch_b[lo][0] * u2;
         py = R.patch_o[lo][1] + R.patch_a[lo][1] * u1 + R.patch_b[lo][1] * u2;
@@ -252,7 +254,7 @@ __global__ void points_kernel(const RoomGPU R, int64_t n_points, int n_buckets, 
     const uint32_t w = unorm8(nx * 0.5f + 0.5f) | (unorm8(ny * 0.5f + 0.5f) << 8) | (unorm8(nz * 0.5f + 0.5f) << 16) |
                        (unorm8(R.r_boost / 25.f) << 24);
     const int64_t b = k % n_buckets, slot = k / n_buckets;
-    points[b * stride + slot] = make_float4(px, py, pz, __uint_as_float(w));
+    points[MLGI_IX(b * stride + slot, (int64_t)n_buckets * stride)] = make_float4(px, py, pz, __uint_as_float(w));
 }
 
 __global__ void counts_kernel(int64_t n_points, int n_buckets, uint32_t* counts) {
@@ -296,3 +298,5 @@ extern "C" mlgi_status mlgi_scene_generate_device(const mlgi_scene_desc* desc, m
     if (counts) counts_kernel<<<(desc->n_buckets + 255) / 256, 256, 0, s>>>(desc->n_points, desc->n_buckets, counts);
     return cudaGetLastError() == cudaSuccess ? MLGI_OK : MLGI_ECUDA;
 }
+
+MLGI_CHECK_UNIT(scene_kernels)

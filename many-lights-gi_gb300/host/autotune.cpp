@@ -17,6 +17,7 @@
 
 #include <cuda_runtime.h>
 
+#include "kernels.h"
 #include "mlgi.h"
 
 namespace {
@@ -42,7 +43,7 @@ struct DevBuf {
         if (p) cudaFree(p);
     }
     bool alloc(size_t bytes) {
-        if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+        if (mlgi::dev_alloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
             cudaGetLastError();
             p = nullptr;
             return false;

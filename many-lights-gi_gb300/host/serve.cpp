@@ -26,6 +26,7 @@
 
 #include <cuda_runtime.h>
 
+#include "kernels.h"
 #include "mlgi.h"
 
 namespace {
@@ -162,7 +163,7 @@ size_t frame_bytes(int max_w, int max_h, int rsm) {
 }
 
 bool dalloc(void** p, size_t bytes) {
-    if (cudaMalloc(p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+    if (mlgi::dev_alloc(p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;
         return false;
@@ -192,7 +193,7 @@ Slot* make_slot(mlgi_server* sv) {
     ok = ok && dalloc((void**)&sl->gd, px * 4) && dalloc(&sl->gn, px * 8) && dalloc((void**)&sl->rgb, px * 12) &&
          dalloc((void**)&sl->rd, rt * 4) && dalloc((void**)&sl->rn, rt * 4) && dalloc((void**)&sl->rf, rt * 4) &&
          dalloc((void**)&sl->part_h, (kDigestBlocks + 1) * 16);
-    ok = ok && cudaMallocHost((void**)&sl->h_out, 16) == cudaSuccess;
+    ok = ok && mlgi::pinned_alloc((void**)&sl->h_out, 16) == cudaSuccess;
     ok = ok && cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) == cudaSuccess;
     if (ok && sv->reserved_vpl > 0) ok = mlgi_ctx_reserve(sl->ctx, sv->reserved_vpl, sv->reserved_texels) == MLGI_OK;
     if (!ok) {
@@ -262,7 +263,7 @@ Fit get_room(mlgi_server* sv, const mlgi_request& r, cudaStream_t s, RoomState**
     if (fixed + sv->room_bytes + bytes > sv->desc.hbm_budget) return Fit::kWait;
     RoomState st;
     void* p = nullptr;
-    if (cudaMallocAsync(&p, bytes, s) != cudaSuccess) {
+    if (mlgi::dev_alloc_async(&p, bytes, s) != cudaSuccess) {
         cudaGetLastError();
         return Fit::kNoMem;
     }
@@ -502,9 +503,10 @@ mlgi_status mlgi_server_create(const mlgi_server_desc* desc, mlgi_server** out) 
         return MLGI_ENOMEM;
     }
     mlgi_ctx_desc cd{desc->device, 0};
-    if (mlgi_create(&sv->tune_ctx, &cd) != MLGI_OK) {
+    const mlgi_status cst = mlgi_create(&sv->tune_ctx, &cd);
+    if (cst != MLGI_OK) {
         mlgi_server_destroy(sv);
-        return MLGI_ECUDA;
+        return cst;
     }
     for (int i = 0; i < desc->slots; ++i) {
         Slot* sl = make_slot(sv);

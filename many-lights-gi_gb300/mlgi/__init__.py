@@ -2,7 +2,8 @@
 
 This module is a thin caller of the C ABI: every device computation goes through the CUDA
 kernels in libmlgi.so. Loading fails loudly when the library has not been built; there is no
-fallback implementation.
+fallback implementation. With MLGI_CHECKED=1 in the environment it loads the bounds-checked
+variant, libmlgi_checked.so, instead.
 """
 from __future__ import annotations
 
@@ -14,9 +15,11 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(_HERE)
-LIB_PATH = os.path.join(PKG, "_build", "libmlgi.so")
+LIB_PATH_NORMAL = os.path.join(PKG, "_build", "libmlgi.so")
+LIB_PATH_CHECKED = os.path.join(PKG, "_build_checked", "libmlgi_checked.so")
+LIB_PATH = LIB_PATH_CHECKED if os.environ.get("MLGI_CHECKED") == "1" else LIB_PATH_NORMAL
 
-OK, EINVAL, ENOMEM, ETIMEDOUT, ECUDA, ECANCELED = 0, 1, 2, 3, 4, 5
+OK, EINVAL, ENOMEM, ETIMEDOUT, ECUDA, ECANCELED, EBOUNDS = 0, 1, 2, 3, 4, 5, 6
 F32, F16, BF16, R11G11B10F, RGBA8 = 0, 1, 2, 3, 4
 
 _p = C.c_void_p
@@ -213,6 +216,9 @@ _SIGS = {
     "mlgi_last_timings": (C.c_int32, [_p, _p, C.c_int]),
     "mlgi_check_device_status": (C.c_int32, [_p, _p]),
     "mlgi_set_gather_wait_test": (C.c_int32, [_p, C.c_int64, C.c_uint32]),
+    "mlgi_set_alloc_fault": (C.c_int32, [C.c_int64]),
+    "mlgi_checks_enabled": (C.c_int, []),
+    "mlgi_check_index_selftest": (C.c_int32, [_p, C.c_int64, C.c_int64]),
     "mlgi_scene_generate": (C.c_int32, [C.POINTER(SceneDesc), C.POINTER(SceneInfo), _p, _p, _p, _p, _p, _p, _p, _p]),
     "mlgi_scene_generate_device": (C.c_int32, [C.POINTER(SceneDesc), C.POINTER(SceneInfo), _p, _p, C.c_int, _p, _p, _p,
                                                _p, _p, _p, _p]),
@@ -221,18 +227,23 @@ _SIGS = {
 _lib = None
 
 
+def load(path: str) -> C.CDLL:
+    """Load a build of the library at `path` with the ctypes signature of every entry point."""
+    if not os.path.exists(path):
+        raise RuntimeError(f"{os.path.basename(path)} is not built ({path}); run __graft_entry__.build()")
+    L = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
 def lib() -> C.CDLL:
-    """Load libmlgi.so (raises if it was not built)."""
+    """Load libmlgi.so, or libmlgi_checked.so under MLGI_CHECKED=1 (raises if it was not built)."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise RuntimeError(f"libmlgi.so is not built ({LIB_PATH}); run __graft_entry__.build()")
-        L = C.CDLL(LIB_PATH)
-        for name, (res, args) in _SIGS.items():
-            fn = getattr(L, name)
-            fn.restype = res
-            fn.argtypes = args
-        _lib = L
+        _lib = load(LIB_PATH)
     return _lib
 
 

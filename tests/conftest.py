@@ -16,12 +16,27 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def _built_libraries():
-    """Build the oracle and libmlgi.so once per session (no-ops when up to date)."""
+    """Build the oracle, libmlgi.so and libmlgi_checked.so once per session (no-ops when up to date)."""
     import importlib.util
 
     for path in (os.path.join(ROOT, "oracle", "build.py"), os.path.join(PKG, "build.py")):
         spec = importlib.util.spec_from_file_location("_b_" + os.path.basename(os.path.dirname(path)), path)
         mod = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(mod)
-        mod.build()
+        getattr(mod, "build_all", mod.build)()
     yield
+
+
+@pytest.fixture(autouse=True)
+def _no_index_violations(request):
+    """Under the bounds-checked library (MLGI_CHECKED=1), every GPU test must end with no index
+    violation recorded by any kernel it ran."""
+    yield
+    if os.environ.get("MLGI_CHECKED") == "1" and request.node.get_closest_marker("gpu"):
+        import mlgi
+
+        ctx = mlgi.Context(0)
+        try:
+            ctx.check_device_status()
+        finally:
+            ctx.close()

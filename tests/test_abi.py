@@ -60,6 +60,22 @@ def test_status_strings():
     L = mlgi.lib()
     assert L.mlgi_status_string(mlgi.OK) == b"ok"
     assert L.mlgi_status_string(mlgi.ETIMEDOUT) == b"device wait timed out"
+    assert L.mlgi_status_string(mlgi.EBOUNDS) == b"index out of bounds"
+
+
+def test_checked_library_exports_every_declared_symbol_and_says_it_checks():
+    normal = mlgi.load(mlgi.LIB_PATH_NORMAL)
+    checked = mlgi.load(mlgi.LIB_PATH_CHECKED)
+    missing = [n for n in header_functions() if not hasattr(checked, n)]
+    assert not missing, missing
+    assert normal.mlgi_checks_enabled() == 0 and checked.mlgi_checks_enabled() == 1
+
+
+def test_allocation_hook_arguments():
+    L = mlgi.lib()
+    assert L.mlgi_set_alloc_fault(-2) == mlgi.EINVAL
+    assert L.mlgi_set_alloc_fault(3) == mlgi.OK
+    assert L.mlgi_set_alloc_fault(-1) == mlgi.OK
 
 
 def test_null_context_is_rejected():
