@@ -537,8 +537,9 @@ def c4_views(ctx, n_views=32, n_rooms=8, seed=4):
 
 def measure_batch(local_rank, n_views, steps, warmup, batch_streams):
     """Batched views (n_views views of 8 rooms), replayed from CUDA graphs in two forms -- one
-    persistent launch per pass over all views, and each view's kernels spread over several streams --
-    against one mlgi_gi_frame per view on one stream. Returns the measurements as a dict."""
+    persistent launch per pass over all views (or over each of 2..4 view groups on their own
+    streams), and each view's kernels spread over several streams -- against one mlgi_gi_frame per
+    view on one stream. Returns the measurements as a dict."""
     import numpy as np
     import torch
 
@@ -569,14 +570,22 @@ def measure_batch(local_rank, n_views, steps, warmup, batch_streams):
 
     sampler = ClockSampler(local_rank)
     sampler.start()
-    forms = {}
-    for name, form, streams in (("persistent", mlgi.BATCH_PERSISTENT, 0),
-                                ("concurrent", mlgi.BATCH_CONCURRENT, batch_streams)):
+    forms, groups = {}, {}
+    # the persistent form with 1..4 view groups (each group's passes on its own stream), the best
+    # reported as "persistent"; the concurrent form on batch_streams streams
+    for name, form, streams in [(f"persistent_g{g}", mlgi.BATCH_PERSISTENT, g) for g in (1, 2, 3, 4)] + \
+                               [("concurrent", mlgi.BATCH_CONCURRENT, batch_streams)]:
         batch = Batch(ctx, frames, form, streams)
         ms = timed(lambda: batch.launch(ctx.stream()))
-        forms[name] = {"ms_per_batch": ms, "frames_per_s": len(frames) / (ms * 1e-3),
-                       "kernel_launches": batch.kernel_launches(), **({"streams": streams} if streams else {})}
+        r = {"ms_per_batch": ms, "frames_per_s": len(frames) / (ms * 1e-3), "kernel_launches": batch.kernel_launches()}
+        if form == mlgi.BATCH_PERSISTENT:
+            groups[streams] = dict(r, groups=streams)
+        else:
+            forms[name] = dict(r, streams=streams)
         batch.close()
+    g_best = min(groups, key=lambda g: groups[g]["ms_per_batch"])
+    forms = {"persistent": groups[g_best], **forms,
+             "persistent_by_groups": {str(g): round(groups[g]["ms_per_batch"], 4) for g in groups}}
     # plain: the same views, one mlgi_gi_frame per view on one stream
     plain_ms = timed(lambda: [ctx.gi_frame(f.frame_desc(), f.radiance(), ctx.stream()) for f in frames])
     clocks = sampler.stop()
@@ -589,7 +598,7 @@ def measure_batch(local_rank, n_views, steps, warmup, batch_streams):
     ctx.set_timing(False)
     ctx.check_device_status()
     ctx.close()
-    best = min(forms, key=lambda k: forms[k]["ms_per_batch"])
+    best = min(("persistent", "concurrent"), key=lambda k: forms[k]["ms_per_batch"])
     n = len(frames)
     return {"views": n, "form": best, "ms_per_batch": forms[best]["ms_per_batch"],
             "frames_per_s": n / (forms[best]["ms_per_batch"] * 1e-3), "forms": forms, "plain_ms_per_batch": plain_ms,

@@ -166,9 +166,10 @@ mlgi_status mlgi_ism_splat_range(mlgi_ctx* ctx, const mlgi_points* pts, const ml
 mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_params* params, int row0, int row1,
                                mlgi_stream stream);
 /* No counterpart in the reference: the number of kernel launches mlgi_pullpush issues for this
- * geometry -- 1 when an ISM's whole pyramid runs in one block (ISM edges up to 128 with two or more
- * levels, far plane in [2^-20, 2^20]), 4 (2 for one level) otherwise -- or -1 for a geometry
- * mlgi_pullpush refuses. */
+ * geometry -- 1 when each ISM's whole pyramid runs in one block (ISM edges up to 128 with two or
+ * more levels, far plane in [2^-20, 2^20], and at most one wave of such blocks on this GPU: 3 per
+ * SM for edges up to 64, else 2), 4 (2 for one level) otherwise -- or -1 for a geometry
+ * mlgi_pullpush refuses. mlgi_pullpush_rows decides the same way for the ISMs of its rows. */
 int mlgi_pullpush_launches(const mlgi_ism_params* params);
 
 /* No counterpart in the reference. Allocation-free ISM rendering for callers that cannot
@@ -326,16 +327,18 @@ mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_des
 mlgi_status mlgi_batch_launch(mlgi_batch* b, mlgi_stream stream);
 void mlgi_batch_destroy(mlgi_batch* b);
 
-/* Batch forms. PERSISTENT (mlgi_batch_create): one persistent launch per pass over all views.
- * CONCURRENT: each view's own single-frame kernels, the views spread over `streams` CUDA streams
- * (balanced by estimated cost) and joined in one graph, so that the kernels of different views
- * overlap (filling each other's tail waves and launch gaps). Both give results bit-identical to
- * mlgi_gi_frame on each view. */
+/* Batch forms. PERSISTENT (mlgi_batch_create): one persistent launch per pass over all views --
+ * or, with `streams` = G > 1, over each of G view groups (balanced by estimated cost), every group
+ * on its own stream with persistent grids of 1/G of the GPU, so that different groups' passes run
+ * side by side (9 G launches). CONCURRENT: each view's own single-frame kernels, the views spread
+ * over `streams` CUDA streams (balanced the same way) and joined in one graph, so that the kernels
+ * of different views overlap (filling each other's tail waves and launch gaps). All give results
+ * bit-identical to mlgi_gi_frame on each view. */
 #define MLGI_BATCH_PERSISTENT 0
 #define MLGI_BATCH_CONCURRENT 1
 typedef struct {
     int form;     /* MLGI_BATCH_PERSISTENT or MLGI_BATCH_CONCURRENT */
-    int streams;  /* CONCURRENT: streams the views are spread over (0 selects 4) */
+    int streams;  /* PERSISTENT: view groups (0 selects 1); CONCURRENT: streams (0 selects 4); at most 64 */
 } mlgi_batch_opts;
 mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_desc* views,
                                  const mlgi_radiance* outputs, const mlgi_batch_opts* opts, mlgi_batch** out);

@@ -30,7 +30,7 @@ CUDA_UNITS = [
     ("csrc/mlgi_api.cu", []),
     ("csrc/ism_static.cu", []),
     ("csrc/scene_kernels.cu", []),
-    ("csrc/post_kernels.cu", []),
+    ("csrc/post_kernels.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     ("csrc/cluster_kernels.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     ("host/serve.cpp", []),
     ("host/autotune.cpp", []),

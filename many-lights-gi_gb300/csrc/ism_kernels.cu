@@ -878,7 +878,7 @@ static PullPushGrids pullpush_grids(const PullPushArgs& a) {
 
 cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
     if (a.row1 <= a.row0) return cudaSuccess;
-    if (pyramid_fused(a.ism_size, a.levels, a.z_far)) {
+    if (pyramid_launch_fused(a)) {
         launch_pyramid(a, s);
         return cudaGetLastError();
     }
@@ -894,7 +894,7 @@ cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
 
 cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks) {
     if (a.row1 <= a.row0) return cudaSuccess;
-    if (pyramid_fused(a.ism_size, a.levels, a.z_far)) {
+    if (pyramid_launch_fused(a)) {
         const cudaError_t e = pyramid_prepare();
         if (e != cudaSuccess) return e;
         if (marks)  // one launch: the pass's time lands in the last of the four slots

@@ -80,7 +80,9 @@ struct PullPushArgs {
     float4* lv2;          // scratch: pyramid level 2, (atlas_w/4) x (atlas_h/4), when levels >= 2
     uint32_t m_c0, m_c1;  // ceil(2^32 / d) for d = ism_size / 2 and ism_size / 4 when d >= 2, else 0
     int row0, row1;       // the launch covers ISM rows [row0, row1) of the grid (0, grid_y: all)
+    int pyr_form;         // kPyrByCount or kPyrWhereFits (see pyramid_fused)
 };
+constexpr int kPyrByCount = 0, kPyrWhereFits = 1;
 
 struct FgArgs {
     int width, height;
@@ -218,7 +220,9 @@ size_t pullmid_smem_bytes(int ism_size, int levels);
 // Whether launch_pullpush runs an ISM's whole pyramid in one block (pyramid_kernel, no scratch;
 // ISM edges up to 128, far plane in [2^-20, 2^20]) rather than in four launches over the lv1/lv2
 // scratch; its shared memory per block.
-bool pyramid_fused(int ism_size, int levels, float z_far);
+bool pyramid_fits(int ism_size, int levels, float z_far);
+bool pyramid_fused(int ism_size, int levels, float z_far, long long n_isms);
+bool pyramid_launch_fused(const PullPushArgs& a);
 size_t pyramid_smem_bytes(int ism_size, int levels);
 size_t pullpush_scratch_bytes(int atlas_w, int atlas_h, int levels, size_t* lv2_offset);
 int pullpush_batch_items(int pass, int atlas_w, int atlas_h, int ism_count, int levels);

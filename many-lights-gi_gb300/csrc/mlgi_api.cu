@@ -1,6 +1,7 @@
 // C ABI of the GI hot path: argument checking, context-owned buffers, per-pass timing and the
 // frame-level chain (GIStage::process's GI part, GIStage.cpp:346-418).
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -306,7 +307,8 @@ mlgi_status check_atlas(mlgi_ctx* ctx, const mlgi_atlas* a, const mlgi_ism_param
 // Pull-push scratch of a context: the lv1/lv2 levels of the four-launch form, none for ISMs whose
 // pyramid runs in one block (a token allocation, so that the scratch pointer is never NULL).
 size_t pullpush_scratch_need(int atlas_w, int atlas_h, const mlgi_ism_params* p) {
-    if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far)) return 16;
+    // the whole atlas in one block per ISM: then every launch over some of its rows is too
+    if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far, (long long)p->grid_x * p->grid_y)) return 16;
     return std::max<size_t>(16, mlgi::pullpush_scratch_bytes(atlas_w, atlas_h, p->levels, nullptr));
 }
 
@@ -699,7 +701,7 @@ mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_
 int mlgi_pullpush_launches(const mlgi_ism_params* p) {
     char why[160];
     if (!mlgi::ism_params_valid(p, why, sizeof(why))) return -1;
-    if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far)) return 1;
+    if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far, (long long)p->grid_x * p->grid_y)) return 1;
     return p->levels >= 2 ? 4 : 2;
 }
 
@@ -1143,7 +1145,7 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     // form keeps runs of at most 3/16 of the grid alternating between the two streams. Runs write
     // disjoint rows.
     const int gy = d.ism.grid_y;
-    const bool one_block = mlgi::pyramid_fused(d.ism.ism_size, d.ism.levels, d.ism.z_far);
+    const bool one_block = mlgi::pyramid_fits(d.ism.ism_size, d.ism.levels, d.ism.z_far);
     const int final_rows = h.chunks > 1 && !one_block ? std::max(2, 3 * gy / 16) : gy;
     std::vector<char> done(gy, 0);
     MLGI_CUDA(ctx, mlgi::pullpush_prepare(mlgi::pullmid_smem_bytes(d.ism.ism_size, d.ism.levels)));
@@ -1158,6 +1160,7 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
             mlgi::PullPushArgs part = pa;
             part.row0 = r;
             part.row1 = r1;
+            part.pyr_form = mlgi::kPyrWhereFits;
             const cudaError_t e = mlgi::launch_pullpush_captured(part, last && (run & 1) == 0 ? s : s2);
             if (e != cudaSuccess) return e;
             ++run;
@@ -1333,12 +1336,16 @@ struct mlgi_batch {
     mlgi::BatchView* h_views = nullptr;  // pinned host copy, uploaded by the graph
     mlgi::BatchView* d_views = nullptr;
     int* d_prefix = nullptr;
-    int grid[mlgi::kBpCount] = {};
     size_t pp_smem = 0;  // shared memory of the per-ISM middle-level pass
     int form = MLGI_BATCH_PERSISTENT;
     int launches = 0;                  // kernels per mlgi_batch_launch
-    std::vector<cudaStream_t> side;    // concurrent form: the views' streams (used during capture)
-    std::vector<cudaEvent_t> events;   // concurrent form: fork and join events of the capture
+    // persistent form: the views in groups, each group's views contiguous in the view table
+    // (view i at slot[i]) with its own running item counts and grids
+    std::vector<int> slot;
+    std::vector<int> group_start;      // groups + 1 slots
+    std::vector<std::array<int, mlgi::kBpCount>> grid;  // per group and pass
+    std::vector<cudaStream_t> side;    // the groups' (persistent) or views' (concurrent) streams
+    std::vector<cudaEvent_t> events;   // fork and join events of the capture
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1403,66 +1410,81 @@ mlgi_status build_view(mlgi_ctx* ctx, const mlgi_frame_desc& f, const mlgi_radia
     return MLGI_OK;
 }
 
-// Capture the batch's graph from its view table: the table upload and one persistent launch per
-// pass, or (concurrent form) each view's kernels on its stream between a fork and a join.
+// Views into k lanes of about equal work: costliest first onto the least-loaded lane, the cost
+// estimated from the work measured per unit at 1080p (gathered pairs, splatted points, atlas
+// texels).
+std::vector<std::vector<int>> balance_views(const mlgi_frame_desc* views, int n_views, int k) {
+    std::vector<std::pair<double, int>> cost;
+    for (int i = 0; i < n_views; ++i) {
+        const mlgi_frame_desc& f = views[i];
+        const double pairs =
+            (double)f.gbuffer.width * f.gbuffer.height * f.vpl.count / ((double)f.fg.interleave * f.fg.interleave);
+        const double texels = (double)f.ism.grid_x * f.ism.ism_size * f.ism.grid_y * f.ism.ism_size;
+        const double points = (double)f.points.n_buckets * f.points.bucket_stride;
+        cost.push_back({pairs * 4.3e-9 + points * 4.1e-8 + texels * 1.9e-8, i});
+    }
+    std::sort(cost.begin(), cost.end(), std::greater<std::pair<double, int>>());
+    std::vector<double> load(k, 0.0);
+    std::vector<std::vector<int>> lane(k);
+    for (const auto& c : cost) {
+        const int j = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[j] += c.first;
+        lane[j].push_back(c.second);
+    }
+    return lane;
+}
+
+// Capture the batch's graph from its view table: the table upload and, per view group, one
+// persistent launch per pass on the group's stream (groups forked from and joined to the batch
+// stream when there are several), or (concurrent form) each view's kernels on its stream between
+// a fork and a join.
 mlgi_status capture_batch(mlgi_batch* b) {
     const int n_views = b->n, form = b->form;
     const mlgi_frame_desc* views = b->frames.data();
-    const mlgi::BatchTable t{b->d_views, b->d_prefix, n_views};
     b->launches = 0;
     cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
     if (form == MLGI_BATCH_PERSISTENT) {
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(mlgi::BatchView) * n_views, cudaMemcpyHostToDevice,
                                 b->stream);
-        for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid, mlgi::kBpPush1,
-                      mlgi::kBpPush0}) {
-            if (e == cudaSuccess && b->grid[p] > 0) {
-                e = mlgi::launch_batch_ism(t, p, b->grid[p], p == mlgi::kBpPullMid ? b->pp_smem : 0, b->stream);
-                ++b->launches;
+        const int G = (int)b->group_start.size() - 1;
+        if (G > 1 && e == cudaSuccess) e = cudaEventRecord(b->events[G], b->stream);  // fork
+        for (int g = 0; g < G; ++g) {
+            const int v0 = b->group_start[g], ng = b->group_start[g + 1] - v0;
+            const mlgi::BatchTable tg{b->d_views + v0, b->d_prefix + (size_t)mlgi::kBpCount * (v0 + g), ng};
+            cudaStream_t s = G > 1 ? b->side[g] : b->stream;
+            if (G > 1 && e == cudaSuccess) e = cudaStreamWaitEvent(s, b->events[G], 0);
+            for (int p : {mlgi::kBpClear, mlgi::kBpVpl, mlgi::kBpSplat, mlgi::kBpPull1, mlgi::kBpPullMid,
+                          mlgi::kBpPush1, mlgi::kBpPush0}) {
+                if (e == cudaSuccess && b->grid[g][p] > 0) {
+                    e = mlgi::launch_batch_ism(tg, p, b->grid[g][p], p == mlgi::kBpPullMid ? b->pp_smem : 0, s);
+                    ++b->launches;
+                }
             }
-        }
-        for (int p : {mlgi::kBpFg, mlgi::kBpFg16}) {
-            if (e == cudaSuccess && b->grid[p] > 0) {
-                e = mlgi::launch_batch_fg(t, p, b->grid[p], b->stream);
-                ++b->launches;
+            for (int p : {mlgi::kBpFg, mlgi::kBpFg16}) {
+                if (e == cudaSuccess && b->grid[g][p] > 0) {
+                    e = mlgi::launch_batch_fg(tg, p, b->grid[g][p], s);
+                    ++b->launches;
+                }
             }
+            if (G > 1 && e == cudaSuccess) e = cudaEventRecord(b->events[g], s);  // join
+            if (G > 1 && e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->events[g], 0);
         }
     } else {
-        // views to streams, costliest first onto the least-loaded stream (estimated from the work
-        // measured per unit at 1080p: gathered pairs, splatted points, atlas texels)
         const int k = (int)b->side.size();
-        std::vector<std::pair<double, int>> cost;
-        for (int i = 0; i < n_views; ++i) {
-            const mlgi_frame_desc& f = views[i];
-            const double pairs = (double)f.gbuffer.width * f.gbuffer.height * f.vpl.count /
-                                 ((double)f.fg.interleave * f.fg.interleave);
-            const double texels = (double)f.ism.grid_x * f.ism.ism_size * f.ism.grid_y * f.ism.ism_size;
-            const double points = (double)f.points.n_buckets * f.points.bucket_stride;
-            cost.push_back({pairs * 4.3e-9 + points * 4.1e-8 + texels * 1.9e-8, i});
-        }
-        std::sort(cost.begin(), cost.end(), std::greater<std::pair<double, int>>());
-        std::vector<double> load(k, 0.0);
-        std::vector<std::vector<int>> lane(k);
-        for (const auto& c : cost) {
-            const int j = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-            load[j] += c.first;
-            lane[j].push_back(c.second);
-        }
+        const std::vector<std::vector<int>> lane = balance_views(views, n_views, k);
         if (e == cudaSuccess) e = cudaEventRecord(b->events[k], b->stream);  // fork
         for (int j = 0; j < k && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(b->side[j], b->events[k], 0);
         for (int j = 0; j < k; ++j) {
             for (int i : lane[j]) {
-                const mlgi::BatchView& v = b->h_views[i];
+                const mlgi::BatchView& v = b->h_views[b->slot[i]];
                 cudaStream_t s = b->side[j];
                 if (e == cudaSuccess) e = mlgi::launch_vpl_process(v.vpl, s);
                 if (e == cudaSuccess) e = mlgi::launch_ism_clear(v.keys, v.atlas_texels, s);
                 if (e == cudaSuccess) e = mlgi::launch_ism_splat(v.splat, s);
                 if (e == cudaSuccess) e = mlgi::launch_pullpush_captured(v.pp, s);
                 if (e == cudaSuccess) e = mlgi::launch_final_gather(v.fg, s);
-                b->launches += 3 + (mlgi::pyramid_fused(v.pp.ism_size, v.pp.levels, v.pp.z_far) ? 1
-                                    : v.pp.levels >= 2                                          ? 4
-                                                                                                : 2) + 1;
+                b->launches += 3 + (mlgi::pyramid_launch_fused(v.pp) ? 1 : v.pp.levels >= 2 ? 4 : 2) + 1;
             }
             if (e == cudaSuccess) e = cudaEventRecord(b->events[j], b->side[j]);  // join
             if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->events[j], 0);
@@ -1511,6 +1533,8 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
     const int form = opts ? opts->form : MLGI_BATCH_PERSISTENT;
     if (form != MLGI_BATCH_PERSISTENT && form != MLGI_BATCH_CONCURRENT) return fail(ctx, MLGI_EINVAL, "bad batch form");
     if (opts && (opts->streams < 0 || opts->streams > 64)) return fail(ctx, MLGI_EINVAL, "streams must be 0..64");
+    // persistent form: view groups (0 selects 1); concurrent form: streams (0 selects 4)
+    const int G = form == MLGI_BATCH_PERSISTENT ? std::min(n_views, opts && opts->streams > 0 ? opts->streams : 1) : 1;
     *out = nullptr;
     mlgi_batch* b = new mlgi_batch();
     b->form = form;
@@ -1532,27 +1556,59 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
     }
     if (mlgi::pinned_alloc((void**)&b->h_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
         mlgi::dev_alloc((void**)&b->d_views, sizeof(mlgi::BatchView) * n_views) != cudaSuccess ||
-        mlgi::dev_alloc((void**)&b->d_prefix, sizeof(int) * mlgi::kBpCount * (n_views + 1)) != cudaSuccess) {
+        mlgi::dev_alloc((void**)&b->d_prefix, sizeof(int) * mlgi::kBpCount * (n_views + G)) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(ctx, MLGI_ENOMEM, "batch tables"));
     }
-    std::vector<int> prefix(mlgi::kBpCount * (n_views + 1), 0);
-    for (int i = 0; i < n_views; ++i) {
-        int counts[mlgi::kBpCount];
-        const mlgi_status st = build_view(ctx, views[i], outputs[i], static_cast<char*>(b->arena) + b->arena_off[i],
-                                          b->h_views[i], counts);
-        if (st != MLGI_OK) return bail(st);
-        for (int p = 0; p < mlgi::kBpCount; ++p) prefix[p * (n_views + 1) + i + 1] = prefix[p * (n_views + 1) + i] + counts[p];
-        b->pp_smem = std::max(b->pp_smem, mlgi::pullmid_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
+    // view groups: one keeps the views' order; several are balanced by estimated work
+    std::vector<std::vector<int>> groups;
+    if (G == 1) {
+        groups.assign(1, std::vector<int>(n_views));
+        std::iota(groups[0].begin(), groups[0].end(), 0);
+    } else {
+        groups = balance_views(views, n_views, G);
+    }
+    std::vector<int> order;  // slot -> view
+    b->slot.assign(n_views, 0);
+    b->group_start.assign(1, 0);
+    for (const auto& grp : groups) {
+        for (int i : grp) {
+            b->slot[i] = (int)order.size();
+            order.push_back(i);
+        }
+        b->group_start.push_back((int)order.size());
+    }
+    // per group: running item counts per pass, kBpCount x (views + 1) ints after the earlier groups'
+    std::vector<int> prefix((size_t)mlgi::kBpCount * (n_views + G), 0);
+    for (int g = 0; g < G; ++g) {
+        const int v0 = b->group_start[g], ng = b->group_start[g + 1] - v0;
+        int* pre = prefix.data() + (size_t)mlgi::kBpCount * (v0 + g);
+        for (int j = 0; j < ng; ++j) {
+            const int i = order[v0 + j];
+            int counts[mlgi::kBpCount];
+            const mlgi_status st = build_view(ctx, views[i], outputs[i], static_cast<char*>(b->arena) + b->arena_off[i],
+                                              b->h_views[v0 + j], counts);
+            if (st != MLGI_OK) return bail(st);
+            for (int p = 0; p < mlgi::kBpCount; ++p) pre[p * (ng + 1) + j + 1] = pre[p * (ng + 1) + j] + counts[p];
+            b->pp_smem = std::max(b->pp_smem, mlgi::pullmid_smem_bytes(views[i].ism.ism_size, views[i].ism.levels));
+        }
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    for (int p = 0; p < mlgi::kBpCount; ++p) {
-        const int items = prefix[p * (n_views + 1) + n_views];
-        const int per_sm = p == mlgi::kBpFg || p == mlgi::kBpFg16
-                               ? 8
-                               : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
-        b->grid[p] = std::min(items, std::max(1, sms) * per_sm);
+    // every group's persistent grids fill the GPU: the blocks of one group's pass take the SMs that
+    // the other groups' passes leave idle in their tail waves (grids of 1/G of the GPU measured
+    // slower: a group alone then uses only its share)
+    b->grid.assign(G, {});
+    for (int g = 0; g < G; ++g) {
+        const int v0 = b->group_start[g], ng = b->group_start[g + 1] - v0;
+        const int* pre = prefix.data() + (size_t)mlgi::kBpCount * (v0 + g);
+        for (int p = 0; p < mlgi::kBpCount; ++p) {
+            const int items = pre[p * (ng + 1) + ng];
+            const int per_sm = p == mlgi::kBpFg || p == mlgi::kBpFg16
+                                   ? 8
+                                   : mlgi::batch_blocks_per_sm(p, p == mlgi::kBpPullMid ? b->pp_smem : 0);
+            b->grid[g][p] = std::min(items, std::max(1, sms) * per_sm);
+        }
     }
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMemcpy(b->d_prefix, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -1560,8 +1616,8 @@ mlgi_status mlgi_batch_create_ex(mlgi_ctx* ctx, int n_views, const mlgi_frame_de
         return bail(fail(ctx, MLGI_ECUDA, "batch set-up"));
     }
     cudaError_t e = cudaSuccess;
-    if (form == MLGI_BATCH_CONCURRENT) {
-        const int k = std::min(n_views, opts && opts->streams > 0 ? opts->streams : 4);
+    if (form == MLGI_BATCH_CONCURRENT || G > 1) {
+        const int k = form == MLGI_BATCH_PERSISTENT ? G : std::min(n_views, opts && opts->streams > 0 ? opts->streams : 4);
         b->side.assign(k, nullptr);
         b->events.assign(k + 1, nullptr);
         for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking);
@@ -1591,7 +1647,7 @@ mlgi_status mlgi_batch_update_view(mlgi_batch* b, int view, const mlgi_frame_des
     mlgi::BatchView v;
     const mlgi_status st = build_view(ctx, *desc, *output, static_cast<char*>(b->arena) + b->arena_off[view], v, counts);
     if (st != MLGI_OK) return st;
-    b->h_views[view] = v;
+    b->h_views[b->slot[view]] = v;
     b->frames[view] = *desc;
     if (b->form == MLGI_BATCH_CONCURRENT) {  // its graph holds the kernel arguments: capture it again
         if (b->exec) cudaGraphExecDestroy(b->exec);

@@ -1,10 +1,11 @@
 // After the gathering: the R11G11B10F GI buffer format, the separable bilateral blur and the GI
 // part of the deferred composite.
 //
-// The reference runs the blur and the composite as GL fragment shaders, whose arithmetic GL does
-// not pin to the bit, so these kernels use fast FP32 (FMA contraction, approximate division and
-// reciprocal square root, __powf) and match the oracle within stated tolerances; the R11G11B10F
-// conversions are exact bit manipulations:
+// This translation unit is compiled with -fmad=false and IEEE division and square root. The blur
+// performs the shader's operations in the shader's order (normalize as v / length(v), sums from
+// +0), so its output equals the oracle's bit for bit. The composite takes its powers with the fast
+// __powf (the accurate powf cost 2.5 times the pass's time and still is not the oracle's pow), within
+// a stated tolerance of the oracle; the R11G11B10F conversions are exact bit manipulations:
 //   gi_blur_kernel    <- data/shaders/gi/gi_blur.frag:24-72 driven by GIStage::blur (GIStage.cpp:308-344)
 //   composite_kernel  <- data/shaders/deferredshading.frag:39-44, 69-80 (GI ambient term, Reinhard, toSRGB)
 //   R11G11B10F        <- the GI buffers' GL_R11F_G11F_B10F (GIStage.cpp:470)
@@ -103,7 +104,7 @@ constexpr int kBlurTx = 32, kBlurTy = 16, kBlurR = 3;  // KERNEL_RADIUS (gi_blur
 constexpr int kBlurThreads = 256;
 constexpr int kRegW = kBlurTx + 2 * kBlurR, kRegH = kBlurTy + 2 * kBlurR;
 
-// the gathering's octahedral decode (fg_kernels.cu), normalised with a reciprocal square root
+// the gathering's octahedral decode (fg_kernels.cu), normalised as GLSL's normalize: v / length(v)
 __device__ __forceinline__ v3 blur_oct_decode(float ex, float ey) {
     v3 n = mk(ex, ey, 1.0f - fabsf(ex) - fabsf(ey));
     if (n.z < 0.f) {
@@ -111,7 +112,8 @@ __device__ __forceinline__ v3 blur_oct_decode(float ex, float ey) {
         n.x = (1.0f - fabsf(ey)) * sx;
         n.y = (1.0f - fabsf(ex)) * sy;
     }
-    return n * rsqrtf(dot(n, n));
+    const float len = sqrtf(dot(n, n));
+    return mk(n.x / len, n.y / len, n.z / len);
 }
 
 struct BlurSmem {
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(kBlurThreads) gi_blur_kernel(BlurArgs a) {
         const size_t p = MLGI_IX((size_t)gy * a.width + gx, (size_t)a.width * a.height);
         // linearDepth (reprojection.glsl:6-14)
         const float z_n = 2.0f * __ldg(a.depth + p) - 1.0f;
-        const float lin = __fdividef(-a.proj_b, a.proj_a + z_n);
+        const float lin = -a.proj_b / (a.proj_a + z_n);
         float ex, ey;
         if (a.normal_f16) {
             const __half2 h = reinterpret_cast<const __half2*>(a.normal)[p];
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(kBlurThreads) gi_blur_kernel(BlurArgs a) {
         const float4 cg = S.gi[ry][cx];
         if (cg.w == 0.f) continue;  // outside the image: never read by an output inside it
         const float4 c = S.nl[ry][cx];
-        v3 acc = mk(cg.x, cg.y, cg.z);
+        v3 acc = mk(0.0f + cg.x, 0.0f + cg.y, 0.0f + cg.z);  // the shader's sums start at +0
         float factorAcc = 1.0f;
 #pragma unroll
         for (int side = -1; side <= 1; side += 2)
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(kBlurThreads) gi_blur_kernel(BlurArgs a) {
                 const float4 g = S.gi[ry][cx + side * i];
                 if (g.w != 0.f) blur_sample(c, S.nl[ry][cx + side * i], g, float(i), acc, factorAcc);
             }
-        v3 o = acc * __fdividef(1.0f, factorAcc);
+        v3 o = mk(acc.x / factorAcc, acc.y / factorAcc, acc.z / factorAcc);
         if (a.packed) o = unpack_r11g11b10f(pack_r11g11b10f(o));  // the temp buffer is R11G11B10F
         S.tx[ry][tx] = make_float4(o.x, o.y, o.z, 0.f);
     }
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(kBlurThreads) gi_blur_kernel(BlurArgs a) {
         const int cy = ty + kBlurR, cx = tx + kBlurR;
         const float4 c = S.nl[cy][cx];
         const float4 ct = S.tx[cy][tx];
-        v3 acc = mk(ct.x, ct.y, ct.z);
+        v3 acc = mk(0.0f + ct.x, 0.0f + ct.y, 0.0f + ct.z);
         float factorAcc = 1.0f;
 #pragma unroll
         for (int side = -1; side <= 1; side += 2)
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(kBlurThreads) gi_blur_kernel(BlurArgs a) {
             for (int i = 1; i <= kBlurR; ++i)
                 if (S.gi[cy + side * i][cx].w != 0.f)
                     blur_sample(c, S.nl[cy + side * i][cx], S.tx[cy + side * i][tx], float(i), acc, factorAcc);
-        const v3 o = acc * __fdividef(1.0f, factorAcc);
+        const v3 o = mk(acc.x / factorAcc, acc.y / factorAcc, acc.z / factorAcc);
         const size_t p = MLGI_IX((size_t)gy * a.width + gx, (size_t)a.width * a.height);
         if (a.packed) {
             reinterpret_cast<uint32_t*>(a.gi_out)[p] = pack_r11g11b10f(o);
@@ -228,13 +230,12 @@ __device__ __forceinline__ v3 composite_pixel(const CompositeArgs& a, const v3 g
     const float gamma = 2.2f;  // srgb_utils.glsl:6 (linearRendering)
     const float inv_gamma = 1.0f / gamma;
     // toLinear(texture(diffuseSampler).xyz): RGBA8 UNORM, then pow(v, gamma)
-    const v3 diffuse = mk(__powf(float(al & 0xFFu) * (1.0f / 255.0f), gamma),
-                          __powf(float((al >> 8) & 0xFFu) * (1.0f / 255.0f), gamma),
-                          __powf(float((al >> 16) & 0xFFu) * (1.0f / 255.0f), gamma));
+    const v3 diffuse = mk(__powf(float(al & 0xFFu) / 255.0f, gamma), __powf(float((al >> 8) & 0xFFu) / 255.0f, gamma),
+                          __powf(float((al >> 16) & 0xFFu) / 255.0f, gamma));
     v3 c = gi * diffuse * occlusion + direct;  // ambientTerm + (diffuseTerm + specularTerm)
     // tonemap (deferredshading.frag:39-44)
     c = c * a.exposure;
-    c = mk(__fdividef(c.x, 1.0f + c.x), __fdividef(c.y, 1.0f + c.y), __fdividef(c.z, 1.0f + c.z));
+    c = mk(c.x / (1.0f + c.x), c.y / (1.0f + c.y), c.z / (1.0f + c.z));
     // toSRGB
     return mk(__powf(c.x, inv_gamma), __powf(c.y, inv_gamma), __powf(c.z, inv_gamma));
 }

@@ -50,9 +50,45 @@ size_t pyramid_smem_bytes(int ism_size, int levels) {
     return b;
 }
 
-bool pyramid_fused(int ism_size, int levels, float z_far) {
+bool pyramid_fits(int ism_size, int levels, float z_far) {
     return levels >= 2 && ism_size % 4 == 0 && pyramid_smem_bytes(ism_size, levels) <= kPyramidSmemMax &&
            z_far >= 0x1p-20f && z_far <= 0x1p+20f;
+}
+
+// ISM blocks the GPU holds at once: three per SM for edges up to 64, else two (the kernel forms
+// below), times the current device's SMs (152 when it cannot be asked).
+long long pyramid_wave(int ism_size) {
+    constexpr int kMaxDevices = 64;
+    static int sms[kMaxDevices] = {};
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        n = 152;
+    } else if (!(n = sms[dev])) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 152;
+        }
+        sms[dev] = n;
+    }
+    return (long long)n * (ism_size > 64 ? 2 : 3);
+}
+
+// One block per ISM runs a launch of n_isms ISMs when the pyramid fits and the ISMs make at most
+// one wave of blocks. Beyond a wave the per-level launches are faster, its middle levels being a
+// chain of barrier-separated steps with few threads busy (GB300, ms for fused / per level:
+// 64^2 ISMs 256: 0.035 / 0.045, 512: 0.058 / 0.057, 1024: 0.095 / 0.085, 4096: 0.366 / 0.262;
+// 128^2 ISMs 256: 0.080 / 0.086, 1024: 0.253 / 0.245; 96^2 ISMs 1024: 0.158 / 0.150).
+bool pyramid_fused(int ism_size, int levels, float z_far, long long n_isms) {
+    return pyramid_fits(ism_size, levels, z_far) && n_isms <= pyramid_wave(ism_size);
+}
+
+// The form of a launch: one block per ISM when its arguments ask for it wherever it fits
+// (kPyrWhereFits), else by pyramid_fused.
+bool pyramid_launch_fused(const PullPushArgs& a) {
+    return a.pyr_form == kPyrWhereFits ? pyramid_fits(a.ism_size, a.levels, a.z_far)
+                                       : pyramid_fused(a.ism_size, a.levels, a.z_far,
+                                                       (long long)(a.row1 - a.row0) * a.grid_x);
 }
 
 __device__ __forceinline__ void fill_pyramid_tables(PyramidTables& T, const float z_far) {

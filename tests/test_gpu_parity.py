@@ -188,7 +188,9 @@ def test_ism_splat_empty_buckets(ctx):
 @pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2, mlgi.C3B.replace(reduced=False, name="c3b_fp32")],
                          ids=lambda c: c.name)
 def test_pullpush_bit_exact(ctx, cfg):
-    """The one-block-per-ISM pyramid vs the level-by-level restatement of pull.comp/push.comp."""
+    """mlgi_pullpush vs the level-by-level restatement of pull.comp/push.comp: one block per ISM
+    where the atlas's ISMs make at most one wave of blocks (C0, C1, C3), else the per-level launches
+    (C2, C3-B)."""
     import torch
 
     sc = scene(cfg)
@@ -202,6 +204,31 @@ def test_pullpush_bit_exact(ctx, cfg):
     torch.cuda.synchronize()
     fin = df.atlas_np()
     assert (ofin < 0.99).mean() > (okeys >> 8 < 0.99 * 2 ** 24).mean()  # the pyramid fills holes
+    mism = int((fin.view(np.uint32) != ofin.view(np.uint32)).sum())
+    assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
+
+
+@pytest.mark.parametrize("cfg", [mlgi.C2, mlgi.C3B.replace(reduced=False, name="c3b_fp32")], ids=lambda c: c.name)
+def test_one_block_pyramid_on_large_atlases_bit_exact(ctx, cfg):
+    """The one-block-per-ISM pyramid on atlases of several waves of ISMs, run as mlgi_pullpush_rows
+    over row runs of at most one wave each (152 SMs x 2 blocks of 128^2 or 96^2 ISMs: 304, so runs of
+    8 rows of 32 or 4 rows of 64 ISMs), against the oracle."""
+    import torch
+
+    sc = scene(cfg)
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    ofin = O.pullpush(okeys, cfg.ism_size, cfg.levels, cfg.z_far)
+    assert mlgi.pullpush_launches(cfg) == 4  # the whole atlas: several waves, level by level
+    df = DeviceFrame(sc)
+    df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
+    ip = mlgi.ism_params(cfg)
+    rows = max(1, 256 // cfg.grid_x)
+    for r0 in range(0, cfg.grid_y, rows):
+        ctx.pullpush_rows(df.atlas_view(), ip, r0, min(cfg.grid_y, r0 + rows))
+    torch.cuda.synchronize()
+    fin = df.atlas_np()
     mism = int((fin.view(np.uint32) != ofin.view(np.uint32)).sum())
     assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
 

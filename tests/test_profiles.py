@@ -1,6 +1,7 @@
 """The committed ncu summary of the C2 frame carries, for every kernel ncu captured in full (the
-pull-push pyramid, the gathering and the splat), the per-launch DRAM bytes and issue-slot use
-that bench.py reports beside the roofline fraction, and bench.py reads them back."""
+splat, push level 0, the gathering and the one-block pyramid of the host-buffer frame), the
+per-launch DRAM bytes and issue-slot use that bench.py reports beside the roofline fraction, and
+bench.py reads them back."""
 import os
 import sys
 
@@ -11,7 +12,7 @@ sys.path.insert(0, ROOT)
 
 import bench  # noqa: E402
 
-KERNELS = ["pyramid", "ism_splat", "final_gather"]
+KERNELS = ["ism_splat", "push0", "final_gather", "pyramid"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
