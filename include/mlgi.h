@@ -168,8 +168,12 @@ mlgi_status mlgi_pullpush_rows(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_
 /* No counterpart in the reference: the number of kernel launches mlgi_pullpush issues for this
  * geometry -- 1 when each ISM's whole pyramid runs in one block (ISM edges up to 128 with two or
  * more levels, far plane in [2^-20, 2^20], and at most one wave of such blocks on this GPU: 3 per
- * SM for edges up to 64, else 2), 4 (2 for one level) otherwise -- or -1 for a geometry
- * mlgi_pullpush refuses. mlgi_pullpush_rows decides the same way for the ISMs of its rows. */
+ * SM for edges up to 64, else 2); otherwise the per-level launches, 4 (2 for one level), for each
+ * half of the ISM rows when the grid has two or more rows (the halves run side by side on the
+ * caller's stream and the context's stream); -1 for a geometry mlgi_pullpush refuses.
+ * mlgi_pullpush_rows chooses between the two forms the same way for the ISMs of its rows, and
+ * launches one sequence. With per-pass timing, a pull-push in one block or in two halves reports
+ * its time in the last of its four slots. */
 int mlgi_pullpush_launches(const mlgi_ism_params* params);
 
 /* No counterpart in the reference. Allocation-free ISM rendering for callers that cannot

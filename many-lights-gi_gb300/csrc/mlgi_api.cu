@@ -190,6 +190,7 @@ struct mlgi_ctx {
     bool timed_frame = false;
     cudaEvent_t ev[kNumEvents] = {};
     cudaEvent_t ev_pp[3] = {};  // inside the pull-push pass
+    cudaEvent_t ev_pp_fork = nullptr, ev_pp_join = nullptr;  // the per-level pass's two halves
     // host-buffer frames: the upload stream and its events (RSM, point ranges, G-buffer)
     cudaStream_t copy = nullptr;
     cudaEvent_t ev_rsm = nullptr, ev_gbuf = nullptr, ev_pts[kHostPointChunks] = {};
@@ -306,6 +307,12 @@ mlgi_status check_atlas(mlgi_ctx* ctx, const mlgi_atlas* a, const mlgi_ism_param
 
 // Pull-push scratch of a context: the lv1/lv2 levels of the four-launch form, none for ISMs whose
 // pyramid runs in one block (a token allocation, so that the scratch pointer is never NULL).
+// Whether mlgi_pullpush runs the per-level launches as two halves of the ISM rows side by side.
+bool pullpush_halves(const mlgi_ism_params* p) {
+    return p->grid_y >= 2 &&
+           !mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far, (long long)p->grid_x * p->grid_y);
+}
+
 size_t pullpush_scratch_need(int atlas_w, int atlas_h, const mlgi_ism_params* p) {
     // the whole atlas in one block per ISM: then every launch over some of its rows is too
     if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far, (long long)p->grid_x * p->grid_y)) return 16;
@@ -348,6 +355,8 @@ mlgi_status mlgi_create(mlgi_ctx** out, const mlgi_ctx_desc* desc) {
         e = cudaEventCreateWithFlags(&ctx->ev_pts[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_pp_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_pp_join, cudaEventDisableTiming);
     for (int i = 0; e == cudaSuccess && i < kHostBands; ++i)
         e = cudaEventCreateWithFlags(&ctx->ev_band[i], cudaEventDisableTiming);
     for (int i = 0; e == cudaSuccess && i < kHostPointChunks; ++i)
@@ -385,7 +394,7 @@ void mlgi_destroy(mlgi_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->ev_split)
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_side, ctx->ev_begin, ctx->ev_end})
+    for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_side, ctx->ev_begin, ctx->ev_end, ctx->ev_pp_fork, ctx->ev_pp_join})
         if (e) cudaEventDestroy(e);
     if (ctx->hgraph.exec) cudaGraphExecDestroy(ctx->hgraph.exec);
     for (cudaStream_t cs : {ctx->copy, ctx->side})
@@ -635,7 +644,26 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
     if (st != MLGI_OK) return st;
     mlgi::PullPushArgs a;
     if ((st = build_pullpush_args(ctx, atlas, p, ctx->pp.p, a)) != MLGI_OK) return st;
-    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, pick(ctx, stream), ctx->timing ? ctx->ev_pp : nullptr));
+    cudaStream_t s = pick(ctx, stream);
+    if (pullpush_halves(p)) {
+        // the per-level launches over the two halves of the ISM rows side by side, on the caller's
+        // stream and the context's side stream: their kernels fill each other's tail waves and the
+        // latency-bound middle levels (C2 0.251 -> 0.242 ms, CREF 0.081 -> 0.074, C3-B 0.275 ->
+        // 0.256; three or four parts were no faster). The halves write disjoint rows, and a quad
+        // on a half's border reads the other half's coarse texels only with weight 0.
+        mlgi::PullPushArgs lo = a, hi = a;
+        lo.row1 = hi.row0 = p->grid_y / 2;
+        if (ctx->timing)  // no per-level times for the two halves: the pass's time lands in its last slot
+            for (int k = 0; k < 3; ++k) MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp[k], s));
+        MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp_fork, s));
+        MLGI_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_pp_fork, 0));
+        MLGI_CUDA(ctx, mlgi::launch_pullpush(lo, s));
+        MLGI_CUDA(ctx, mlgi::launch_pullpush(hi, ctx->side));
+        MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp_join, ctx->side));
+        MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_pp_join, 0));
+        return MLGI_OK;
+    }
+    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, s, ctx->timing ? ctx->ev_pp : nullptr));
     return MLGI_OK;
 }
 
@@ -702,7 +730,7 @@ int mlgi_pullpush_launches(const mlgi_ism_params* p) {
     char why[160];
     if (!mlgi::ism_params_valid(p, why, sizeof(why))) return -1;
     if (mlgi::pyramid_fused(p->ism_size, p->levels, p->z_far, (long long)p->grid_x * p->grid_y)) return 1;
-    return p->levels >= 2 ? 4 : 2;
+    return (p->levels >= 2 ? 4 : 2) * (pullpush_halves(p) ? 2 : 1);
 }
 
 mlgi_status mlgi_cluster_lights(mlgi_ctx* ctx, const mlgi_gbuffer_view* g, const mlgi_vpl_buf* vpls, int n_vpl,

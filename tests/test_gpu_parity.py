@@ -220,7 +220,7 @@ def test_one_block_pyramid_on_large_atlases_bit_exact(ctx, cfg):
     okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
                         cfg.grid_y, cfg.z_far)
     ofin = O.pullpush(okeys, cfg.ism_size, cfg.levels, cfg.z_far)
-    assert mlgi.pullpush_launches(cfg) == 4  # the whole atlas: several waves, level by level
+    assert mlgi.pullpush_launches(cfg) == 8  # the whole atlas: several waves, level by level in two halves
     df = DeviceFrame(sc)
     df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
     ip = mlgi.ism_params(cfg)
@@ -248,7 +248,7 @@ def test_pullpush_per_level_form_bit_exact(ctx, geom):
                         cfg.grid_y, cfg.z_far)
     g = cfg.replace(ism_size=ism, grid_x=gx, grid_y=gy, levels=levels, name="per_level")
     assert (g.atlas_w, g.atlas_h) == (cfg.atlas_w, cfg.atlas_h)
-    assert mlgi.pullpush_launches(g) == (4 if levels >= 2 else 2)
+    assert mlgi.pullpush_launches(g) == (4 if levels >= 2 else 2) * 2  # two halves of the ISM rows
     ofin = O.pullpush(okeys, ism, levels, cfg.z_far)
     df = DeviceFrame(sc)
     df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
