@@ -233,12 +233,14 @@ def test_one_block_pyramid_on_large_atlases_bit_exact(ctx, cfg):
     assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
 
 
-@pytest.mark.parametrize("geom", [(mlgi.C1, 256, 4, 4, 4), (mlgi.C0, 32, 8, 8, 1)],
-                         ids=["c1_keys_as_256px_isms", "c0_one_level"])
+@pytest.mark.parametrize("geom", [(mlgi.C1, 256, 4, 4, 4), (mlgi.C1, 256, 4, 3, 4), (mlgi.C0, 32, 8, 8, 1)],
+                         ids=["c1_keys_as_256px_isms", "c1_keys_as_3_rows_of_256px_isms", "c0_one_level"])
 def test_pullpush_per_level_form_bit_exact(ctx, geom):
-    """The four-launch (or, for one level, two-launch) pull-push that serves ISMs whose pyramid does
-    not fit one block's shared memory, against the level-by-level restatement: a splatted atlas read
-    as 4 x 4 ISMs of 256^2 texels with 4 levels, and C0's atlas with a single level."""
+    """The per-level pull-push (four launches, two for one level, over each half of the ISM rows
+    side by side) that serves ISMs whose pyramid does not fit one block's shared memory, against the
+    level-by-level restatement: a splatted atlas read as 4 x 4 ISMs of 256^2 texels with 4 levels,
+    its first 768 rows as 4 x 3 such ISMs (halves of one and two rows), and C0's atlas with a single
+    level."""
     import torch
 
     cfg, ism, gx, gy, levels = geom
@@ -247,14 +249,15 @@ def test_pullpush_per_level_form_bit_exact(ctx, geom):
     okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
                         cfg.grid_y, cfg.z_far)
     g = cfg.replace(ism_size=ism, grid_x=gx, grid_y=gy, levels=levels, name="per_level")
-    assert (g.atlas_w, g.atlas_h) == (cfg.atlas_w, cfg.atlas_h)
+    assert g.atlas_w == cfg.atlas_w and g.atlas_h <= cfg.atlas_h
+    okeys = np.ascontiguousarray(okeys[: g.atlas_h])
     assert mlgi.pullpush_launches(g) == (4 if levels >= 2 else 2) * 2  # two halves of the ISM rows
     ofin = O.pullpush(okeys, ism, levels, cfg.z_far)
     df = DeviceFrame(sc)
-    df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
+    df.keys[: okeys.size].copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
     ctx.pullpush(mlgi.Atlas(g.atlas_w, g.atlas_h, mlgi.ptr(df.keys), mlgi.ptr(df.atlas), mlgi.F32), mlgi.ism_params(g))
     torch.cuda.synchronize()
-    fin = df.atlas_np()
+    fin = df.atlas.float().cpu().numpy()[: okeys.size].reshape(g.atlas_h, g.atlas_w)
     mism = int((fin.view(np.uint32) != ofin.view(np.uint32)).sum())
     assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
 
