@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "batch_items.cuh"
 #include "checks.cuh"
@@ -811,11 +812,15 @@ __global__ void __launch_bounds__(128, 8) fg_class_kernel(FgArgs a, int tile_beg
 // Tile rows [tr0, tr1): tiles are numbered row by row, so a band of tile rows is a contiguous
 // range of tile indices starting at tile0.
 static int sm_count() {
-    static int n[64] = {};
+    static std::atomic<int> n[64];  // contexts on other threads may ask at the same time
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
-    if (!n[dev]) cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev);
-    return n[dev] > 0 ? n[dev] : 152;
+    int v = n[dev].load(std::memory_order_relaxed);
+    if (!v) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) cudaGetLastError();
+        n[dev].store(v, std::memory_order_relaxed);
+    }
+    return v > 0 ? v : 152;
 }
 
 static cudaError_t launch_fg_class(const FgArgs& a, cudaStream_t s, int tr0, int tr1) {

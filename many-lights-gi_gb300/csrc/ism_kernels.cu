@@ -11,6 +11,8 @@
 //                          for ISMs too large for that
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "batch_items.cuh"
 #include "checks.cuh"
 #include "gi_device.cuh"

@@ -80,9 +80,9 @@ struct PullPushArgs {
     float4* lv2;          // scratch: pyramid level 2, (atlas_w/4) x (atlas_h/4), when levels >= 2
     uint32_t m_c0, m_c1;  // ceil(2^32 / d) for d = ism_size / 2 and ism_size / 4 when d >= 2, else 0
     int row0, row1;       // the launch covers ISM rows [row0, row1) of the grid (0, grid_y: all)
-    int pyr_form;         // kPyrByCount or kPyrWhereFits (see pyramid_fused)
+    int pyr_form;         // kPyrByCount, kPyrWhereFits or kPyrPerLevel (see pyramid_launch_fused)
 };
-constexpr int kPyrByCount = 0, kPyrWhereFits = 1;
+constexpr int kPyrByCount = 0, kPyrWhereFits = 1, kPyrPerLevel = 2;
 
 struct FgArgs {
     int width, height;

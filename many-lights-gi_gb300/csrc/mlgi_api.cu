@@ -653,6 +653,7 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
         // on a half's border reads the other half's coarse texels only with weight 0.
         mlgi::PullPushArgs lo = a, hi = a;
         lo.row1 = hi.row0 = p->grid_y / 2;
+        lo.pyr_form = hi.pyr_form = mlgi::kPyrPerLevel;  // as the whole atlas, whose ISMs exceed a wave
         if (ctx->timing)  // no per-level times for the two halves: the pass's time lands in its last slot
             for (int k = 0; k < 3; ++k) MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp[k], s));
         MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp_fork, s));
@@ -879,9 +880,11 @@ mlgi_status mlgi_check_index_selftest(mlgi_ctx* ctx, int64_t index, int64_t exte
         cudaGetLastError();
         return fail(ctx, MLGI_ENOMEM, "self-test buffer");
     }
-    MLGI_CUDA(ctx, cudaMemsetAsync(buf, 0, (size_t)(extent + 1) * sizeof(float), s));
-    check_index_selftest_kernel<<<1, 1, 0, s>>>(buf, index, extent, buf + extent);
-    const cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaMemsetAsync(buf, 0, (size_t)(extent + 1) * sizeof(float), s);
+    if (e == cudaSuccess) {
+        check_index_selftest_kernel<<<1, 1, 0, s>>>(buf, index, extent, buf + extent);
+        e = cudaGetLastError();
+    }
     cudaFreeAsync(buf, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "check_index_selftest_kernel");
     return MLGI_OK;

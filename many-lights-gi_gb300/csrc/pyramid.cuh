@@ -59,17 +59,17 @@ bool pyramid_fits(int ism_size, int levels, float z_far) {
 // below), times the current device's SMs (152 when it cannot be asked).
 long long pyramid_wave(int ism_size) {
     constexpr int kMaxDevices = 64;
-    static int sms[kMaxDevices] = {};
+    static std::atomic<int> sms[kMaxDevices];  // contexts on other threads may ask at the same time
     int dev = 0, n = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
         n = 152;
-    } else if (!(n = sms[dev])) {
+    } else if (!(n = sms[dev].load(std::memory_order_relaxed))) {
         if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
             cudaGetLastError();
             n = 152;
         }
-        sms[dev] = n;
+        sms[dev].store(n, std::memory_order_relaxed);
     }
     return (long long)n * (ism_size > 64 ? 2 : 3);
 }
@@ -83,9 +83,10 @@ bool pyramid_fused(int ism_size, int levels, float z_far, long long n_isms) {
     return pyramid_fits(ism_size, levels, z_far) && n_isms <= pyramid_wave(ism_size);
 }
 
-// The form of a launch: one block per ISM when its arguments ask for it wherever it fits
-// (kPyrWhereFits), else by pyramid_fused.
+// The form of a launch: one block per ISM wherever it fits (kPyrWhereFits), never
+// (kPyrPerLevel), or by pyramid_fused for the launch's ISMs (kPyrByCount).
 bool pyramid_launch_fused(const PullPushArgs& a) {
+    if (a.pyr_form == kPyrPerLevel) return false;
     return a.pyr_form == kPyrWhereFits ? pyramid_fits(a.ism_size, a.levels, a.z_far)
                                        : pyramid_fused(a.ism_size, a.levels, a.z_far,
                                                        (long long)(a.row1 - a.row0) * a.grid_x);
