@@ -270,7 +270,11 @@ typedef struct {
 } mlgi_frame_desc;
 
 /* VPL processing -> ISM splat -> pull-push -> final gathering on device buffers; the VPL
- * buffers and the atlas are context-owned. */
+ * buffers and the atlas are context-owned. A call that repeats the previous call's frame
+ * description and output replays a CUDA graph of the frame, captured from the context's stream by
+ * the second such call and launched on `stream` (the buffers' contents are read when the frame
+ * runs, so new input data needs no new call form). Calls with per-pass timing, with new arguments,
+ * or after a context buffer was reallocated run directly. */
 mlgi_status mlgi_gi_frame(mlgi_ctx* ctx, const mlgi_frame_desc* frame, mlgi_radiance* out, mlgi_stream stream);
 
 /* ---- after the gathering: GI buffer format, bilateral blur, composite ------------------------ */

@@ -210,7 +210,11 @@ struct mlgi_ctx {
         int calls = 0;           // calls with this key that went through
         bool failed = false;     // the capture did not succeed: this key runs directly
         cudaGraphExec_t exec = nullptr;
-    } hgraph;
+        uint64_t gen = 0;        // buf_gen when it was captured
+    } hgraph, dgraph;  // host-buffer frames, device frames
+    // bumped whenever a context buffer is reallocated: a graph captured before holds old addresses
+    uint64_t buf_gen = 0;
+    bool capturing = false;  // a frame is being captured from the context's stream
     float last_ms[kNumTimings] = {};
 };
 
@@ -240,6 +244,7 @@ mlgi_status cuda_fail(mlgi_ctx* ctx, cudaError_t e, const char* what) {
 
 mlgi_status ensure(mlgi_ctx* ctx, DevBuf& b, size_t bytes) {
     if (b.bytes >= bytes) return MLGI_OK;
+    ++ctx->buf_gen;
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.bytes = 0;
@@ -307,6 +312,12 @@ mlgi_status check_atlas(mlgi_ctx* ctx, const mlgi_atlas* a, const mlgi_ism_param
 
 // Pull-push scratch of a context: the lv1/lv2 levels of the four-launch form, none for ISMs whose
 // pyramid runs in one block (a token allocation, so that the scratch pointer is never NULL).
+// The pull-push launches of `a`; inside a frame's capture without the shared-memory attribute
+// calls, which were made before it.
+cudaError_t pp_launch(mlgi_ctx* ctx, const mlgi::PullPushArgs& a, cudaStream_t s, cudaEvent_t* marks) {
+    return ctx->capturing ? mlgi::launch_pullpush_captured(a, s) : mlgi::launch_pullpush(a, s, marks);
+}
+
 // Whether mlgi_pullpush runs the per-level launches as two halves of the ISM rows side by side.
 bool pullpush_halves(const mlgi_ism_params* p) {
     return p->grid_y >= 2 &&
@@ -397,6 +408,7 @@ void mlgi_destroy(mlgi_ctx* ctx) {
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_side, ctx->ev_begin, ctx->ev_end, ctx->ev_pp_fork, ctx->ev_pp_join})
         if (e) cudaEventDestroy(e);
     if (ctx->hgraph.exec) cudaGraphExecDestroy(ctx->hgraph.exec);
+    if (ctx->dgraph.exec) cudaGraphExecDestroy(ctx->dgraph.exec);
     for (cudaStream_t cs : {ctx->copy, ctx->side})
         if (cs) {
             cudaStreamSynchronize(cs);
@@ -658,13 +670,13 @@ mlgi_status mlgi_pullpush(mlgi_ctx* ctx, mlgi_atlas* atlas, const mlgi_ism_param
             for (int k = 0; k < 3; ++k) MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp[k], s));
         MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp_fork, s));
         MLGI_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_pp_fork, 0));
-        MLGI_CUDA(ctx, mlgi::launch_pullpush(lo, s));
-        MLGI_CUDA(ctx, mlgi::launch_pullpush(hi, ctx->side));
+        MLGI_CUDA(ctx, pp_launch(ctx, lo, s, nullptr));
+        MLGI_CUDA(ctx, pp_launch(ctx, hi, ctx->side, nullptr));
         MLGI_CUDA(ctx, cudaEventRecord(ctx->ev_pp_join, ctx->side));
         MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_pp_join, 0));
         return MLGI_OK;
     }
-    MLGI_CUDA(ctx, mlgi::launch_pullpush(a, s, ctx->timing ? ctx->ev_pp : nullptr));
+    MLGI_CUDA(ctx, pp_launch(ctx, a, s, ctx->timing ? ctx->ev_pp : nullptr));
     return MLGI_OK;
 }
 
@@ -1027,12 +1039,68 @@ mlgi_status run_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, mlgi_radiance* ou
 
 }  // namespace
 
+// Captures a device frame from the context's stream into ctx->dgraph.exec; on any failure the
+// capture is ended and discarded and the call reports why.
+mlgi_status capture_device_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, mlgi_radiance* out) {
+    // the pull-push's shared-memory limits are raised outside the capture
+    MLGI_CUDA(ctx, mlgi::pullpush_prepare(mlgi::pullmid_smem_bytes(f->ism.ism_size, f->ism.levels)));
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "device frame capture");
+    ctx->capturing = true;
+    const mlgi_status st = run_frame(ctx, f, out, ctx->stream);
+    ctx->capturing = false;
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (st == MLGI_OK && e == cudaSuccess && graph) e = cudaGraphInstantiate(&ctx->dgraph.exec, graph, 0);
+    ctx->dgraph.gen = ctx->buf_gen;
+    if (graph) cudaGraphDestroy(graph);
+    if (st != MLGI_OK) return st;
+    if (e != cudaSuccess || !ctx->dgraph.exec) {
+        ctx->dgraph.exec = nullptr;
+        return cuda_fail(ctx, e != cudaSuccess ? e : cudaErrorUnknown, "device frame capture");
+    }
+    return MLGI_OK;
+}
+
 mlgi_status mlgi_gi_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, mlgi_radiance* out, mlgi_stream stream) {
     if (!ctx) return MLGI_EINVAL;
     if (!f || !out) return fail(ctx, MLGI_EINVAL, "NULL argument");
     cudaStream_t s = pick(ctx, stream);
-    mark(ctx, kVplp, s);
-    mlgi_status st = run_frame(ctx, f, out, s);
+    // A call that repeats the previous call's arguments replays a CUDA graph of the frame, captured
+    // from the context's stream by the second such call (the first went through directly and made
+    // every allocation the frame needs) and launched on the caller's stream: it spares the launch
+    // gaps between the frame's dozen kernels (C2 0.494 -> 0.484 ms, C1 0.094 -> 0.087, CREF 0.196
+    // -> 0.184). Calls with per-pass timing run directly.
+    auto& g = ctx->dgraph;
+    std::vector<unsigned char> key(sizeof(*f) + sizeof(*out));
+    std::memcpy(key.data(), f, sizeof(*f));
+    std::memcpy(key.data() + sizeof(*f), out, sizeof(*out));
+    if (ctx->timing || key != g.key || (g.exec && g.gen != ctx->buf_gen)) {  // new arguments or buffers
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.key = ctx->timing ? std::vector<unsigned char>() : key;
+        g.calls = 0;
+        g.failed = false;
+    }
+    mlgi_status st;
+    if (g.exec) {
+        const cudaError_t e = cudaGraphLaunch(g.exec, s);
+        st = e == cudaSuccess ? MLGI_OK : cuda_fail(ctx, e, "device frame graph launch");
+    } else if (!ctx->timing && g.calls > 0 && !g.failed) {
+        st = capture_device_frame(ctx, f, out);
+        if (st == MLGI_OK) {
+            const cudaError_t e = cudaGraphLaunch(g.exec, s);
+            st = e == cudaSuccess ? MLGI_OK : cuda_fail(ctx, e, "device frame graph launch");
+        } else {  // argument errors report as before; anything else runs this key directly
+            cudaGetLastError();
+            g.failed = true;
+            if (st == MLGI_ECUDA) st = run_frame(ctx, f, out, s);
+        }
+    } else {
+        mark(ctx, kVplp, s);
+        st = run_frame(ctx, f, out, s);
+    }
+    if (st == MLGI_OK) ++g.calls;
     ctx->timed_frame = st == MLGI_OK && ctx->timing;
     ctx->timed_host_frame = false;
     return st;
@@ -1291,6 +1359,7 @@ mlgi_status capture_host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     e = cudaStreamEndCapture(ctx->stream, &graph);
     if (st == MLGI_OK && e == cudaSuccess && graph)
         e = cudaGraphInstantiate(&ctx->hgraph.exec, graph, 0);
+    ctx->hgraph.gen = ctx->buf_gen;
     if (graph) cudaGraphDestroy(graph);
     if (st != MLGI_OK) return st;
     if (e != cudaSuccess || !ctx->hgraph.exec) {
@@ -1315,7 +1384,8 @@ mlgi_status mlgi_gi_frame_host(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* r
     for (int b = 0; f->points.counts && b < f->points.n_buckets && !overflow; ++b)
         overflow = (int64_t)f->points.counts[b] > f->points.bucket_stride;
     key.back() = overflow ? 1 : 0;
-    if (ctx->timing || key != g.key) {  // new arguments (or per-pass timing): run directly
+    // new arguments, reallocated context buffers or per-pass timing: run directly
+    if (ctx->timing || key != g.key || (g.exec && g.gen != ctx->buf_gen)) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
         g.key = ctx->timing ? std::vector<unsigned char>() : key;

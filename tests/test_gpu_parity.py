@@ -470,6 +470,42 @@ def test_frame_chain_and_host_frame_agree(ctx):
     assert rel_l2(dev, ref) < FG_REL_L2
 
 
+@pytest.mark.parametrize("cfg", [mlgi.C1, mlgi.C2, mlgi.C1.replace(cull=2, name="c1_clustered")], ids=lambda c: c.name)
+def test_repeated_device_frames_replay_the_same_frame(cfg):
+    """mlgi_gi_frame called again with the same arguments captures the frame into a CUDA graph (the
+    second call) and replays it (later calls): every such frame equals the first, issued call by
+    call, bit for bit; new arguments run directly again; so do frames with per-pass timing."""
+    import torch
+
+    ctx = mlgi.Context(0)
+    df = DeviceFrame(scene(cfg))
+    fd, out = df.frame_desc(), df.radiance()
+
+    def frame(f):
+        df.rgb.zero_()
+        torch.cuda.synchronize()
+        ctx.gi_frame(f, out)
+        torch.cuda.synchronize()
+        return df.rgb_np().copy()
+
+    first = frame(fd)
+    assert np.abs(first).max() > 0
+    for _ in range(3):
+        assert (frame(fd).view(np.uint32) == first.view(np.uint32)).all()
+    brighter = df.frame_desc()
+    brighter.vpl.light_intensity *= 2.0
+    other = frame(brighter)
+    assert not (other == first).all()
+    for _ in range(2):
+        assert (frame(brighter).view(np.uint32) == other.view(np.uint32)).all()
+    assert (frame(fd).view(np.uint32) == first.view(np.uint32)).all()
+    ctx.set_timing(True)
+    assert (frame(fd).view(np.uint32) == first.view(np.uint32)).all()
+    ctx.set_timing(False)
+    ctx.check_device_status()
+    ctx.close()
+
+
 @pytest.mark.parametrize("cfg", [mlgi.C0, mlgi.CREF, mlgi.C2, mlgi.C3B, mlgi.C1.replace(cull=2, name="c1_clustered")],
                          ids=lambda c: c.name)
 def test_host_frame_equals_device_frame(ctx, cfg):
