@@ -14,6 +14,7 @@ Prints one JSON line on rank 0. Multi-GPU (torchrun) runs independent replicas (
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import re
@@ -131,9 +132,11 @@ def ncu_traffic(kernel, key="traffic", workload="c2_1920x1080_n1024"):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks, throttle reasons and utilization sampled every 200 ms. mark(True) and
+    mark(False) bracket the timed region; stop() then summarises the samples taken inside it (all
+    samples when no sample fell inside, said in "window")."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
@@ -141,6 +144,7 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
@@ -151,6 +155,12 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+
+    def mark(self, begin):
+        if begin:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
 
     def stop(self):
         if not self.proc:
@@ -163,18 +173,33 @@ class ClockSampler:
         rows = []
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
+            if len(parts) >= 10:
+                try:
+                    parts[0] = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                except ValueError:
+                    parts[0] = None  # kept, but it cannot be placed in the timed region
                 rows.append(parts)
         os.unlink(self.path)
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        window = "timed region"
+        if self.t0 is not None:
+            end = self.t1 if self.t1 is not None else float("inf")
+            inside = [r for r in rows if r[0] is not None and self.t0 <= r[0] <= end]
+            if inside:
+                rows = inside
+            else:
+                window = "whole run (no sample inside the timed region)"
+        else:
+            window = "whole run"
+        num = lambda v: v.replace(".", "").isdigit()
+        sm = [float(r[2]) for r in rows if num(r[2])]
+        mx = [float(r[3]) for r in rows if num(r[3])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower().startswith("active")})
-        busy = [float(r[9]) for r in rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[6:10]) if v.lower().startswith("active")})
+        busy = [float(r[10]) for r in rows if len(r) > 10 and num(r[10])]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows),
+                "reasons": reasons, "samples": len(rows), "window": window,
                 "gpu_busy_pct": statistics.median(busy) if busy else None}
 
 
@@ -393,6 +418,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
         barrier()
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        sampler.mark(True)
         t0 = time.perf_counter()
         for i in range(args.steps):
             flush(i)
@@ -401,6 +427,7 @@ def run_gpu(args, cfg, rank, world, local_rank):
             ends[i].record(stream)
         barrier()
         wall = time.perf_counter() - t0
+        sampler.mark(False)
         clocks = sampler.stop()
         ctx.check_device_status()
         # per-pass device times: the same frames with the per-pass events of mlgi_set_timing
