@@ -108,6 +108,9 @@ struct SplatSmem {
     // per VPL, 16-byte rows: (position, ISM tile x), (normal, ISM tile y), (lookAtRH s, 0),
     // (lookAtRH u, 0); the tile offsets are float(x) and float(y) of ism_utils.glsl:35-37
     float4 pos[16], n[16], s[16], u[16];
+    // the cull's operands by VPL pairs (2j, 2j + 1), each value for both VPLs of the pair side by
+    // side for packed FP32x2 arithmetic: (-x, -y), (-z, normal x), (normal y, normal z)
+    float4 cull[8][3];
     // per warp: (point xyz, VPL slot << 8 | radius byte); up to 31 carried over from the previous
     // group of points plus 4 for each of 32 new points
     float4 tasks[kSplatThreads / 32][kSplatTaskCap];
@@ -153,6 +156,8 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
         const float ty = float(f2i(ismIndex / fgx));
         S.pos[threadIdx.x] = make_float4(pk.x, pk.y, pk.z, float(f2i(ismIndex - ty * fgx)));
         S.n[threadIdx.x] = make_float4(n.x, n.y, n.z, float(f2i(ty)));
+        float* c = reinterpret_cast<float*>(S.cull[threadIdx.x >> 1]) + (threadIdx.x & 1);
+        c[0] = -pk.x, c[2] = -pk.y, c[4] = -pk.z, c[6] = n.x, c[8] = n.y, c[10] = n.z;
     }
     for (int b = threadIdx.x; b < 256; b += kSplatThreads) {
         const float f = float(b) / 255.0f;
@@ -235,15 +240,32 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
             const v3 position = mk(pt.x, pt.y, pt.z);
             const uint32_t nr = __float_as_uint(pt.w);
             const v3 pn = mk(S.unorm[nr & 0xFFu], S.unorm[(nr >> 8) & 0xFFu], S.unorm[(nr >> 16) & 0xFFu]);
-            // gather up to 4 VPLs that pass the two-sided cull (ism.comp:93-107), as 4-bit indices
+            // gather up to 4 VPLs that pass the two-sided cull (ism.comp:93-107), as 4-bit indices.
+            // Two VPLs at a time on packed FP32x2 operations with explicit rounding, which are never
+            // contracted: per VPL, rel = position - vpl (added as position + (-vpl)), then
+            // dot(n_vpl, rel) < 0 and dot(pn, -rel) < 0, each dot (x*x + y*y) + z*z. The second is
+            // tested as dot(pn, rel) > 0: rounding to nearest is symmetric, so the two dots are
+            // negatives of each other up to the sign of a zero, which neither comparison sees.
+            const float2 p2x = make_float2(position.x, position.x), p2y = make_float2(position.y, position.y),
+                         p2z = make_float2(position.z, position.z);
+            const float2 n2x = make_float2(pn.x, pn.x), n2y = make_float2(pn.y, pn.y), n2z = make_float2(pn.z, pn.z);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
+            for (int j = 0; j < 8; ++j) {
                 if (found == 4) break;  // later VPLs are not used (ism.comp:103-106)
-                const float4 vp = S.pos[i], vn = S.n[i];
-                const v3 rel = position - mk(vp.x, vp.y, vp.z);
-                const bool cull = dot(mk(vn.x, vn.y, vn.z), rel) < 0.0f || dot(pn, -rel) < 0.0f;
-                if (!cull) {
-                    used |= (uint32_t)i << (4 * found);
+                const float4 c0 = S.cull[j][0], c1 = S.cull[j][1], c2 = S.cull[j][2];
+                const float2 rx = __fadd2_rn(p2x, make_float2(c0.x, c0.y));
+                const float2 ry = __fadd2_rn(p2y, make_float2(c0.z, c0.w));
+                const float2 rz = __fadd2_rn(p2z, make_float2(c1.x, c1.y));
+                const float2 dv = __fadd2_rn(__fadd2_rn(__fmul2_rn(make_float2(c1.z, c1.w), rx),
+                                                        __fmul2_rn(make_float2(c2.x, c2.y), ry)),
+                                             __fmul2_rn(make_float2(c2.z, c2.w), rz));
+                const float2 dp = __fadd2_rn(__fadd2_rn(__fmul2_rn(n2x, rx), __fmul2_rn(n2y, ry)), __fmul2_rn(n2z, rz));
+                if (!(dv.x < 0.0f || dp.x > 0.0f)) {
+                    used |= (uint32_t)(2 * j) << (4 * found);
+                    ++found;
+                }
+                if (!(dv.y < 0.0f || dp.y > 0.0f) && found < 4) {
+                    used |= (uint32_t)(2 * j + 1) << (4 * found);
                     ++found;
                 }
             }
@@ -284,7 +306,7 @@ __device__ __forceinline__ void splat_bucket(const SplatArgs& a, const int item,
     }
 }
 
-__global__ void __launch_bounds__(kSplatThreads) ism_splat_kernel(SplatArgs a) {
+__global__ void __launch_bounds__(kSplatThreads, 6) ism_splat_kernel(SplatArgs a) {
     __shared__ SplatSmem S;
     splat_bucket(a, blockIdx.x, S);
 }
