@@ -66,8 +66,11 @@ def test_vpl_process_bit_exact(ctx, cfg):
     assert (col.view(np.uint32) == ocol.view(np.uint32)).all()
 
 
-@pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2], ids=lambda c: c.name)
+@pytest.mark.parametrize("cfg", CFGS_SMALL + [mlgi.C2, mlgi.C3B.replace(reduced=False, name="c3b_fp32")],
+                         ids=lambda c: c.name)
 def test_ism_splat_bit_exact(ctx, cfg):
+    """The splat's key atlas against the oracle's, word for word (the cull runs on packed FP32x2,
+    the projections on scalar IEEE arithmetic)."""
     import torch
 
     sc = scene(cfg)
