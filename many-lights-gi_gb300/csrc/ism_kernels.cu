@@ -832,11 +832,22 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) pull1_kernel(PullPushArgs
 
 // NT threads per ISM: kPullMidThreads when the launch fills the GPU with ISM blocks, more when a
 // launch over a few ISM rows would leave most SMs idle (the pass is then bound by one block's time).
-template <int NT>
+__host__ __device__ __forceinline__ bool pyramid_lean_range(float z_far);
+__device__ __forceinline__ void pullmid_lean_ism(const PullPushArgs& a, int ism, unsigned char* smem);
+
+// kLean: the one-block pyramid's arithmetic (pullmid_lean_ism), for ISM edges of at least
+// kPullMidLeanEdge (fewer instructions at 84 registers a thread; C2 0.244 -> 0.236 ms a pass,
+// while 96^2 and 64^2 ISMs, whose pass is bound by latency and residency, took 0.259 -> 0.261 and
+// 0.075 -> 0.081 ms with it).
+template <int NT, bool kLean>
 __global__ void __launch_bounds__(NT) pullmid_kernel(PullPushArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    pullmid_ism(a, a.row0 * a.grid_x + blockIdx.x, smem);
+    if (kLean)
+        pullmid_lean_ism(a, a.row0 * a.grid_x + blockIdx.x, smem);
+    else
+        pullmid_ism(a, a.row0 * a.grid_x + blockIdx.x, smem);
 }
+constexpr int kPullMidLeanEdge = 128;
 constexpr int kPullMidWideThreads = 512;
 constexpr int kPullMidWideBelow = 2 * 152;  // ISMs per launch under which the wide form is used
 
@@ -848,13 +859,15 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH, 5) push0_kernel(PullPushA
     push0_quads(a, blockIdx.x, blockIdx.y);
 }
 
+#include "pyramid.cuh"
+
+// The tables of either middle pass (pullmid_ism's key tables, the lean pass's PyramidTables), then
+// levels 2..L.
 size_t pullmid_smem_bytes(int ism_size, int levels) {
-    size_t b = kPullPushTableBytes;
+    size_t b = std::max(kPullPushTableBytes, kPyramidTableBytes);
     for (int l = 2; l <= levels; ++l) b += (size_t)(ism_size >> l) * (ism_size >> l) * 16;
     return b;
 }
-
-#include "pyramid.cuh"
 
 size_t pullpush_scratch_bytes(int atlas_w, int atlas_h, int levels, size_t* lv2_offset) {
     const size_t lv1 = (size_t)(atlas_w >> 1) * (atlas_h >> 1) * 16;
@@ -869,18 +882,25 @@ __host__ __device__ __forceinline__ int tiles_y(int h) { return (h + kPpTileH - 
 __host__ __device__ __forceinline__ int row_items(int w) { return (tiles_x(w) + kPpBatchTiles - 1) / kPpBatchTiles; }
 
 cudaError_t pullpush_prepare(size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(pullmid_kernel<kPullMidThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(pullmid_kernel<kPullMidThreads, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(pullmid_kernel<kPullMidWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(pullmid_kernel<kPullMidThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(pullmid_kernel<kPullMidWideThreads, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = pyramid_prepare();
     return e;
 }
 
 static void launch_pullmid(const PullPushArgs& a, int isms, size_t smem, cudaStream_t s) {
     if (isms < kPullMidWideBelow)
-        pullmid_kernel<kPullMidWideThreads><<<isms, kPullMidWideThreads, smem, s>>>(a);
+        pullmid_kernel<kPullMidWideThreads, false><<<isms, kPullMidWideThreads, smem, s>>>(a);
+    else if (a.ism_size >= kPullMidLeanEdge && pyramid_lean_range(a.z_far))
+        pullmid_kernel<kPullMidThreads, true><<<isms, kPullMidThreads, smem, s>>>(a);
     else
-        pullmid_kernel<kPullMidThreads><<<isms, kPullMidThreads, smem, s>>>(a);
+        pullmid_kernel<kPullMidThreads, false><<<isms, kPullMidThreads, smem, s>>>(a);
 }
 
 // Grids of the four launches over ISM rows [a.row0, a.row1).

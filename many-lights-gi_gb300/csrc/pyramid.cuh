@@ -479,6 +479,86 @@ __device__ __forceinline__ void pyramid_ism(const PullPushArgs& a, const int ism
     }
 }
 
+// Bounds-checked build: the lean middle pass's last level texel (float4 index `last` after the
+// tables) lies inside the block's dynamic shared memory.
+__device__ __forceinline__ void check_lean_smem(const int last) {
+#ifdef MLGI_CHECKS
+    uint32_t dyn;
+    asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    (void)MLGI_IX(last, dyn > kPyramidTableBytes ? (dyn - kPyramidTableBytes) / 16 : 0);
+#else
+    (void)last;
+#endif
+}
+
+// Far planes for which the lean arithmetic above is exact (its range argument, in the header).
+__host__ __device__ __forceinline__ bool pyramid_lean_range(const float z_far) {
+    return z_far >= 0x1p-20f && z_far <= 0x1p+20f;
+}
+
+// The per-level form's middle pass (pullmid_kernel) with the lean arithmetic: ISM `ism`'s levels
+// 2..L in shared memory after the tables; level 2 pulled from the lv1 scratch, levels 3..L pulled,
+// L-1..2 pushed back by 2x2 quads, and the pushed level 2 written to the lv2 scratch. Bit-identical
+// to pullmid_ism's per-texel forms (the same operations in the same order, see the header), in
+// fewer instructions: the quad's four coarse texels and their terms serve its four outputs. Far
+// planes in pyramid_lean_range only.
+__device__ __forceinline__ void pullmid_lean_ism(const PullPushArgs& a, const int ism, unsigned char* smem) {
+    PyramidTables& T = *reinterpret_cast<PyramidTables*>(smem);
+    float4* const base = reinterpret_cast<float4*>(smem + kPyramidTableBytes);
+    __syncthreads();  // the previous ISM's use of smem is over
+    // levels >= 2 read only the reciprocal table (the key and displacement tables serve level 1)
+    if (threadIdx.x < 20) T.rcp[threadIdx.x] = threadIdx.x == 0 || threadIdx.x > 16 ? 0.f : 1.0f / float(threadIdx.x);
+    __syncthreads();
+    const int s = a.ism_size, L = a.levels, nt = blockDim.x, tid = threadIdx.x;
+    const int im = MLGI_IX(ism, a.grid_x * a.grid_y), ix = im % a.grid_x, iy = im / a.grid_x;
+    auto lvl = [&](const int l) { return base + (pyramid_offset(s, l) - pyramid_offset(s, 2)); };  // l >= 2
+    check_lean_smem(pyramid_offset(s, L + 1) - pyramid_offset(s, 2) - 1);
+    {  // level 2 from lv1
+        const int e2 = s >> 2, w1 = a.atlas_w >> 1;
+        const size_t n1 = (size_t)w1 * (a.atlas_h >> 1);
+        float4* const out = lvl(2);
+        for (int i = tid; i < e2 * e2; i += nt) {
+            const int ly = i / e2, lx = i - ly * e2, gox = ix * e2 + lx, goy = iy * e2 + ly;
+            float4 t4[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                t4[k] = a.lv1[MLGI_IX((size_t)(2 * goy + kPullOff[k][1]) * w1 + 2 * gox + kPullOff[k][0], n1)];
+            out[i] = pull_lean(t4, gox, goy, 0.25f, T);
+        }
+        __syncthreads();
+    }
+    for (int l = 3; l <= L; ++l) {
+        const int el = s >> l;
+        const float4* in = lvl(l - 1);
+        float4* out = lvl(l);
+        const float scale = pow2neg(l);
+        for (int i = tid; i < el * el; i += nt) {
+            const int ly = i / el, lx = i - ly * el;
+            float4 t4[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                t4[k] = in[MLGI_IX((2 * ly + kPullOff[k][1]) * 2 * el + 2 * lx + kPullOff[k][0], 4 * el * el)];
+            out[i] = pull_lean(t4, el * ix + lx, el * iy + ly, scale, T);
+        }
+        __syncthreads();
+    }
+    for (int l = L - 1; l >= 2; --l) {
+        const int el = s >> l, nq = (el >> 1) + 1;
+        const float4* coarse_lvl = lvl(l + 1);
+        float4* same = lvl(l);
+        const float scale = pow2neg(l);
+        for (int i = tid; i < nq * nq; i += nt) {
+            const int gy = i / nq, gx = i - gy * nq;
+            push_quad_smem(same, coarse_lvl, el, gx, gy, scale, T);
+        }
+        __syncthreads();
+    }
+    const int e2 = s >> 2, w2 = a.atlas_w >> 2;
+    const float4* l2 = lvl(2);
+    for (int i = tid; i < e2 * e2; i += nt)
+        a.lv2[MLGI_IX((size_t)(iy * e2 + i / e2) * w2 + ix * e2 + i % e2, (size_t)w2 * (a.atlas_h >> 2))] = l2[i];
+}
+
 // Threads per block: kPyrBigThreads for ISM edges above 64 (two blocks per SM, as their shared
 // memory allows; 384 threads leave 80 registers a thread, measured at C2: 0.256 ms against 0.274 ms
 // with 512 threads at 64 registers and 0.276 ms with 256), kPyrSmallThreads for smaller ones with
