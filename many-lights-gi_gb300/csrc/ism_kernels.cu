@@ -861,6 +861,34 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH, 5) push0_kernel(PullPushA
 
 #include "pyramid.cuh"
 
+// pull1_kernel on the one-block pyramid's arithmetic (pull1_lean: selects instead of branches, the
+// displacement mean from a table), for far planes in pyramid_lean_range; bit-identical.
+__global__ void __launch_bounds__(kPpTileW * kPpTileH) pull1_lean_kernel(PullPushArgs a) {
+    __shared__ PyramidTables T;
+    fill_pyramid_tables(T, a.z_far);
+    __syncthreads();
+    const int s1 = a.ism_size >> 1, w1 = a.atlas_w >> 1;
+    const float fs = float(a.ism_size);
+    const size_t nk = (size_t)a.atlas_w * a.atlas_h - 1;  // a pair's first key
+#pragma unroll 1
+    for (int j = 0; j < kPull1Rows; ++j) {
+        const int x = blockIdx.x * kPpTileW + (threadIdx.x % kPpTileW);
+        const int y = a.row0 * s1 + (blockIdx.y * kPull1Rows + j) * kPpTileH + (threadIdx.x / kPpTileW);
+        if (x >= w1 || y >= a.row1 * s1) continue;
+        const uint2 r0 = __ldg(reinterpret_cast<const uint2*>(a.keys + MLGI_IX((size_t)(2 * y) * a.atlas_w + 2 * x, nk)));
+        const uint2 r1 = __ldg(reinterpret_cast<const uint2*>(a.keys + MLGI_IX((size_t)(2 * y + 1) * a.atlas_w + 2 * x, nk)));
+        const uint32_t key[4] = {r0.x, r1.x, r0.y, r1.y};  // kPullOff order
+        a.lv1[MLGI_IX((uint32_t)y * w1 + x, (uint32_t)w1 * (a.atlas_h >> 1))] = pull1_lean(key, T, a.z_far, fs);
+    }
+}
+
+static void launch_pull1(const PullPushArgs& a, const dim3 grid, cudaStream_t s) {
+    if (pyramid_lean_range(a.z_far))
+        pull1_lean_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(a);
+    else
+        pull1_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(a);
+}
+
 // The tables of either middle pass (pullmid_ism's key tables, the lean pass's PyramidTables), then
 // levels 2..L.
 size_t pullmid_smem_bytes(int ism_size, int levels) {
@@ -927,7 +955,7 @@ cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
         return cudaGetLastError();
     }
     const PullPushGrids g = pullpush_grids(a);
-    pull1_kernel<<<g.g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    launch_pull1(a, g.g1, s);
     if (a.levels >= 2) {
         launch_pullmid(a, g.isms, pullmid_smem_bytes(a.ism_size, a.levels), s);
         push1_kernel<<<g.q1, kPpTileW * kPpTileH, 0, s>>>(a);
@@ -947,7 +975,7 @@ cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* 
         return cudaGetLastError();
     }
     const PullPushGrids g = pullpush_grids(a);
-    pull1_kernel<<<g.g1, kPpTileW * kPpTileH, 0, s>>>(a);
+    launch_pull1(a, g.g1, s);
     if (marks) cudaEventRecord(marks[0], s);
     if (a.levels >= 2) {
         const size_t smem = pullmid_smem_bytes(a.ism_size, a.levels);
