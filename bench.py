@@ -72,11 +72,12 @@ def parse():
 
 
 def launches_per_frame(cfg):
-    """Kernels of one mlgi_gi_frame: VPL processing, atlas clear, splat, the pull-push pass's launches
-    and final gathering."""
+    """Kernels of one timed mlgi_gi_frame: VPL processing and the atlas clear (one launch), splat,
+    the pull-push pass's launches and final gathering. (Frames with per-pass timing launch the VPL
+    pass and the clear separately.)"""
     import mlgi
 
-    return 3 + mlgi.pullpush_launches(cfg) + 1
+    return 2 + mlgi.pullpush_launches(cfg) + 1
 
 
 # ---- algorithmic bytes per pass and per kernel (one launch each per frame) ----------------------

@@ -86,6 +86,31 @@ __global__ void ism_clear_kernel(uint4* p, size_t n4) {
     for (; i < n4; i += stride) p[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
 }
 
+// The VPL pass and the atlas clear in one launch, for the frames: blocks [0, vpl_blocks) run the
+// VPLs (256 a block), the rest clear the key atlas. The two write disjoint buffers, and the VPL
+// pass's few blocks run beside the clear's instead of before them.
+__global__ void __launch_bounds__(256) vpl_clear_kernel(VplArgs va, uint4* p, size_t n4, int vpl_blocks) {
+    if ((int)blockIdx.x < vpl_blocks) {
+        vpl_one(va, blockIdx.x * 256u + threadIdx.x);
+        return;
+    }
+    size_t i = (blockIdx.x - (unsigned)vpl_blocks) * (size_t)blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)(gridDim.x - (unsigned)vpl_blocks) * blockDim.x;
+    for (; i < n4; i += stride) p[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+}
+
+cudaError_t launch_vpl_clear(const VplArgs& va, uint32_t* keys, size_t n, cudaStream_t s) {
+    if (va.n <= 0 || n == 0 || (n & 3) || (reinterpret_cast<uintptr_t>(keys) & 15)) {
+        cudaError_t e = launch_vpl_process(va, s);
+        return e == cudaSuccess ? launch_ism_clear(keys, n, s) : e;
+    }
+    const size_t n4 = n / 4;
+    const int vpl_blocks = (va.n + 255) / 256;
+    const int clear_blocks = (int)std::min<size_t>((n4 + 255) / 256, 152 * 16);
+    vpl_clear_kernel<<<vpl_blocks + clear_blocks, 256, 0, s>>>(va, reinterpret_cast<uint4*>(keys), n4, vpl_blocks);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     if ((n & 3) || (reinterpret_cast<uintptr_t>(keys) & 15)) return cudaMemsetAsync(keys, 0xFF, n * 4, s);

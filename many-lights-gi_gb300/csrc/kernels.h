@@ -204,6 +204,9 @@ constexpr uint32_t kStatusTmaTimeout = 1u;
 
 cudaError_t launch_vpl_process(const VplArgs& a, cudaStream_t s);
 cudaError_t launch_ism_clear(uint32_t* keys, size_t n, cudaStream_t s);
+// launch_vpl_process and launch_ism_clear in one launch (separate launches when the atlas is not
+// a whole number of aligned 16-byte rows).
+cudaError_t launch_vpl_clear(const VplArgs& va, uint32_t* keys, size_t n, cudaStream_t s);
 cudaError_t launch_ism_splat(const SplatArgs& a, cudaStream_t s);
 // The atomics launch_ism_splat would issue (projections that land inside the atlas), added to *count.
 cudaError_t launch_ism_splat_count(const SplatArgs& a, unsigned long long* count, cudaStream_t s);

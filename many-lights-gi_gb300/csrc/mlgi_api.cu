@@ -1026,9 +1026,18 @@ mlgi_status run_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, mlgi_radiance* ou
     mlgi_vpl_buf vb{n, static_cast<float*>(ctx->vpl.p), static_cast<float*>(ctx->packed.p),
                     reduced ? ctx->reduced.p : nullptr};
     mlgi_atlas atlas{aw, ah, static_cast<uint32_t*>(ctx->keys.p), ctx->depth.p, f->atlas_format};
-    if ((st = mlgi_vpl_process(ctx, &f->rsm, &f->vpl, &vb, s)) != MLGI_OK) return st;
-    mark(ctx, kVplp + 1, s);
-    if ((st = mlgi_ism_splat(ctx, &f->points, &vb, n, &f->ism, &atlas, s)) != MLGI_OK) return st;
+    if (ctx->timing) {  // the passes one launch each, so that each has its own time
+        if ((st = mlgi_vpl_process(ctx, &f->rsm, &f->vpl, &vb, s)) != MLGI_OK) return st;
+        mark(ctx, kVplp + 1, s);
+        if ((st = mlgi_ism_splat(ctx, &f->points, &vb, n, &f->ism, &atlas, s)) != MLGI_OK) return st;
+    } else {  // the VPL pass and the atlas clear in one launch, then the splat
+        mlgi::VplArgs va;
+        mlgi::SplatArgs sa;
+        if ((st = build_vpl_args(ctx, &f->rsm, &f->vpl, &vb, va)) != MLGI_OK) return st;
+        if ((st = build_splat_args(ctx, &f->points, &vb, n, &f->ism, &atlas, sa)) != MLGI_OK) return st;
+        MLGI_CUDA(ctx, mlgi::launch_vpl_clear(va, atlas.keys, (size_t)aw * ah, s));
+        MLGI_CUDA(ctx, mlgi::launch_ism_splat(sa, s));
+    }
     mark(ctx, kIsmCs + 1, s);
     if ((st = mlgi_pullpush(ctx, &atlas, &f->ism, s)) != MLGI_OK) return st;
     mark(ctx, kPullPush + 1, s);
@@ -1232,9 +1241,13 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
 
     MLGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_rsm, 0));
     mark(ctx, kVplp, s);
-    MLGI_CUDA(ctx, mlgi::launch_vpl_process(va, s));
-    mark(ctx, kIsmClear, s);
-    MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas.keys, (size_t)aw * ah, s));
+    if (ctx->timing) {  // one launch each, so that each pass has its own time
+        MLGI_CUDA(ctx, mlgi::launch_vpl_process(va, s));
+        mark(ctx, kIsmClear, s);
+        MLGI_CUDA(ctx, mlgi::launch_ism_clear(atlas.keys, (size_t)aw * ah, s));
+    } else {
+        MLGI_CUDA(ctx, mlgi::launch_vpl_clear(va, atlas.keys, (size_t)aw * ah, s));
+    }
     mark(ctx, kIsmCs, s);
     // Rows are pulled and pushed in runs: rows completed by the chunks so far go to the side
     // stream, concurrent with the next chunks' splats, once they make up a quarter of the grid
