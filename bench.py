@@ -199,9 +199,13 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({n for r in rows for n, v in zip(names, r[6:10]) if v.lower().startswith("active")})
         busy = [float(r[10]) for r in rows if len(r) > 10 and num(r[10])]
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows), "window": window,
-                "gpu_busy_pct": statistics.median(busy) if busy else None}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+               "reasons": reasons, "samples": len(rows), "window": window}
+        # utilization.gpu averages over nvidia-smi's own period, which a timed region of a second or
+        # two does not fill: it is reported for the long streams only
+        if window != "timed region":
+            out["gpu_busy_pct"] = statistics.median(busy) if busy else None
+        return out
 
 
 # ---- CPU implementation of the path (the oracle's FP32 restatement, all host threads) -----------

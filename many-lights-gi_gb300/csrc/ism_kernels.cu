@@ -907,6 +907,59 @@ __global__ void __launch_bounds__(kPpTileW * kPpTileH) pull1_lean_kernel(PullPus
     }
 }
 
+// push1_kernel on the one-block pyramid's arithmetic (push_term, push_out_lean) for far planes in
+// pyramid_lean_range and ISM edges above 64: a quad's four coarse level-2 texels and their terms
+// serve its four outputs; a quad whose radius test meets the band is redone with push1_quads'
+// exact per-output code. Three blocks a SM (80 registers): C2's pass 0.2315 -> 0.2264 ms, C3-B's
+// 0.2536 -> 0.2483; 64^2 ISMs (CREF) took 0.0743 -> 0.0754, so they keep push1_kernel. As
+// compiled (105 registers, two blocks) it was slower everywhere.
+__global__ void __launch_bounds__(kPpTileW * kPpTileH, 3) push1_lean_kernel(PullPushArgs a) {
+    __shared__ PyramidTables T;  // levels >= 1 read only the reciprocal table
+    if (threadIdx.x < 20) T.rcp[threadIdx.x] = threadIdx.x == 0 || threadIdx.x > 16 ? 0.f : 1.0f / float(threadIdx.x);
+    __syncthreads();
+    const int w1 = a.atlas_w >> 1, h1 = a.atlas_h >> 1, w2 = a.atlas_w >> 2, h2 = a.atlas_h >> 2;
+    const int s1 = a.ism_size >> 1, Y0 = a.row0 * s1, Y1 = a.row1 * s1;
+    const int gx = blockIdx.x * kPpTileW + (threadIdx.x % kPpTileW);
+    const int gy = (Y0 >> 1) + blockIdx.y * kPpTileH + (threadIdx.x / kPpTileW);
+    if (gx > w2 || gy > (Y1 >> 1)) return;
+    const int sc = a.ism_size >> 2;  // ISM edge at level 2
+    PushTerm c[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {  // coordinates off the level are clamped, as push_coarse does
+        const int cx = min(max(gx - 1 + kPushOff[k][0], 0), w2 - 1), cy = min(max(gy - 1 + kPushOff[k][1], 0), h2 - 1);
+        c[k] = push_term(a.lv2[MLGI_IX((uint32_t)cy * (uint32_t)w2 + (uint32_t)cx, (uint32_t)w2 * (uint32_t)h2)], 0.5f);
+    }
+    const bool bx = multiple_of(gx, sc, a.m_c1), by = multiple_of(gy, sc, a.m_c1);
+    const int x0 = 2 * gx - 1, y0 = 2 * gy - 1;
+    const bool okx0 = x0 >= 0, okx1 = x0 + 1 < w1, oky0 = y0 >= Y0, oky1 = y0 + 1 < Y1;
+    const uint32_t n1 = (uint32_t)w1 * h1;
+    const uint32_t o0 = (uint32_t)max(y0, 0) * w1 + x0, o1 = (uint32_t)min(y0 + 1, h1 - 1) * w1 + x0;  // x0 < 0: unused
+    float4* lv1 = a.lv1;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 p00 = oky0 && okx0 ? lv1[MLGI_IX(o0, n1)] : z, p10 = oky0 && okx1 ? lv1[MLGI_IX(o0 + 1, n1)] : z;
+    const float4 p01 = oky1 && okx0 ? lv1[MLGI_IX(o1, n1)] : z, p11 = oky1 && okx1 ? lv1[MLGI_IX(o1 + 1, n1)] : z;
+    bool band = false;
+    const float4 r00 = push_out_lean<true, 0, 0>(c, bx, by, p00, band, T);
+    const float4 r10 = push_out_lean<true, 1, 0>(c, bx, by, p10, band, T);
+    const float4 r01 = push_out_lean<true, 0, 1>(c, bx, by, p01, band, T);
+    const float4 r11 = push_out_lean<true, 1, 1>(c, bx, by, p11, band, T);
+    if (band) {  // a radius test within 2^-20 of the radius: the exact per-output form
+        push1_quads(a, blockIdx.x, blockIdx.y);
+        return;
+    }
+    if (oky0 && okx0) lv1[MLGI_IX(o0, n1)] = r00;
+    if (oky0 && okx1) lv1[MLGI_IX(o0 + 1, n1)] = r10;
+    if (oky1 && okx0) lv1[MLGI_IX(o1, n1)] = r01;
+    if (oky1 && okx1) lv1[MLGI_IX(o1 + 1, n1)] = r11;
+}
+
+static void launch_push1(const PullPushArgs& a, const dim3 grid, cudaStream_t s) {
+    if (a.ism_size > 64 && pyramid_lean_range(a.z_far))
+        push1_lean_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(a);
+    else
+        push1_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(a);
+}
+
 static void launch_pull1(const PullPushArgs& a, const dim3 grid, cudaStream_t s) {
     if (pyramid_lean_range(a.z_far))
         pull1_lean_kernel<<<grid, kPpTileW * kPpTileH, 0, s>>>(a);
@@ -983,7 +1036,7 @@ cudaError_t launch_pullpush_captured(const PullPushArgs& a, cudaStream_t s) {
     launch_pull1(a, g.g1, s);
     if (a.levels >= 2) {
         launch_pullmid(a, g.isms, pullmid_smem_bytes(a.ism_size, a.levels), s);
-        push1_kernel<<<g.q1, kPpTileW * kPpTileH, 0, s>>>(a);
+        launch_push1(a, g.q1, s);
     }
     push0_kernel<<<g.q0, kPpTileW * kPpTileH, 0, s>>>(a);
     return cudaGetLastError();
@@ -1008,7 +1061,7 @@ cudaError_t launch_pullpush(const PullPushArgs& a, cudaStream_t s, cudaEvent_t* 
         if (e != cudaSuccess) return e;
         launch_pullmid(a, g.isms, smem, s);
         if (marks) cudaEventRecord(marks[1], s);
-        push1_kernel<<<g.q1, kPpTileW * kPpTileH, 0, s>>>(a);
+        launch_push1(a, g.q1, s);
     } else if (marks) {
         cudaEventRecord(marks[1], s);
     }
