@@ -1254,10 +1254,15 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     // (a run costs about four rows' time whatever its size); the rest after the last chunk. With
     // the one-block pyramid those rest in one run (one wave of ISM blocks: C2 end to end 0.793 ms,
     // against 0.811 ms in runs of 3/16 of the grid and 0.896 ms in runs of 1/16); the per-level
-    // form keeps runs of at most 3/16 of the grid alternating between the two streams. Runs write
-    // disjoint rows.
+    // form keeps runs of at most 3/16 of the grid alternating between the two streams. The early
+    // runs take the one-block pyramid, whose small DRAM traffic suits them beside the splats; the
+    // last runs, which nothing overlaps, run level by level where the whole atlas would (more than
+    // a wave of ISM blocks; only then does the context hold the level-1 and level-2 scratch): C2
+    // end to end 0.760 -> 0.743 ms, by ISM count 0.752. Runs write disjoint rows.
     const int gy = d.ism.grid_y;
     const bool one_block = mlgi::pyramid_fits(d.ism.ism_size, d.ism.levels, d.ism.z_far);
+    const bool last_per_level =
+        !mlgi::pyramid_fused(d.ism.ism_size, d.ism.levels, d.ism.z_far, (long long)d.ism.grid_x * d.ism.grid_y);
     const int final_rows = h.chunks > 1 && !one_block ? std::max(2, 3 * gy / 16) : gy;
     std::vector<char> done(gy, 0);
     MLGI_CUDA(ctx, mlgi::pullpush_prepare(mlgi::pullmid_smem_bytes(d.ism.ism_size, d.ism.levels)));
@@ -1272,7 +1277,7 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
             mlgi::PullPushArgs part = pa;
             part.row0 = r;
             part.row1 = r1;
-            part.pyr_form = mlgi::kPyrWhereFits;
+            part.pyr_form = last && last_per_level ? mlgi::kPyrPerLevel : mlgi::kPyrWhereFits;
             const cudaError_t e = mlgi::launch_pullpush_captured(part, last && (run & 1) == 0 ? s : s2);
             if (e != cudaSuccess) return e;
             ++run;
