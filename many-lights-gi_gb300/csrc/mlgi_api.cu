@@ -1598,12 +1598,13 @@ mlgi_status capture_batch(mlgi_batch* b) {
             for (int i : lane[j]) {
                 const mlgi::BatchView& v = b->h_views[b->slot[i]];
                 cudaStream_t s = b->side[j];
-                if (e == cudaSuccess) e = mlgi::launch_vpl_process(v.vpl, s);
-                if (e == cudaSuccess) e = mlgi::launch_ism_clear(v.keys, v.atlas_texels, s);
+                if (e == cudaSuccess) e = mlgi::launch_vpl_clear(v.vpl, v.keys, v.atlas_texels, s);
                 if (e == cudaSuccess) e = mlgi::launch_ism_splat(v.splat, s);
                 if (e == cudaSuccess) e = mlgi::launch_pullpush_captured(v.pp, s);
                 if (e == cudaSuccess) e = mlgi::launch_final_gather(v.fg, s);
-                b->launches += 3 + (mlgi::pyramid_launch_fused(v.pp) ? 1 : v.pp.levels >= 2 ? 4 : 2) + 1;
+                // the VPL pass and the clear are one launch unless the atlas is not whole 16-byte rows
+                const bool one = v.atlas_texels % 4 == 0 && (reinterpret_cast<uintptr_t>(v.keys) & 15) == 0;
+                b->launches += (one ? 2 : 3) + (mlgi::pyramid_launch_fused(v.pp) ? 1 : v.pp.levels >= 2 ? 4 : 2) + 1;
             }
             if (e == cudaSuccess) e = cudaEventRecord(b->events[j], b->side[j]);  // join
             if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->events[j], 0);
