@@ -1263,6 +1263,9 @@ mlgi_status host_frame(mlgi_ctx* ctx, const mlgi_frame_desc* f, float* rgb_host)
     const bool one_block = mlgi::pyramid_fits(d.ism.ism_size, d.ism.levels, d.ism.z_far);
     const bool last_per_level =
         !mlgi::pyramid_fused(d.ism.ism_size, d.ism.levels, d.ism.z_far, (long long)d.ism.grid_x * d.ism.grid_y);
+    // per-level runs write the level-1 and level-2 scratch, which pullpush_scratch_need sized above
+    if ((last_per_level || !one_block) && ctx->pp.bytes < mlgi::pullpush_scratch_bytes(aw, ah, d.ism.levels, nullptr))
+        return fail(ctx, MLGI_ECUDA, "pull-push scratch of %zu bytes is too small", ctx->pp.bytes);
     const int final_rows = h.chunks > 1 && !one_block ? std::max(2, 3 * gy / 16) : gy;
     std::vector<char> done(gy, 0);
     MLGI_CUDA(ctx, mlgi::pullpush_prepare(mlgi::pullmid_smem_bytes(d.ism.ism_size, d.ism.levels)));
