@@ -8,7 +8,9 @@
 //                          ImperfectShadowmap::pullpush (ImperfectShadowmap.cpp:121-182): an
 //                          ISM's whole pyramid in one block (pyramid.cuh); pull1_kernel,
 //                          pullmid_kernel, push1_kernel and push0_kernel run it level by level
-//                          for ISMs too large for that
+//                          for launches of more than a wave of ISMs (pull1_lean_kernel,
+//                          pullmid_kernel<., true> and push1_lean_kernel: the same results on
+//                          the one-block pyramid's leaner arithmetic, where it is faster)
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -362,8 +364,8 @@ cudaError_t launch_ism_splat_count(const SplatArgs& a, unsigned long long* count
 // next finer (pull) or next coarser (push) level of its own ISM:
 //   pull1_kernel    level 1 from the keys, one thread per level-1 texel            -> lv1
 //   pullmid_kernel  one block per ISM: pull 2..L, push L-1..2 in shared memory     -> lv2
-//   push1_kernel    push level 1 from lv2 onto lv1 in place, one thread per texel
-//   push0_kernel    push level 0 (depth only) from lv1 and the keys, one thread per texel -> out
+//   push1_kernel    push level 1 from lv2 onto lv1 in place, one thread per 2x2 quad
+//   push0_kernel    push level 0 (depth only) from lv1 and the keys, one thread per 2x2 quad -> out
 // Texels of levels >= 1 are (depth, maxDepth, radius, packHalf2x16(dx, dy)), the reference's
 // RGBA32F pyramid. Coordinates entering the displacement arithmetic are global coordinates of the
 // level, as in the level-by-level shaders.
