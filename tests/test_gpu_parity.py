@@ -265,6 +265,30 @@ def test_pullpush_per_level_form_bit_exact(ctx, geom):
     assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
 
 
+@pytest.mark.parametrize("cfg,z_far", [(mlgi.C1, 3.0e6), (mlgi.C1, 1.0e-7), (mlgi.C2, 3.0e6)],
+                         ids=["c1_far_3e6", "c1_far_1e-7", "c2_far_3e6"])
+def test_pullpush_far_planes_outside_the_lean_range(ctx, cfg, z_far):
+    """A far plane outside [2^-20, 2^20] takes the per-level kernels' general arithmetic (pull1_kernel,
+    pullmid_kernel's per-texel forms, push1_kernel) instead of the one-block pyramid's lean forms,
+    in two halves of the ISM rows: bit for bit the level-by-level restatement with that far plane."""
+    import torch
+
+    sc = scene(cfg)
+    opos, _, _, opn = oracle_vpls(cfg, sc)
+    okeys = O.ism_splat(sc.points, sc.counts, sc.bucket_stride, opos, opn, cfg.n_vpl, cfg.ism_size, cfg.grid_x,
+                        cfg.grid_y, cfg.z_far)
+    g = cfg.replace(z_far=z_far, name=cfg.name + "_far")
+    assert mlgi.pullpush_launches(g) == (4 if cfg.levels >= 2 else 2) * 2
+    ofin = O.pullpush(okeys, cfg.ism_size, cfg.levels, z_far)
+    df = DeviceFrame(sc)
+    df.keys.copy_(torch.from_numpy(okeys.view(np.int32).ravel()))
+    ctx.pullpush(df.atlas_view(), mlgi.ism_params(g))
+    torch.cuda.synchronize()
+    fin = df.atlas_np()
+    mism = int((fin.view(np.uint32) != ofin.view(np.uint32)).sum())
+    assert mism == 0, f"{mism} of {fin.size} atlas texels differ"
+
+
 @pytest.mark.parametrize("cfg", [mlgi.C0, mlgi.C2, mlgi.C3B.replace(reduced=False, name="c3b_fp32")],
                          ids=lambda c: c.name)
 def test_splat_ranges_and_pullpush_rows_equal_whole_passes(ctx, cfg):
