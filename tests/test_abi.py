@@ -124,3 +124,15 @@ def test_frame_host_sizes():
     assert z.points == cfg.n_vpl * sc.bucket_stride * 16
     assert z.radiance == cfg.width * cfg.height * 12
     assert z.gbuf_normal == cfg.width * cfg.height * 8
+
+
+def test_pullpush_form_selection():
+    """mlgi_pullpush_launches: one launch (each ISM's pyramid in one block) while the ISMs make at most
+    one wave of such blocks (152 SMs here, the GB300's count, as no GPU answers: three blocks a SM for
+    ISM edges up to 64, else two) and the far plane lies in [2^-20, 2^20]; else the per-level
+    launches, four per sequence (two for a single level), in two halves of the ISM rows."""
+    cases = [(mlgi.C0, 1), (mlgi.C1, 1), (mlgi.C2, 8), (mlgi.CREF, 8), (mlgi.C3B, 8),
+             (mlgi.C2.replace(z_far=3.0e6, name="c2_far"), 8), (mlgi.C1.replace(z_far=1.0e-7, name="c1_near"), 8),
+             (mlgi.C1.replace(levels=1, name="c1_one_level"), 4)]
+    for cfg, launches in cases:
+        assert mlgi.pullpush_launches(cfg) == launches, cfg.name
